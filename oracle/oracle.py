@@ -1,0 +1,138 @@
+"""ctypes binding of the CPU oracle (amie_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke`` and
+by the CPU-baseline leg of ``bench.py`` -- never by the GPU library.
+
+Functions take a ``MeshData`` (xfem-amie_gb300/amie_mesh.py) and numpy arrays
+and return numpy arrays.  Matrices use AMIE's padded column-major block layout
+(``row_size``, ``column_index``, ``array``) exactly as the reference's
+CoordinateIndexedSparseMatrix stores them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_port", "liboracle.so")
+
+_lib = None
+
+
+class _OracleMesh(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32), ("stride", C.c_int32), ("n_elem", C.c_uint32), ("ndofmax", C.c_uint32),
+        ("kind", C.c_void_p), ("dof_ptr", C.c_void_p), ("dof_ids", C.c_void_p), ("gp_ptr", C.c_void_p),
+        ("gp", C.c_void_p), ("jinv", C.c_void_p), ("moved", C.c_void_p), ("jinv_gp", C.c_void_p), ("mat", C.c_void_p), ("cmat_table", C.c_void_p),
+        ("cscale", C.c_void_p), ("scale", C.c_void_p), ("enr_ptr", C.c_void_p), ("enr_type", C.c_void_p),
+        ("enr_vertex", C.c_void_p), ("enr_data", C.c_void_p), ("enr_jump", C.c_void_p), ("enr_grad", C.c_void_p),
+    ]
+
+
+def build() -> str:
+    """Compile liboracle.so (make -C oracle port)."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = C.CDLL(LIB_PATH)
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _mesh_struct(m):
+    s = _OracleMesh(m.dim, m.stride, m.n_elem, m.ndofmax)
+    for name in ("kind", "dof_ptr", "dof_ids", "gp_ptr", "gp", "jinv", "moved", "jinv_gp", "mat", "cmat_table", "cscale", "scale",
+                 "enr_ptr", "enr_type", "enr_vertex", "enr_data", "enr_jump", "enr_grad"):
+        setattr(s, name, _p(getattr(m, name)))
+    return s
+
+
+def threads() -> int:
+    return int(lib().oracle_threads())
+
+
+def element_matrices(m):
+    off = m.ke_offsets()
+    ke = np.zeros(int(off[-1]), np.float64)
+    st = _mesh_struct(m)
+    rc = lib().oracle_element_matrices(C.byref(st), _p(off), _p(ke))
+    if rc != 0:
+        raise RuntimeError(f"oracle_element_matrices failed: {rc}")
+    return off, ke
+
+
+def pattern(m):
+    st = _mesh_struct(m)
+    nr = C.c_uint32()
+    nnz = C.c_uint64()
+    lib().oracle_pattern(C.byref(st), C.byref(nr), C.byref(nnz), None, None)
+    rs = np.zeros(nr.value, np.uint32)
+    ci = np.zeros(nnz.value, np.uint32)
+    lib().oracle_pattern(C.byref(st), C.byref(nr), C.byref(nnz), _p(rs), _p(ci))
+    return rs, ci
+
+
+def block_size(stride: int) -> int:
+    return stride * (stride + stride % 2)
+
+
+def scatter(m, off, ke, rs, ci):
+    arr = np.zeros(len(ci) * block_size(m.stride), np.float64)
+    st = _mesh_struct(m)
+    rc = lib().oracle_scatter(C.byref(st), _p(off), _p(ke), C.c_uint32(len(rs)), _p(rs), _p(ci), _p(arr))
+    if rc != 0:
+        raise RuntimeError(f"oracle_scatter failed: {rc}")
+    return arr
+
+
+def dirichlet(stride, rs, ci, arr, ids, values, kinds, rhs):
+    rc = lib().oracle_dirichlet(C.c_int32(stride), C.c_uint32(len(rs)), _p(rs), _p(ci), _p(arr),
+                                C.c_uint32(len(ids)), _p(ids), _p(values), _p(kinds), _p(rhs))
+    if rc != 0:
+        raise RuntimeError(f"oracle_dirichlet failed: {rc}")
+
+
+def spmv(stride, rs, ci, arr, x, y0=None):
+    y = np.zeros(len(rs) * stride, np.float64)
+    lib().oracle_spmv(C.c_int32(stride), C.c_uint32(len(rs)), _p(rs), _p(ci), _p(arr), _p(x), _p(y0), _p(y))
+    return y
+
+
+def cg_amie(stride, rs, ci, arr, b, x0=None, eps=1e-10, nssor=32, maxit=-1):
+    x = np.zeros(len(rs) * stride) if x0 is None else np.array(x0, np.float64, copy=True)
+    it = C.c_int64()
+    rc = lib().oracle_cg_amie(C.c_int32(stride), C.c_uint32(len(rs)), _p(rs), _p(ci), _p(arr), _p(b), _p(x),
+                              C.c_double(eps), C.c_int32(nssor), C.c_int64(maxit), C.byref(it))
+    return x, int(it.value), int(rc)
+
+
+def pcg(stride, rs, ci, arr, b, x0=None, rtol=1e-10, maxit=100000):
+    x = np.zeros(len(rs) * stride) if x0 is None else np.array(x0, np.float64, copy=True)
+    it = C.c_int64()
+    rr = C.c_double()
+    rc = lib().oracle_pcg(C.c_int32(stride), C.c_uint32(len(rs)), _p(rs), _p(ci), _p(arr), _p(b), _p(x),
+                          C.c_double(rtol), C.c_int64(maxit), C.byref(it), C.byref(rr))
+    return x, int(it.value), float(rr.value), int(rc)
+
+
+def assemble(m, bc_ids, bc_values, bc_kinds, rhs0=None):
+    """Full host pipeline: K_e -> pattern -> Kahan scatter -> Dirichlet."""
+    off, ke = element_matrices(m)
+    rs, ci = pattern(m)
+    arr = scatter(m, off, ke, rs, ci)
+    rhs = np.zeros(len(rs) * m.stride) if rhs0 is None else np.array(rhs0, np.float64, copy=True)
+    dirichlet(m.stride, rs, ci, arr, np.ascontiguousarray(bc_ids, np.uint32),
+              np.ascontiguousarray(bc_values, np.float64), np.ascontiguousarray(bc_kinds, np.uint8), rhs)
+    return dict(off=off, ke=ke, row_size=rs, column_index=ci, array=arr, rhs=rhs)
