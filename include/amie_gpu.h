@@ -1,0 +1,234 @@
+/* amie_gpu.h -- C-ABI of the GB300 (sm_103a) implementation of AMIE's
+ * finite-element hot path:
+ *
+ *   element stiffness  K_e = sum_g w_g B_i^T C B_j   (incl. XFEM enrichment)
+ *   -> scatter into AMIE's block-sparse CoordinateIndexedSparseMatrix
+ *   -> Dirichlet elimination
+ *   -> Jacobi-preconditioned conjugate gradient (FP64, FP32-inner with FP64
+ *      iterative refinement, or AMIE's own ConjugateGradient semantics)
+ *
+ * plus a continuous-batching solve server.
+ *
+ * Plain C types only: host pointers unless a name ends in `_dev`.  Every call
+ * returns an amie_status.  The library owns all device memory it allocates;
+ * callers own every host array they pass (arrays are read during the call
+ * only).  Calls on one handle must not overlap; distinct handles may be driven
+ * from distinct host threads.
+ *
+ * Reference interfaces (paths relative to the AMIE source tree) are cited at
+ * each entry point.
+ */
+#ifndef AMIE_GPU_H
+#define AMIE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMIE_GPU_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define AMIE_API __attribute__((visibility("default")))
+#else
+#define AMIE_API
+#endif
+
+typedef enum amie_status {
+    AMIE_OK = 0,
+    AMIE_NOT_CONVERGED = 1,   /* ConjugateGradient::solve returned false (solvers/conjugategradient.cpp:316) */
+    AMIE_NAN = 2,             /* NaN residual; the reference exit(0)s (solvers/conjugategradient.cpp:160-165) */
+    AMIE_OOM = 3,             /* device allocation failed or would exceed the configured HBM budget */
+    AMIE_BAD_INPUT = 4,       /* malformed arrays (ids out of range, counts inconsistent, ...) */
+    AMIE_TIMEOUT = 5,         /* a bounded device wait or a server deadline ran out */
+    AMIE_CUDA_ERROR = 6,      /* a CUDA runtime call failed; see amie_last_error() */
+    AMIE_NOT_READY = 7,       /* amie_poll: the request is still running */
+    AMIE_CANCELLED = 8        /* amie_poll: the request was cancelled */
+} amie_status;
+
+/* Element kinds (TriElement LINEAR / QUADRATIC, TetrahedralElement LINEAR). */
+enum { AMIE_TRI3 = 1, AMIE_TRI6 = 2, AMIE_TET4 = 3 };
+/* Enrichment function kinds. */
+enum { AMIE_ENR_TABULATED = 0, AMIE_ENR_HEAVISIDE = 1 };
+/* Multiplier kinds: displacement (SET_ALONG_* / FIX_ALONG_*, eliminated) or
+ * nodal force (SET_FORCE_*, added to the right-hand side). */
+enum { AMIE_BC_DISPLACEMENT = 0, AMIE_BC_FORCE = 1 };
+/* Solver algorithms. */
+enum {
+    AMIE_SOLVER_PCG_FP64 = 0,   /* Jacobi-PCG, FP64 throughout, stop ||b-Ax|| <= rtol ||b|| */
+    AMIE_SOLVER_PCG_MIXED = 1,  /* FP32 SpMV/preconditioner/direction updates inside an FP64
+                                   iterative-refinement loop (FP64 residual, dots of the outer
+                                   loop and solution accumulation) */
+    AMIE_SOLVER_AMIE_CG = 2     /* ConjugateGradient::solve semantics: Jacobi smoothing,
+                                   absolute stop sqrt(r.D^-1 r) < max(1e-12, eps), restarts */
+};
+
+typedef struct amie_ctx amie_ctx;
+typedef struct amie_topo amie_topo;
+typedef struct amie_server amie_server;
+
+typedef struct amie_config {
+    int32_t device;            /* CUDA device ordinal */
+    uint64_t hbm_budget_bytes; /* 0 = no limit besides free memory */
+    int32_t verbose;
+} amie_config;
+
+/* Element data of one mesh, as held by Assembly after FeatureTree::assemble
+ * (features/features.cpp:3337-3408).  n_elem elements in Assembly::element2d /
+ * element3d order, which is the order the reference scatters in
+ * (solvers/assembly.cpp:657). */
+typedef struct amie_mesh {
+    int32_t dim;                 /* 2 or 3 */
+    int32_t stride;              /* DOF per node: equals dim (elasticity) */
+    uint32_t n_elem;
+    uint32_t ndofmax;            /* Assembly::setMaxDof (solvers/assembly.h:286); 0 = max id + 1 */
+    const uint8_t *kind;         /* [n_elem] AMIE_TRI3 / AMIE_TRI6 / AMIE_TET4 */
+    const uint32_t *dof_ptr;     /* [n_elem+1] */
+    const uint32_t *dof_ids;     /* getDofIds (elements/elements.cpp:204): node ids, then enrichment ids */
+    const uint32_t *gp_ptr;      /* [n_elem+1]; an element with 0 points uses its kind's default rule */
+    const double *gp;            /* (dim+1) per point: local coordinates, weight * det J */
+    const double *jinv;          /* [n_elem*dim*dim] inverse Jacobian at the centroid, row-major */
+    const uint8_t *moved;        /* [n_elem] or NULL: 1 = inverse Jacobian per Gauss point */
+    const double *jinv_gp;       /* [n_gp*dim*dim], read for moved elements only */
+    const uint32_t *mat;         /* [n_elem] row of cmat_table */
+    const double *cmat_table;    /* [n_mat*nv*nv], nv = 3 (2D) or 6 (3D): Form::param */
+    uint32_t n_mat;
+    const double *cscale;        /* [n_elem] or NULL: factor on C ((1-d) damage, per-element modulus) */
+    const double *scale;         /* [n_elem] or NULL: Assembly::add scale (solvers/assembly.cpp:106) */
+    const uint32_t *enr_ptr;     /* [n_elem+1] or NULL: enrichment functions of element e */
+    const uint8_t *enr_type;     /* [n_enr] AMIE_ENR_* */
+    const uint8_t *enr_vertex;   /* [n_enr] P1 vertex (0,1,2) of a Heaviside function */
+    const uint32_t *enr_data;    /* [n_enr] first per-GP entry of the function */
+    uint64_t n_enr_gp;           /* entries of enr_jump / enr_grad (per dim) */
+    const int8_t *enr_jump;      /* Heaviside: H(x_g) - H(x_k), per (function, GP) */
+    const double *enr_grad;      /* Tabulated: local gradient, dim per (function, GP) */
+} amie_mesh;
+
+typedef struct amie_solve_opts {
+    int32_t solver;              /* AMIE_SOLVER_* */
+    double rtol;                 /* relative residual target (PCG solvers); default 1e-10 */
+    double eps;                  /* AMIE_CG absolute tolerance (Assembly::setEpsilon); default 1e-10 */
+    int32_t nssor;               /* AMIE_CG smoothing sweeps (Assembly::setSSORIterations); default 32 */
+    int64_t maxit;               /* iteration cap; <= 0 = reference default n/2 (AMIE_CG) / 20 n (PCG) */
+    double inner_rtol;           /* MIXED: FP32 inner solve reduction per refinement step; default 1e-5 */
+    int32_t use_x0;              /* 1 = start from x_inout (Assembly::extrapolate warm start) */
+} amie_solve_opts;
+
+typedef struct amie_solve_stats {
+    int64_t iterations;          /* total (inner) CG iterations */
+    int32_t refinements;         /* MIXED: outer refinement steps */
+    int32_t status;              /* amie_status of the solve */
+    double relres;               /* final true relative residual ||b - A x|| / ||b|| */
+    double seconds;              /* wall time of the solve on the device */
+} amie_solve_stats;
+
+/* ------------------------------------------------------------------ context */
+AMIE_API amie_status amie_ctx_create(const amie_config *cfg, amie_ctx **out);
+AMIE_API amie_status amie_ctx_destroy(amie_ctx *ctx);
+AMIE_API const char *amie_last_error(void);
+AMIE_API int32_t amie_abi_version(void);
+
+/* ------------------------------------------------------------------ topology
+ * Uploads the element data and builds, on the device, the block sparsity
+ * pattern of Assembly::make_final (solvers/assembly.cpp:445-537: every
+ * (ids[j], ids[k]) pair, diagonal gap fill, (ndofmax-1, ndofmax-1)) and the
+ * scatter map that assembles without atomics.  The pattern is bit-exact with
+ * the reference's row_size / column_index. */
+AMIE_API amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh, amie_topo **out);
+AMIE_API amie_status amie_topology_destroy(amie_topo *topo);
+/* n_rows = block rows, nnzb = stored blocks, n = n_rows * stride scalar DOFs. */
+AMIE_API amie_status amie_topology_sizes(const amie_topo *topo, uint32_t *n_rows, uint64_t *nnzb, uint64_t *n);
+/* row_size [n_rows] and column_index [nnzb] of CoordinateIndexedSparseMatrix
+ * (sparse/sparse_matrix.h:129-179). */
+AMIE_API amie_status amie_topology_pattern(const amie_topo *topo, uint32_t *row_size, uint32_t *column_index);
+
+/* ------------------------------------------------------------------ assembly
+ * Element matrices (DelaunayTriangle::getElementaryMatrix, mesher/delaunay.cpp:2408;
+ * Stiffness::apply, physics/stiffness.cpp:43) and the Kahan-compensated
+ * element-order scatter of Assembly::make_final (solvers/assembly.cpp:657-803)
+ * into the device-resident block matrix.  Clears any previous Dirichlet
+ * elimination and right-hand side. */
+AMIE_API amie_status amie_assemble(amie_topo *topo);
+/* Re-integrate with new per-element factors on C (damage step:
+ * StiffnessAndFracture::apply, physics/stiffness_and_fracture.cpp:75-79). */
+AMIE_API amie_status amie_set_cscale(amie_topo *topo, const double *cscale);
+/* Element matrices as dense (nf*s)^2 row-major blocks, element after element. */
+AMIE_API amie_status amie_element_matrices(const amie_topo *topo, double *ke, uint64_t capacity);
+
+/* Dirichlet elimination of Assembly::setBoundaryConditions
+ * (solvers/assembly.cpp:125-283) for multipliers set by Assembly::setPointAlong
+ * (solvers/assembly.cpp:1590) or SET_FORCE_*.  rhs0: initial force vector
+ * [n] or NULL (zero). */
+AMIE_API amie_status amie_apply_dirichlet(amie_topo *topo, uint32_t n_bc, const uint32_t *ids, const double *values,
+                                 const uint8_t *kinds, const double *rhs0);
+
+/* Matrix and right-hand side in AMIE's own layout (CoordinateIndexedSparseMatrix::array,
+ * blocks column-major with even-padded columns, sparse/sparse_vector.cpp:50-58):
+ * array [nnzb * s * (s + s%2)], rhs [n] (Assembly::getForces, solvers/assembly.h:343). */
+AMIE_API amie_status amie_matrix_download(const amie_topo *topo, double *array, double *rhs);
+
+/* y = A x on the device-resident matrix (CoordinateIndexedSparseMatrix::operator*,
+ * sparse/sparse_matrix.cpp:505-547).  Host x, y of length n. */
+AMIE_API amie_status amie_spmv(amie_topo *topo, const double *x, double *y);
+
+/* ------------------------------------------------------------------ solve
+ * Assembly::cgsolve (solvers/assembly.cpp:1829-1953) after make_final: solves
+ * A x = rhs on the device.  x_inout [n] (host): warm start in (if use_x0),
+ * solution out (Assembly::getDisplacements, solvers/assembly.h:349). */
+AMIE_API amie_status amie_solve(amie_topo *topo, const amie_solve_opts *opts, double *x_inout, amie_solve_stats *stats);
+/* Same, with the right-hand side and the solution left on the device (no host
+ * copies); read the solution with amie_solution_download. */
+AMIE_API amie_status amie_solve_resident(amie_topo *topo, const amie_solve_opts *opts, amie_solve_stats *stats);
+AMIE_API amie_status amie_solution_download(const amie_topo *topo, double *x);
+
+/* ------------------------------------------------------------------ serving
+ * Continuous-batching solve server: independent meshes (microstructure or
+ * damage-step solves) are admitted while others run, as free HBM allows; all
+ * admitted solves advance together in one batched PCG iteration captured in a
+ * CUDA graph. */
+typedef struct amie_server_config {
+    int32_t solver;              /* AMIE_SOLVER_PCG_FP64 or AMIE_SOLVER_PCG_MIXED */
+    double rtol;                 /* per request relative residual target */
+    uint64_t hbm_budget_bytes;   /* admission limit; 0 = 90% of free memory */
+    int32_t max_slots;           /* concurrent solves; 0 = 256 */
+    int32_t iters_per_launch;    /* PCG iterations per graph launch; 0 = 16 */
+} amie_server_config;
+
+typedef struct amie_request {
+    const amie_mesh *mesh;       /* copied at submit */
+    uint32_t n_bc;
+    const uint32_t *bc_ids;
+    const double *bc_values;
+    const uint8_t *bc_kinds;
+    const double *x0;            /* warm start [n] or NULL */
+} amie_request;
+
+typedef struct amie_result {
+    int32_t status;              /* amie_status */
+    int64_t iterations;
+    double relres;
+    double latency_s;            /* submit -> completion */
+    double queue_s;              /* submit -> admission */
+    uint64_t n;                  /* scalar DOFs */
+} amie_result;
+
+AMIE_API amie_status amie_server_start(amie_ctx *ctx, const amie_server_config *cfg, amie_server **out);
+/* Copies the request; returns a ticket. */
+AMIE_API amie_status amie_submit(amie_server *srv, const amie_request *req, uint64_t *ticket);
+/* AMIE_NOT_READY while running; on completion fills res and, if x != NULL,
+ * copies the solution [n]. */
+AMIE_API amie_status amie_poll(amie_server *srv, uint64_t ticket, amie_result *res, double *x);
+AMIE_API amie_status amie_cancel(amie_server *srv, uint64_t ticket);
+/* Runs the server loop until every submitted request is finished or timeout_s elapses. */
+AMIE_API amie_status amie_server_drain(amie_server *srv, double timeout_s);
+AMIE_API amie_status amie_server_stop(amie_server *srv);
+
+/* Number of kernels this library has launched (process-wide counter). */
+AMIE_API uint64_t amie_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,356 @@
+"""ctypes binding of libamie_gpu.so (include/amie_gpu.h) and a host-side
+mirror of AMIE's ``Assembly`` for the element-stiffness -> scatter -> CG path.
+
+``Assembly`` keeps the reference's method names and meaning
+(solvers/assembly.h:228-450): elements are added, Dirichlet multipliers set with
+``setPointAlong``, ``cgsolve`` solves, ``getMatrix`` / ``getForces`` /
+``getDisplacements`` return the results.  Everything runs on the GPU through the
+C-ABI; there is no CPU fallback: loading fails loudly if the library or a GPU is
+missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+import amie_mesh as am
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libamie_gpu.so")
+
+AMIE_OK, AMIE_NOT_CONVERGED, AMIE_NAN, AMIE_OOM, AMIE_BAD_INPUT, AMIE_TIMEOUT, AMIE_CUDA_ERROR, \
+    AMIE_NOT_READY, AMIE_CANCELLED = range(9)
+STATUS_NAMES = ["OK", "NOT_CONVERGED", "NAN", "OOM", "BAD_INPUT", "TIMEOUT", "CUDA_ERROR", "NOT_READY",
+                "CANCELLED"]
+SOLVER_PCG_FP64, SOLVER_PCG_MIXED, SOLVER_AMIE_CG = 0, 1, 2
+
+EXPORTED = [
+    "amie_ctx_create", "amie_ctx_destroy", "amie_last_error", "amie_abi_version", "amie_topology_build",
+    "amie_topology_destroy", "amie_topology_sizes", "amie_topology_pattern", "amie_assemble", "amie_set_cscale",
+    "amie_element_matrices", "amie_apply_dirichlet", "amie_matrix_download", "amie_spmv", "amie_solve",
+    "amie_solve_resident", "amie_solution_download", "amie_server_start", "amie_submit", "amie_poll",
+    "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches",
+]
+
+
+class AmieError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        name = STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else str(status)
+        super().__init__(f"{where}: {name} {detail}".strip())
+
+
+class _Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("hbm_budget_bytes", C.c_uint64), ("verbose", C.c_int32)]
+
+
+class _Mesh(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int32), ("stride", C.c_int32), ("n_elem", C.c_uint32), ("ndofmax", C.c_uint32),
+        ("kind", C.c_void_p), ("dof_ptr", C.c_void_p), ("dof_ids", C.c_void_p), ("gp_ptr", C.c_void_p),
+        ("gp", C.c_void_p), ("jinv", C.c_void_p), ("moved", C.c_void_p), ("jinv_gp", C.c_void_p),
+        ("mat", C.c_void_p), ("cmat_table", C.c_void_p), ("n_mat", C.c_uint32), ("cscale", C.c_void_p),
+        ("scale", C.c_void_p), ("enr_ptr", C.c_void_p), ("enr_type", C.c_void_p), ("enr_vertex", C.c_void_p),
+        ("enr_data", C.c_void_p), ("n_enr_gp", C.c_uint64), ("enr_jump", C.c_void_p), ("enr_grad", C.c_void_p),
+    ]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("solver", C.c_int32), ("rtol", C.c_double), ("eps", C.c_double), ("nssor", C.c_int32),
+                ("maxit", C.c_int64), ("inner_rtol", C.c_double), ("use_x0", C.c_int32)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int64), ("refinements", C.c_int32), ("status", C.c_int32),
+                ("relres", C.c_double), ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("solver", C.c_int32), ("rtol", C.c_double), ("hbm_budget_bytes", C.c_uint64),
+                ("max_slots", C.c_int32), ("iters_per_launch", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("mesh", C.c_void_p), ("n_bc", C.c_uint32), ("bc_ids", C.c_void_p), ("bc_values", C.c_void_p),
+                ("bc_kinds", C.c_void_p), ("x0", C.c_void_p)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_int64), ("relres", C.c_double),
+                ("latency_s", C.c_double), ("queue_s", C.c_double), ("n", C.c_uint64)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libamie_gpu.so (build it first with build.py / __graft_entry__.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run `python xfem-amie_gb300/build.py` first")
+        L = C.CDLL(LIB_PATH)
+        L.amie_last_error.restype = C.c_char_p
+        L.amie_kernel_launches.restype = C.c_uint64
+        for name in EXPORTED:
+            if name not in ("amie_last_error", "amie_kernel_launches", "amie_abi_version"):
+                getattr(L, name).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def check(rc: int, where: str, ok=(AMIE_OK,)):
+    if rc not in ok:
+        raise AmieError(rc, where, lib().amie_last_error().decode(errors="replace"))
+    return rc
+
+
+def kernel_launches() -> int:
+    return int(lib().amie_kernel_launches())
+
+
+def mesh_struct(m: am.MeshData):
+    """ctypes amie_mesh over the arrays of a MeshData (which must outlive it)."""
+    s = _Mesh(m.dim, m.stride, m.n_elem, m.ndofmax)
+    for name in ("kind", "dof_ptr", "dof_ids", "gp_ptr", "gp", "jinv", "moved", "jinv_gp", "mat", "cmat_table",
+                 "cscale", "scale", "enr_ptr", "enr_type", "enr_vertex", "enr_data", "enr_jump", "enr_grad"):
+        setattr(s, name, _p(getattr(m, name)))
+    s.n_mat = len(m.cmat_table) // (m.nv * m.nv)
+    s.n_enr_gp = len(m.enr_jump) if len(m.enr_jump) else (len(m.enr_grad) // m.dim)
+    if len(m.enr_grad) // m.dim > s.n_enr_gp:
+        s.n_enr_gp = len(m.enr_grad) // m.dim
+    if m.enr_ptr is not None and int(m.enr_ptr[-1]) == 0:
+        s.enr_ptr = None
+    return s
+
+
+class Context:
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, verbose: int = 0):
+        self.ptr = C.c_void_p()
+        check(lib().amie_ctx_create(C.byref(_Config(device, hbm_budget_bytes, verbose)), C.byref(self.ptr)),
+              "amie_ctx_create")
+
+    def close(self):
+        if self.ptr:
+            lib().amie_ctx_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Topology:
+    """Device-resident mesh: element data, pattern, scatter map, matrix, vectors."""
+
+    def __init__(self, ctx: Context, m: am.MeshData):
+        self.ctx = ctx
+        self.mesh = m
+        self._ms = mesh_struct(m)
+        self.ptr = C.c_void_p()
+        check(lib().amie_topology_build(ctx.ptr, C.byref(self._ms), C.byref(self.ptr)), "amie_topology_build")
+        nr, nz, n = C.c_uint32(), C.c_uint64(), C.c_uint64()
+        lib().amie_topology_sizes(self.ptr, C.byref(nr), C.byref(nz), C.byref(n))
+        self.n_rows, self.nnzb, self.n = nr.value, nz.value, n.value
+
+    def close(self):
+        if self.ptr:
+            lib().amie_topology_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pattern(self):
+        rs = np.zeros(self.n_rows, np.uint32)
+        ci = np.zeros(self.nnzb, np.uint32)
+        check(lib().amie_topology_pattern(self.ptr, _p(rs), _p(ci)), "amie_topology_pattern")
+        return rs, ci
+
+    def assemble(self):
+        check(lib().amie_assemble(self.ptr), "amie_assemble")
+
+    def set_cscale(self, cscale):
+        cs = np.ascontiguousarray(cscale, np.float64)
+        check(lib().amie_set_cscale(self.ptr, _p(cs)), "amie_set_cscale")
+
+    def element_matrices(self):
+        off = self.mesh.ke_offsets()
+        ke = np.zeros(int(off[-1]), np.float64)
+        check(lib().amie_element_matrices(self.ptr, _p(ke), C.c_uint64(len(ke))), "amie_element_matrices")
+        return off, ke
+
+    def apply_dirichlet(self, ids, values, kinds=None, rhs0=None):
+        ids = np.ascontiguousarray(ids, np.uint32)
+        values = np.ascontiguousarray(values, np.float64)
+        kinds = None if kinds is None else np.ascontiguousarray(kinds, np.uint8)
+        rhs0 = None if rhs0 is None else np.ascontiguousarray(rhs0, np.float64)
+        check(lib().amie_apply_dirichlet(self.ptr, C.c_uint32(len(ids)), _p(ids), _p(values), _p(kinds), _p(rhs0)),
+              "amie_apply_dirichlet")
+
+    def matrix(self):
+        """(array in AMIE's padded column-major block layout, rhs)."""
+        s = self.mesh.stride
+        arr = np.zeros(self.nnzb * s * (s + s % 2), np.float64)
+        rhs = np.zeros(self.n, np.float64)
+        check(lib().amie_matrix_download(self.ptr, _p(arr), _p(rhs)), "amie_matrix_download")
+        return arr, rhs
+
+    def spmv(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.n, np.float64)
+        check(lib().amie_spmv(self.ptr, _p(x), _p(y)), "amie_spmv")
+        return y
+
+    def solve(self, solver=SOLVER_PCG_FP64, rtol=1e-10, x0=None, maxit=0, eps=1e-10, nssor=32,
+              inner_rtol=1e-5, accept=(AMIE_OK,)):
+        x = np.zeros(self.n, np.float64) if x0 is None else np.array(x0, np.float64, copy=True)
+        opts = SolveOpts(solver, rtol, eps, nssor, maxit, inner_rtol, 1 if x0 is not None else 0)
+        st = SolveStats()
+        rc = lib().amie_solve(self.ptr, C.byref(opts), _p(x), C.byref(st))
+        check(rc, "amie_solve", ok=accept)
+        return x, st.as_dict()
+
+    def solve_resident(self, solver=SOLVER_PCG_FP64, rtol=1e-10, maxit=0, inner_rtol=1e-5, use_x0=False,
+                       accept=(AMIE_OK,)):
+        opts = SolveOpts(solver, rtol, 1e-10, 32, maxit, inner_rtol, 1 if use_x0 else 0)
+        st = SolveStats()
+        rc = lib().amie_solve_resident(self.ptr, C.byref(opts), C.byref(st))
+        check(rc, "amie_solve_resident", ok=accept)
+        return st.as_dict()
+
+    def solution(self):
+        x = np.zeros(self.n, np.float64)
+        check(lib().amie_solution_download(self.ptr, _p(x)), "amie_solution_download")
+        return x
+
+
+class Assembly:
+    """Mirror of AMIE's ``Assembly`` (solvers/assembly.h:228-450) on the GPU path.
+
+    Elements arrive as a ``MeshData`` batch (``add``), Dirichlet multipliers
+    through ``setPointAlong`` / ``fixPoint``, nodal forces through
+    ``setForceOn``; ``cgsolve`` runs make_final (pattern, scatter, elimination)
+    and the solve, and keeps the displacement history used by ``extrapolate``
+    (solvers/assembly.cpp:1772-1814) as the next warm start.
+    """
+
+    XI, ETA, ZETA = 0, 1, 2
+
+    def __init__(self, ctx: Optional[Context] = None):
+        self.ctx = ctx or Context()
+        self.mesh: Optional[am.MeshData] = None
+        self.topo: Optional[Topology] = None
+        self.multipliers = {}        # dof id -> (value, kind)
+        self.epsilon = 1e-10
+        self.nssor = 32
+        self.solver = SOLVER_PCG_FP64
+        self.rtol = 1e-10
+        self.ndofmax = 0
+        self.displacements = np.zeros(0)
+        self.history = []
+        self.last_stats = {}
+        self._dirty_topology = True
+
+    # element side ------------------------------------------------------
+    def add(self, mesh: am.MeshData):
+        self.mesh = mesh
+        self._dirty_topology = True
+
+    def setMaxDof(self, n: int):
+        self.ndofmax = n
+
+    def setEpsilon(self, e: float):
+        self.epsilon = e
+
+    def setSSORIterations(self, n: int):
+        self.nssor = n
+
+    def setSolver(self, solver: int, rtol: float = 1e-10):
+        self.solver = solver
+        self.rtol = rtol
+
+    def setCScale(self, cscale):
+        """New per-element factor on C (damage step), keeps the topology."""
+        self.mesh.cscale = np.ascontiguousarray(cscale, np.float64)
+        if self.topo is not None:
+            self.topo.set_cscale(self.mesh.cscale)
+
+    # multipliers -------------------------------------------------------
+    def setPointAlong(self, axis: int, value: float, node_id: int):
+        self.multipliers[node_id * self.mesh.stride + axis] = (float(value), am.BC_DISPLACEMENT)
+
+    def fixPoint(self, node_id: int, axis: int):
+        self.setPointAlong(axis, 0.0, node_id)
+
+    def setForceOn(self, axis: int, value: float, node_id: int):
+        key = node_id * self.mesh.stride + axis
+        old = self.multipliers.get(key, (0.0, am.BC_FORCE))
+        self.multipliers[key] = (old[0] + float(value), am.BC_FORCE)
+
+    def setMultipliers(self, ids, values, kinds=None):
+        kinds = np.zeros(len(ids), np.uint8) if kinds is None else kinds
+        for i, v, k in zip(ids, values, kinds):
+            self.multipliers[int(i)] = (float(v), int(k))
+
+    def clear(self):
+        self.multipliers.clear()
+        self.topo = None
+        self.history.clear()
+
+    # solve -------------------------------------------------------------
+    def make_final(self):
+        if self.topo is None or self._dirty_topology:
+            if self.ndofmax:
+                self.mesh.ndofmax = self.ndofmax
+            self.topo = Topology(self.ctx, self.mesh)
+            self._dirty_topology = False
+        self.topo.assemble()
+        ids = np.array(sorted(self.multipliers), np.uint32)
+        vals = np.array([self.multipliers[i][0] for i in ids], np.float64)
+        kinds = np.array([self.multipliers[i][1] for i in ids], np.uint8)
+        self.topo.apply_dirichlet(ids, vals, kinds)
+
+    def extrapolate(self):
+        if len(self.history) < 2:
+            return self.displacements if len(self.displacements) else None
+        a, b = self.history[-2], self.history[-1]
+        return b + (b - a)
+
+    def cgsolve(self, maxit: int = -1) -> bool:
+        self.make_final()
+        x0 = self.extrapolate()
+        if x0 is not None and len(x0) != self.topo.n:
+            x0 = None
+        x, st = self.topo.solve(self.solver, rtol=self.rtol, x0=x0, maxit=max(maxit, 0), eps=self.epsilon,
+                                nssor=self.nssor, accept=(AMIE_OK, AMIE_NOT_CONVERGED))
+        self.displacements = x
+        self.history = (self.history + [x])[-2:]
+        self.last_stats = st
+        return st["status"] == AMIE_OK
+
+    def getMatrix(self):
+        rs, ci = self.topo.pattern()
+        arr, _ = self.topo.matrix()
+        return rs, ci, arr
+
+    def getForces(self):
+        return self.topo.matrix()[1]
+
+    def getDisplacements(self):
+        return self.displacements

@@ -1,0 +1,1000 @@
+// assemble.cu -- topology (pattern + scatter map), element stiffness
+// quadrature, atomic-free gather assembly and Dirichlet elimination.
+//
+// Reference path (paths relative to the AMIE source tree):
+//   pattern     Assembly::make_final            solvers/assembly.cpp:445-537
+//   K_e         DelaunayTriangle::getElementaryMatrix  mesher/delaunay.cpp:2408-2535
+//               Stiffness::apply                physics/stiffness.cpp:43-48
+//               VirtualMachine::ieval / geval   polynomial/vm_base.cpp:2974-2989, 2156-2298
+//   scatter     Assembly::make_final            solvers/assembly.cpp:657-803 (Kahan)
+//   Dirichlet   Assembly::setBoundaryConditions solvers/assembly.cpp:125-283
+#include "internal.h"
+
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+
+namespace amie {
+
+// ------------------------------------------------------------------ helpers
+
+__host__ __device__ inline int nshape_of(int kind) { return kind == AMIE_TRI3 ? 3 : kind == AMIE_TRI6 ? 6 : kind == AMIE_TET4 ? 4 : 0; }
+
+// Local gradients of the shape functions of TriElement LINEAR / QUADRATIC
+// (elements/elements.cpp:976-1060) and TetrahedralElement LINEAR
+// (elements/elements.cpp:2496-2530); x = xi, y = eta.
+__device__ inline void shape_grad(int kind, int f, double x, double y, double g[3])
+{
+    g[2] = 0.0;
+    if (kind == AMIE_TRI3) {
+        const double gx[3] = {0.0, -1.0, 1.0}, gy[3] = {1.0, -1.0, 0.0};
+        g[0] = gx[f]; g[1] = gy[f];
+    } else if (kind == AMIE_TRI6) {
+        switch (f) {
+        case 0: g[0] = 0.0; g[1] = 4.0 * y - 1.0; break;
+        case 1: g[0] = -4.0 * y; g[1] = 4.0 - 4.0 * x - 8.0 * y; break;
+        case 2: g[0] = 4.0 * y + 4.0 * x - 3.0; g[1] = 4.0 * x + 4.0 * y - 3.0; break;
+        case 3: g[0] = 4.0 - 8.0 * x - 4.0 * y; g[1] = -4.0 * x; break;
+        case 4: g[0] = 4.0 * x - 1.0; g[1] = 0.0; break;
+        default: g[0] = 4.0 * y; g[1] = 4.0 * x; break;
+        }
+    } else {
+        const double gx[4] = {0.0, -1.0, 1.0, 0.0}, gy[4] = {0.0, -1.0, 0.0, 1.0}, gz[4] = {1.0, -1.0, 0.0, 0.0};
+        g[0] = gx[f]; g[1] = gy[f]; g[2] = gz[f];
+    }
+}
+
+// Default Gauss rules (elements/elements.cpp:666-697, 2397-2400), with the
+// reference's literal coordinates and weights.
+__device__ inline int default_rule(int kind, int g, double p[3], double *w)
+{
+    p[2] = 0.0;
+    if (kind == AMIE_TRI3) {
+        p[0] = p[1] = 0.333333333333333; *w = 0.5;
+        return 1;
+    }
+    if (kind == AMIE_TRI6) {
+        const double px[4] = {0.2, 0.6, 0.2, 0.33333333333333}, py[4] = {0.2, 0.2, 0.6, 0.33333333333333};
+        const double pw[4] = {0.260416666666667, 0.260416666666667, 0.260416666666667, -0.28125};
+        p[0] = px[g]; p[1] = py[g]; *w = pw[g];
+        return 4;
+    }
+    p[0] = p[1] = p[2] = 0.25; *w = 0.1666666666666667;
+    return 1;
+}
+
+template <int DIM>
+__device__ inline double det_small(const double *J)
+{
+    if (DIM == 2) return J[0] * J[3] - J[1] * J[2];
+    return J[0] * (J[4] * J[8] - J[5] * J[7]) - J[1] * (J[3] * J[8] - J[5] * J[6]) + J[2] * (J[3] * J[7] - J[4] * J[6]);
+}
+
+// Physical gradient d_r = sum_c g_c Jinv[r][c] (polynomial/vm_base.cpp:2251-2252).
+template <int DIM>
+__device__ inline void phys_grad(const double *J, const double *g, double *d)
+{
+#pragma unroll
+    for (int r = 0; r < DIM; r++) {
+        double a = 0.0;
+#pragma unroll
+        for (int c = 0; c < DIM; c++) a += g[c] * J[r * DIM + c];
+        d[r] = a;
+    }
+}
+
+// Contribution w * B_i C B_j^T (s x s) for the Voigt B of geval
+// (polynomial/vm_base.cpp:2244-2255 in 2D, 2278-2296 in 3D).
+template <int DIM>
+__device__ inline void bcb(const double *di, const double *dj, const double *C, double w, double *out)
+{
+    constexpr int NV = DIM == 2 ? 3 : 6;
+    double Bi[DIM][NV], Bj[DIM][NV];
+#pragma unroll
+    for (int r = 0; r < DIM; r++)
+#pragma unroll
+        for (int k = 0; k < NV; k++) { Bi[r][k] = 0.0; Bj[r][k] = 0.0; }
+    if (DIM == 2) {
+        Bi[0][0] = di[0]; Bi[0][2] = di[1]; Bi[1][1] = di[1]; Bi[1][2] = di[0];
+        Bj[0][0] = dj[0]; Bj[0][2] = dj[1]; Bj[1][1] = dj[1]; Bj[1][2] = dj[0];
+    } else {
+        Bi[0][0] = di[0]; Bi[0][4] = di[2]; Bi[0][5] = di[1];
+        Bi[1][1] = di[1]; Bi[1][3] = di[2]; Bi[1][5] = di[0];
+        Bi[2][2] = di[2]; Bi[2][3] = di[1]; Bi[2][4] = di[0];
+        Bj[0][0] = dj[0]; Bj[0][4] = dj[2]; Bj[0][5] = dj[1];
+        Bj[1][1] = dj[1]; Bj[1][3] = dj[2]; Bj[1][5] = dj[0];
+        Bj[2][2] = dj[2]; Bj[2][3] = dj[1]; Bj[2][4] = dj[0];
+    }
+#pragma unroll
+    for (int r = 0; r < DIM; r++) {
+        double BiC[NV];
+#pragma unroll
+        for (int l = 0; l < NV; l++) {
+            double a = 0.0;
+#pragma unroll
+            for (int k = 0; k < NV; k++) a += Bi[r][k] * C[k * NV + l];
+            BiC[l] = a;
+        }
+#pragma unroll
+        for (int c = 0; c < DIM; c++) {
+            double a = 0.0;
+#pragma unroll
+            for (int l = 0; l < NV; l++) a += BiC[l] * Bj[c][l];
+            out[r * DIM + c] += w * a;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ kernels
+
+// Thread per unenriched element: loops over lower block pairs (i >= j), and
+// for each pair over the Gauss points; writes block (i,j) and its transpose
+// (j,i), as the reference does (mesher/delaunay.cpp:2462-2467).
+template <int DIM>
+__global__ void __launch_bounds__(128) k_quad_simple(MeshView m, const uint32_t *list, uint32_t count)
+{
+    constexpr int NV = DIM == 2 ? 3 : 6;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const uint32_t e = list[t];
+    const int kind = m.kind[e];
+    const int nf = nshape_of(kind);
+    double C[NV * NV];
+    const double cs = m.cscale ? m.cscale[e] : 1.0;
+    const double *Ct = m.cmat_table + (size_t)m.mat[e] * NV * NV;
+#pragma unroll
+    for (int i = 0; i < NV * NV; i++) C[i] = cs * Ct[i];
+    double Je[DIM * DIM];
+#pragma unroll
+    for (int i = 0; i < DIM * DIM; i++) Je[i] = m.jinv[(size_t)e * DIM * DIM + i];
+    const uint32_t g0 = m.gp_ptr[e], g1 = m.gp_ptr[e + 1];
+    const bool explicit_gp = g1 > g0;
+    const bool moved = explicit_gp && m.moved && m.moved[e];
+    const int ngp = explicit_gp ? (int)(g1 - g0) : (kind == AMIE_TRI6 ? 4 : 1);
+    const double inv_det = 1.0 / det_small<DIM>(Je);
+    double *K = m.ke + m.blk_off[e] * DIM * DIM;
+    for (int i = 0; i < nf; i++) {
+        for (int j = 0; j <= i; j++) {
+            double acc[DIM * DIM];
+#pragma unroll
+            for (int q = 0; q < DIM * DIM; q++) acc[q] = 0.0;
+            for (int g = 0; g < ngp; g++) {
+                double p[3], w;
+                if (explicit_gp) {
+                    const double *gp = m.gp + (size_t)(g0 + g) * (DIM + 1);
+                    p[0] = gp[0]; p[1] = gp[1]; p[2] = DIM == 3 ? gp[2] : 0.0;
+                    w = gp[DIM];
+                } else {
+                    default_rule(kind, g, p, &w);
+                    w *= inv_det;   // weight / det(J^-1) (elements/elements.cpp:939-945)
+                }
+                const double *J = moved ? m.jinv_gp + (size_t)(g0 + g) * DIM * DIM : Je;
+                double gi[3], gj[3], di[3], dj[3];
+                shape_grad(kind, i, p[0], p[1], gi);
+                shape_grad(kind, j, p[0], p[1], gj);
+                phys_grad<DIM>(J, gi, di);
+                phys_grad<DIM>(J, gj, dj);
+                bcb<DIM>(di, dj, C, w, acc);
+            }
+            double *Kij = K + (size_t)(i * nf + j) * DIM * DIM;
+            double *Kji = K + (size_t)(j * nf + i) * DIM * DIM;
+#pragma unroll
+            for (int r = 0; r < DIM; r++)
+#pragma unroll
+                for (int c = 0; c < DIM; c++) {
+                    Kij[r * DIM + c] = acc[r * DIM + c];
+                    if (i != j) Kji[c * DIM + r] = acc[r * DIM + c];
+                }
+        }
+    }
+}
+
+// Warp per enriched element (any number of functions <= kMaxFunctions and any
+// number of Gauss points).  Gauss points are processed in tiles: the lanes
+// first stage the physical gradients of every function at the tile's points
+// in shared memory, then each lane accumulates its own lower block pairs.
+template <int DIM>
+__global__ void __launch_bounds__(32) k_quad_warp(MeshView m, const uint32_t *list, uint32_t count)
+{
+    constexpr int NV = DIM == 2 ? 3 : 6;
+    constexpr int T = kMaxGpWarpTile;
+    constexpr int NPAIR = kMaxFunctions * (kMaxFunctions + 1) / 2;
+    __shared__ double sC[NV * NV];
+    __shared__ double sGrad[T][kMaxFunctions][DIM];
+    __shared__ double sW[T];
+    __shared__ double sAcc[NPAIR * DIM * DIM];
+    const uint32_t w = blockIdx.x;
+    if (w >= count) return;
+    const int lane = threadIdx.x;
+    const uint32_t e = list[w];
+    const int kind = m.kind[e];
+    const int nshape = nshape_of(kind);
+    const uint32_t f0 = m.enr_ptr[e], f1 = m.enr_ptr[e + 1];
+    const int nf = nshape + (int)(f1 - f0);
+    const int npair = nf * (nf + 1) / 2;
+    const double cs = m.cscale ? m.cscale[e] : 1.0;
+    for (int i = lane; i < NV * NV; i += 32) sC[i] = cs * m.cmat_table[(size_t)m.mat[e] * NV * NV + i];
+    for (int i = lane; i < npair * DIM * DIM; i += 32) sAcc[i] = 0.0;
+    double Je[DIM * DIM];
+#pragma unroll
+    for (int i = 0; i < DIM * DIM; i++) Je[i] = m.jinv[(size_t)e * DIM * DIM + i];
+    const uint32_t g0 = m.gp_ptr[e], g1 = m.gp_ptr[e + 1];
+    const bool explicit_gp = g1 > g0;
+    const bool moved = explicit_gp && m.moved && m.moved[e];
+    const int ngp = explicit_gp ? (int)(g1 - g0) : (kind == AMIE_TRI6 ? 4 : 1);
+    const double inv_det = 1.0 / det_small<DIM>(Je);
+    __syncwarp();
+    for (int t0 = 0; t0 < ngp; t0 += T) {
+        const int nt = min(T, ngp - t0);
+        for (int item = lane; item < nt * nf; item += 32) {
+            const int tg = item / nf, f = item % nf, g = t0 + tg;
+            double p[3], wt;
+            if (explicit_gp) {
+                const double *gp = m.gp + (size_t)(g0 + g) * (DIM + 1);
+                p[0] = gp[0]; p[1] = gp[1]; p[2] = DIM == 3 ? gp[2] : 0.0;
+                wt = gp[DIM];
+            } else {
+                default_rule(kind, g, p, &wt);
+                wt *= inv_det;
+            }
+            double lg[3] = {0.0, 0.0, 0.0};
+            if (f < nshape) {
+                shape_grad(kind, f, p[0], p[1], lg);
+            } else {
+                const uint32_t fj = f0 + (f - nshape);
+                const uint64_t off = (uint64_t)m.enr_data[fj] + g;
+                if (m.enr_type[fj] == AMIE_ENR_HEAVISIDE) {
+                    // grad(N_k^{P1} (H - H_k)) = grad N_k^{P1} * jump away from the crack
+                    // (features/crack.cpp:1316,1332,1347)
+                    const int v = m.enr_vertex[fj];
+                    const double jump = (double)m.enr_jump[off];
+                    const double gx[3] = {0.0, -1.0, 1.0}, gy[3] = {1.0, -1.0, 0.0};
+                    lg[0] = gx[v] * jump;
+                    lg[1] = gy[v] * jump;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < DIM; c++) lg[c] = m.enr_grad[off * DIM + c];
+                }
+            }
+            const double *J = moved ? m.jinv_gp + (size_t)(g0 + g) * DIM * DIM : Je;
+            double d[3];
+            phys_grad<DIM>(J, lg, d);
+#pragma unroll
+            for (int c = 0; c < DIM; c++) sGrad[tg][f][c] = d[c];
+            if (f == 0) sW[tg] = wt;
+        }
+        __syncwarp();
+        for (int pidx = lane; pidx < npair; pidx += 32) {
+            // pair index -> (i, j), i >= j, row-major lower triangle
+            int i = (int)((sqrt(8.0 * pidx + 1.0) - 1.0) * 0.5);
+            while ((i + 1) * (i + 2) / 2 <= pidx) i++;
+            while (i * (i + 1) / 2 > pidx) i--;
+            const int j = pidx - i * (i + 1) / 2;
+            double acc[DIM * DIM];
+#pragma unroll
+            for (int q = 0; q < DIM * DIM; q++) acc[q] = sAcc[pidx * DIM * DIM + q];
+            for (int tg = 0; tg < nt; tg++) bcb<DIM>(sGrad[tg][i], sGrad[tg][j], sC, sW[tg], acc);
+#pragma unroll
+            for (int q = 0; q < DIM * DIM; q++) sAcc[pidx * DIM * DIM + q] = acc[q];
+        }
+        __syncwarp();
+    }
+    double *K = m.ke + m.blk_off[e] * DIM * DIM;
+    for (int pidx = lane; pidx < npair; pidx += 32) {
+        int i = (int)((sqrt(8.0 * pidx + 1.0) - 1.0) * 0.5);
+        while ((i + 1) * (i + 2) / 2 <= pidx) i++;
+        while (i * (i + 1) / 2 > pidx) i--;
+        const int j = pidx - i * (i + 1) / 2;
+        double *Kij = K + (size_t)(i * nf + j) * DIM * DIM;
+        double *Kji = K + (size_t)(j * nf + i) * DIM * DIM;
+#pragma unroll
+        for (int r = 0; r < DIM; r++)
+#pragma unroll
+            for (int c = 0; c < DIM; c++) {
+                const double v = sAcc[pidx * DIM * DIM + r * DIM + c];
+                Kij[r * DIM + c] = v;
+                if (i != j) Kji[c * DIM + r] = v;
+            }
+    }
+}
+
+// Pattern keys: (row << 32 | col) for every (ids[j], ids[k]) of every element
+// (value = staged block index, so a stable sort keeps each slot's contributions
+// in element order) plus the diagonal gap fill and (ndofmax-1, ndofmax-1)
+// (value = no contribution).
+constexpr uint32_t kNoContribution = 0xffffffffu;
+
+__global__ void k_pattern_keys(uint32_t n_elem, const uint32_t *dof_ptr, const uint32_t *dof_ids,
+                               const uint64_t *blk_off, uint64_t *keys, uint32_t *vals)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_elem) return;
+    const uint32_t a = dof_ptr[e], nf = dof_ptr[e + 1] - a;
+    const uint64_t base = blk_off[e];
+    for (uint32_t j = 0; j < nf; j++) {
+        const uint64_t rj = (uint64_t)dof_ids[a + j] << 32;
+        for (uint32_t k = 0; k < nf; k++) {
+            keys[base + j * nf + k] = rj | dof_ids[a + k];
+            vals[base + j * nf + k] = (uint32_t)(base + j * nf + k);
+        }
+    }
+}
+
+__global__ void k_fill_keys(uint64_t offset, uint32_t n_diag, uint32_t last, uint64_t *keys, uint32_t *vals)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_diag) {
+        keys[offset + i] = ((uint64_t)i << 32) | i;
+        vals[offset + i] = kNoContribution;
+    } else if (i == n_diag) {
+        keys[offset + i] = ((uint64_t)last << 32) | last;
+        vals[offset + i] = kNoContribution;
+    }
+}
+
+__global__ void k_unique_flags(uint64_t n, const uint64_t *keys, const uint32_t *vals, uint32_t *is_new,
+                               uint32_t *is_contrib)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    is_new[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+    is_contrib[i] = vals[i] != kNoContribution ? 1u : 0u;
+}
+
+__global__ void k_pattern_emit(uint64_t n, const uint64_t *keys, const uint32_t *vals, const uint32_t *is_new,
+                               const uint32_t *slot_scan, const uint32_t *contrib_scan, uint32_t *col,
+                               uint32_t *row_count, uint64_t *map_ptr, uint32_t *map)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (is_new[i]) {
+        const uint32_t slot = slot_scan[i];
+        col[slot] = (uint32_t)(keys[i] & 0xffffffffu);
+        atomicAdd(&row_count[keys[i] >> 32], 1u);
+        map_ptr[slot] = contrib_scan[i];
+    }
+    if (vals[i] != kNoContribution) map[contrib_scan[i]] = vals[i];
+}
+
+__global__ void k_diag_pos(uint32_t n_rows, const uint32_t *row_ptr, const uint32_t *col, uint32_t *diag_pos)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_rows) return;
+    uint32_t lo = row_ptr[k], hi = row_ptr[k + 1];
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (col[mid] < k) lo = mid + 1; else hi = mid;
+    }
+    diag_pos[k] = lo;   // the diagonal gap fill guarantees (k, k) exists
+}
+
+__global__ void k_block_elem(uint32_t n_elem, const uint64_t *blk_off, uint32_t *blk_elem)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_elem) return;
+    for (uint64_t b = blk_off[e]; b < blk_off[e + 1]; b++) blk_elem[b] = e;
+}
+
+// Gather assembly: one thread per stored block, summing its contributions in
+// element order with the Kahan compensation of solvers/assembly.cpp:676-694:
+//   y = scale*K - c; t = a + y; c = (t - a) - y; a = t.
+template <int S>
+__global__ void k_gather(uint64_t nnzb, const uint64_t *map_ptr, const uint32_t *map, const double *ke,
+                         const uint32_t *blk_elem, const double *scale, double *val)
+{
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nnzb) return;
+    double a[S * S], c[S * S];
+#pragma unroll
+    for (int q = 0; q < S * S; q++) { a[q] = 0.0; c[q] = 0.0; }
+    for (uint64_t k = map_ptr[b]; k < map_ptr[b + 1]; k++) {
+        const uint32_t blk = map[k];
+        const double sc = scale ? scale[blk_elem[blk]] : 1.0;
+        const double *src = ke + (uint64_t)blk * S * S;
+#pragma unroll
+        for (int q = 0; q < S * S; q++) {
+            const double y = sc * src[q] - c[q];
+            const double t = a[q] + y;
+            c[q] = (t - a[q]) - y;
+            a[q] = t;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < S * S; q++) val[b * S * S + q] = a[q];
+}
+
+// Dirichlet elimination, one thread per block row, blocks in column order and
+// constrained columns in increasing id order: the accumulation order of
+// solvers/assembly.cpp:137-249.  Free rows move value * A[row][col] of every
+// constrained column to the right-hand side and zero the entry; constrained
+// rows become unit rows.
+template <int S>
+__global__ void k_dirichlet(uint32_t n_rows, const uint32_t *row_ptr, const uint32_t *col, double *val,
+                            const uint8_t *fixed, const double *fixval, double *rhs)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_rows) return;
+    for (int r = 0; r < S; r++) {
+        const uint64_t row = (uint64_t)k * S + r;
+        if (fixed[row]) {
+            for (uint32_t p = row_ptr[k]; p < row_ptr[k + 1]; p++)
+                for (int c = 0; c < S; c++)
+                    val[(uint64_t)p * S * S + r * S + c] = ((uint64_t)col[p] * S + c == row) ? 1.0 : 0.0;
+            rhs[row] = fixval[row];
+            continue;
+        }
+        double f = rhs[row];
+        for (uint32_t p = row_ptr[k]; p < row_ptr[k + 1]; p++) {
+            const uint64_t cb = (uint64_t)col[p] * S;
+            for (int c = 0; c < S; c++) {
+                if (!fixed[cb + c]) continue;
+                double *a = &val[(uint64_t)p * S * S + r * S + c];
+                f -= fixval[cb + c] * *a;
+                *a = 0.0;
+            }
+        }
+        rhs[row] = f;
+    }
+}
+
+__global__ void k_mark_fixed(uint32_t n_bc, const uint32_t *ids, const double *vals, const uint8_t *kinds,
+                             uint8_t *fixed, double *fixval)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_bc) return;
+    if (kinds && kinds[i] == AMIE_BC_FORCE) return;
+    fixed[ids[i]] = 1;
+    fixval[ids[i]] = vals[i];
+}
+
+// SET_FORCE_* multipliers, added in multiplier order after elimination
+// (solvers/assembly.cpp:277-283).
+__global__ void k_add_forces(uint32_t n_bc, const uint32_t *ids, const double *vals, const uint8_t *kinds,
+                             double *rhs)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0 || !kinds) return;
+    for (uint32_t i = 0; i < n_bc; i++)
+        if (kinds[i] == AMIE_BC_FORCE) rhs[ids[i]] += vals[i];
+}
+
+// InverseDiagonal: 1/A_ii if |A_ii| > 1e-12 else 0 (sparse/sparse_matrix.cpp:216-231),
+// plus the FP32 copies used by the mixed-precision solver.
+template <int S>
+__global__ void k_invdiag(uint32_t n_rows, const uint32_t *diag_pos, const double *val, double *inv, float *inv32)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)n_rows * S) return;
+    const uint32_t k = (uint32_t)(i / S), r = (uint32_t)(i % S);
+    const double v = val[(uint64_t)diag_pos[k] * S * S + r * S + r];
+    const double d = fabs(v) > 1e-12 ? 1.0 / v : 0.0;
+    inv[i] = d;
+    if (inv32) inv32[i] = (float)d;
+}
+
+__global__ void k_to_f32(uint64_t n, const double *a, float *b)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+// Unpadded row-major blocks -> AMIE's column-major, even-padded blocks
+// (sparse/sparse_vector.cpp:57: array[blk*s*cl + c*cl + r]).
+template <int S>
+__global__ void k_to_amie_layout(uint64_t nnzb, const double *val, double *out)
+{
+    constexpr int CL = S + S % 2;
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nnzb) return;
+#pragma unroll
+    for (int c = 0; c < S; c++) {
+#pragma unroll
+        for (int r = 0; r < S; r++) out[b * S * CL + c * CL + r] = val[b * S * S + r * S + c];
+        if (CL != S) out[b * S * CL + c * CL + S] = 0.0;
+    }
+}
+
+inline unsigned blocks_for(uint64_t n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
+
+template <typename T>
+amie_status upload(amie_ctx *ctx, DevArray<T> &d, const T *h, size_t n)
+{
+    AMIE_TRY(d.alloc(ctx, n));
+    if (n) AMIE_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return AMIE_OK;
+}
+
+MeshView mesh_view(amie_topo *t)
+{
+    MeshView m;
+    m.dim = t->dim; m.s = t->s; m.nv = t->nv; m.n_elem = t->n_elem;
+    m.kind = t->kind.p; m.dof_ptr = t->dof_ptr.p; m.dof_ids = t->dof_ids.p;
+    m.gp_ptr = t->gp_ptr.p; m.gp = t->gp.p; m.jinv = t->jinv.p;
+    m.moved = t->has_moved ? t->moved.p : nullptr; m.jinv_gp = t->jinv_gp.p;
+    m.mat = t->mat.p; m.cmat_table = t->cmat_table.p; m.cscale = t->has_cscale ? t->cscale.p : nullptr;
+    m.enr_ptr = t->enr_ptr.p; m.enr_type = t->enr_type.p; m.enr_vertex = t->enr_vertex.p;
+    m.enr_data = t->enr_data.p; m.enr_jump = t->enr_jump.p; m.enr_grad = t->enr_grad.p;
+    m.blk_off = t->blk_off.p; m.ke = t->ke.p;
+    return m;
+}
+
+amie_status validate_mesh(const amie_mesh *m, std::vector<uint32_t> &nf, uint64_t &n_gp, uint32_t &max_id)
+{
+    if (!m || (m->dim != 2 && m->dim != 3) || m->stride != m->dim) {
+        set_error("dim must be 2 or 3 and stride == dim");
+        return AMIE_BAD_INPUT;
+    }
+    if (!m->kind || !m->dof_ptr || !m->dof_ids || !m->gp_ptr || !m->jinv || !m->mat || !m->cmat_table ||
+        m->n_mat == 0) {
+        set_error("missing element arrays");
+        return AMIE_BAD_INPUT;
+    }
+    if (m->n_elem == 0) {
+        set_error("empty mesh");
+        return AMIE_BAD_INPUT;
+    }
+    nf.resize(m->n_elem);
+    max_id = 0;
+    if (m->dof_ptr[0] != 0 || m->gp_ptr[0] != 0 || (m->enr_ptr && m->enr_ptr[0] != 0)) {
+        set_error("offset arrays must start at 0");
+        return AMIE_BAD_INPUT;
+    }
+    for (uint32_t e = 0; e < m->n_elem; e++) {
+        const int ns = nshape_of(m->kind[e]);
+        if (ns == 0 || (m->dim == 2) != (m->kind[e] != AMIE_TET4)) {
+            set_error("element %u: kind %d does not match dim %d", e, m->kind[e], m->dim);
+            return AMIE_BAD_INPUT;
+        }
+        if (m->dof_ptr[e + 1] < m->dof_ptr[e] || m->gp_ptr[e + 1] < m->gp_ptr[e]) {
+            set_error("element %u: offsets decrease", e);
+            return AMIE_BAD_INPUT;
+        }
+        const uint32_t ne = m->enr_ptr ? m->enr_ptr[e + 1] - m->enr_ptr[e] : 0;
+        if (m->enr_ptr && m->enr_ptr[e + 1] < m->enr_ptr[e]) {
+            set_error("element %u: enrichment offsets decrease", e);
+            return AMIE_BAD_INPUT;
+        }
+        nf[e] = m->dof_ptr[e + 1] - m->dof_ptr[e];
+        if (nf[e] != (uint32_t)ns + ne || nf[e] > (uint32_t)kMaxFunctions) {
+            set_error("element %u: %u DOF ids for %d shape + %u enrichment functions (max %d)", e, nf[e], ns, ne,
+                      kMaxFunctions);
+            return AMIE_BAD_INPUT;
+        }
+        if (m->mat[e] >= m->n_mat) {
+            set_error("element %u: material %u >= n_mat %u", e, m->mat[e], m->n_mat);
+            return AMIE_BAD_INPUT;
+        }
+        if (ne) {
+            const uint32_t ngp = m->gp_ptr[e + 1] - m->gp_ptr[e];
+            const uint32_t ngp_eff = ngp ? ngp : (m->kind[e] == AMIE_TRI6 ? 4 : 1);
+            for (uint32_t j = m->enr_ptr[e]; j < m->enr_ptr[e + 1]; j++) {
+                if ((uint64_t)m->enr_data[j] + ngp_eff > m->n_enr_gp) {
+                    set_error("element %u: enrichment data of function %u out of range", e, j);
+                    return AMIE_BAD_INPUT;
+                }
+                if (m->enr_type[j] == AMIE_ENR_HEAVISIDE ? (!m->enr_jump || m->enr_vertex[j] > 2 || m->dim != 2)
+                                                         : (m->enr_type[j] != AMIE_ENR_TABULATED || !m->enr_grad)) {
+                    set_error("element %u: bad enrichment function %u", e, j);
+                    return AMIE_BAD_INPUT;
+                }
+            }
+        }
+        if (m->moved && m->moved[e] && (m->gp_ptr[e + 1] == m->gp_ptr[e] || !m->jinv_gp)) {
+            set_error("element %u: moved elements need explicit Gauss points and jinv_gp", e);
+            return AMIE_BAD_INPUT;
+        }
+        for (uint32_t k = m->dof_ptr[e]; k < m->dof_ptr[e + 1]; k++) max_id = std::max(max_id, m->dof_ids[k]);
+    }
+    if (max_id >= 0x7fffffffu || (m->ndofmax && m->ndofmax >= 0x7fffffffu)) {
+        set_error("DOF ids too large");
+        return AMIE_BAD_INPUT;
+    }
+    n_gp = m->gp_ptr[m->n_elem];
+    return AMIE_OK;
+}
+
+}  // namespace amie
+
+using namespace amie;
+
+extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh, amie_topo **out)
+{
+    if (!ctx || !out) return AMIE_BAD_INPUT;
+    *out = nullptr;
+    std::vector<uint32_t> nf;
+    uint64_t n_gp = 0;
+    uint32_t max_id = 0;
+    AMIE_TRY(validate_mesh(mesh, nf, n_gp, max_id));
+    AMIE_CUDA(cudaSetDevice(ctx->device));
+    amie_topo *t = new amie_topo();
+    auto fail = [&](amie_status s) {
+        delete t;
+        return s;
+    };
+    t->ctx = ctx;
+    t->dim = mesh->dim;
+    t->s = mesh->stride;
+    t->nv = mesh->dim == 2 ? 3 : 6;
+    t->n_elem = mesh->n_elem;
+    t->n_mat = mesh->n_mat;
+    t->ndofmax = mesh->ndofmax;
+    const uint32_t E = mesh->n_elem;
+    const int s = t->s;
+    cudaStream_t st = ctx->stream;
+
+    // staged block offsets and kernel partition
+    std::vector<uint64_t> blk_off(E + 1, 0);
+    std::vector<uint32_t> simple, warp;
+    for (uint32_t e = 0; e < E; e++) {
+        blk_off[e + 1] = blk_off[e] + (uint64_t)nf[e] * nf[e];
+        const uint32_t ne = mesh->enr_ptr ? mesh->enr_ptr[e + 1] - mesh->enr_ptr[e] : 0;
+        (ne ? warp : simple).push_back(e);
+    }
+    t->n_blocks_staged = blk_off[E];
+    if (t->n_blocks_staged >= 0xffffffffull) {
+        delete t;
+        set_error("too many element blocks (%llu)", (unsigned long long)blk_off[E]);
+        return AMIE_BAD_INPUT;
+    }
+    t->h_dof_ptr.assign(mesh->dof_ptr, mesh->dof_ptr + E + 1);
+    t->n_simple = (uint32_t)simple.size();
+    t->n_warp = (uint32_t)warp.size();
+
+    amie_status rc;
+#define UP(dst, src, cnt)                                   \
+    if ((rc = upload(ctx, dst, src, cnt)) != AMIE_OK) return fail(rc);
+    UP(t->kind, mesh->kind, E);
+    UP(t->dof_ptr, mesh->dof_ptr, E + 1);
+    UP(t->dof_ids, mesh->dof_ids, mesh->dof_ptr[E]);
+    UP(t->gp_ptr, mesh->gp_ptr, E + 1);
+    UP(t->gp, mesh->gp, n_gp * (t->dim + 1));
+    UP(t->jinv, mesh->jinv, (size_t)E * t->dim * t->dim);
+    if (mesh->moved) {
+        t->has_moved = true;
+        UP(t->moved, mesh->moved, E);
+        if (mesh->jinv_gp) UP(t->jinv_gp, mesh->jinv_gp, n_gp * t->dim * t->dim);
+    }
+    UP(t->mat, mesh->mat, E);
+    UP(t->cmat_table, mesh->cmat_table, (size_t)mesh->n_mat * t->nv * t->nv);
+    if (mesh->cscale) {
+        t->has_cscale = true;
+        UP(t->cscale, mesh->cscale, E);
+    }
+    if (mesh->enr_ptr) {
+        const uint32_t n_enr = mesh->enr_ptr[E];
+        UP(t->enr_ptr, mesh->enr_ptr, E + 1);
+        UP(t->enr_type, mesh->enr_type, n_enr);
+        UP(t->enr_vertex, mesh->enr_vertex, n_enr);
+        UP(t->enr_data, mesh->enr_data, n_enr);
+        if (mesh->enr_jump) UP(t->enr_jump, mesh->enr_jump, mesh->n_enr_gp);
+        if (mesh->enr_grad) UP(t->enr_grad, mesh->enr_grad, mesh->n_enr_gp * t->dim);
+    }
+    UP(t->blk_off, blk_off.data(), E + 1);
+    UP(t->simple_list, simple.data(), simple.size());
+    UP(t->warp_list, warp.data(), warp.size());
+    if (mesh->scale) {
+        bool all_one = true;
+        for (uint32_t e = 0; e < E; e++) all_one &= mesh->scale[e] == 1.0;
+        if (!all_one) {
+            t->has_scale = true;
+            UP(t->scale, mesh->scale, E);
+            if ((rc = t->blk_elem.alloc(ctx, t->n_blocks_staged)) != AMIE_OK) return fail(rc);
+            k_block_elem<<<blocks_for(E, 256), 256, 0, st>>>(E, t->blk_off.p, t->blk_elem.p);
+            AMIE_LAUNCHED();
+        }
+    }
+#undef UP
+
+    // ---- pattern: keys of all element pairs + fills, stable radix sort, unique
+    const uint32_t n_diag = max_id + 1;
+    const uint32_t last = mesh->ndofmax ? mesh->ndofmax - 1 : max_id;
+    const uint64_t N = t->n_blocks_staged + n_diag + 1;
+    DevArray<uint64_t> keys, keys2;
+    DevArray<uint32_t> vals, vals2, is_new, is_contrib, slot_scan, contrib_scan, row_count;
+    if ((rc = keys.alloc(ctx, N)) || (rc = keys2.alloc(ctx, N)) || (rc = vals.alloc(ctx, N)) ||
+        (rc = vals2.alloc(ctx, N)))
+        return fail(rc);
+    k_pattern_keys<<<blocks_for(E, 128), 128, 0, st>>>(E, t->dof_ptr.p, t->dof_ids.p, t->blk_off.p, keys.p, vals.p);
+    k_fill_keys<<<blocks_for(n_diag + 1, 256), 256, 0, st>>>(t->n_blocks_staged, n_diag, last, keys.p, vals.p);
+    g_launches += 2;
+    const uint32_t max_row = std::max(max_id, last);
+    int end_bit = 32;
+    while (end_bit < 64 && (max_row >> (end_bit - 32)) != 0) end_bit++;
+    size_t temp_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, keys.p, keys2.p, vals.p, vals2.p, (int64_t)N, 0, end_bit, st);
+    DevArray<uint8_t> temp;
+    size_t scan_bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, (const uint32_t *)nullptr, (uint32_t *)nullptr, (int64_t)N, st);
+    if ((rc = temp.alloc(ctx, std::max(temp_bytes, scan_bytes) + 256))) return fail(rc);
+    size_t tb = temp.n;
+    AMIE_CUDA(cub::DeviceRadixSort::SortPairs(temp.p, tb, keys.p, keys2.p, vals.p, vals2.p, (int64_t)N, 0, end_bit, st));
+    keys.release();
+    vals.release();
+    if ((rc = is_new.alloc(ctx, N)) || (rc = is_contrib.alloc(ctx, N)) || (rc = slot_scan.alloc(ctx, N)) ||
+        (rc = contrib_scan.alloc(ctx, N)))
+        return fail(rc);
+    k_unique_flags<<<blocks_for(N, 256), 256, 0, st>>>(N, keys2.p, vals2.p, is_new.p, is_contrib.p);
+    g_launches += 1;
+    tb = temp.n;
+    AMIE_CUDA(cub::DeviceScan::ExclusiveSum(temp.p, tb, is_new.p, slot_scan.p, (int64_t)N, st));
+    tb = temp.n;
+    AMIE_CUDA(cub::DeviceScan::ExclusiveSum(temp.p, tb, is_contrib.p, contrib_scan.p, (int64_t)N, st));
+    uint32_t tail[4];
+    AMIE_CUDA(cudaMemcpyAsync(&tail[0], slot_scan.p + N - 1, 4, cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaMemcpyAsync(&tail[1], is_new.p + N - 1, 4, cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaMemcpyAsync(&tail[2], contrib_scan.p + N - 1, 4, cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaMemcpyAsync(&tail[3], is_contrib.p + N - 1, 4, cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    t->nnzb = (uint64_t)tail[0] + tail[1];
+    t->n_contrib = (uint64_t)tail[2] + tail[3];
+    t->n_rows = max_row + 1;
+    t->n = (uint64_t)t->n_rows * s;
+    if ((rc = t->col.alloc(ctx, t->nnzb)) || (rc = t->map.alloc(ctx, t->n_contrib)) ||
+        (rc = t->map_ptr.alloc(ctx, t->nnzb + 1)) || (rc = row_count.alloc(ctx, t->n_rows + 1)) ||
+        (rc = t->row_ptr.alloc(ctx, t->n_rows + 1)))
+        return fail(rc);
+    AMIE_CUDA(cudaMemsetAsync(row_count.p, 0, (t->n_rows + 1) * 4, st));
+    k_pattern_emit<<<blocks_for(N, 256), 256, 0, st>>>(N, keys2.p, vals2.p, is_new.p, slot_scan.p, contrib_scan.p,
+                                                       t->col.p, row_count.p, t->map_ptr.p, t->map.p);
+    g_launches += 1;
+    const uint64_t nc = t->n_contrib;
+    AMIE_CUDA(cudaMemcpyAsync(t->map_ptr.p + t->nnzb, &nc, 8, cudaMemcpyHostToDevice, st));
+    tb = temp.n;
+    AMIE_CUDA(cub::DeviceScan::ExclusiveSum(temp.p, tb, row_count.p, t->row_ptr.p, (int64_t)t->n_rows + 1, st));
+    if ((rc = t->diag_pos.alloc(ctx, t->n_rows))) return fail(rc);
+    k_diag_pos<<<blocks_for(t->n_rows, 256), 256, 0, st>>>(t->n_rows, t->row_ptr.p, t->col.p, t->diag_pos.p);
+    g_launches += 1;
+    AMIE_CUDA(cudaStreamSynchronize(st));   // nc lives on this stack frame
+    if (t->nnzb >= 0xffffffffull) return fail(AMIE_BAD_INPUT);
+
+    // rows ~ blocks per row -> lanes per block row in the SpMV
+    const double avg = (double)t->nnzb / t->n_rows;
+    t->spmv_group = avg <= 4.5 ? 4 : avg <= 9 ? 8 : avg <= 18 ? 16 : 32;
+
+    // matrix, vectors and staging
+    const uint64_t n = t->n;
+    if ((rc = t->ke.alloc(ctx, t->n_blocks_staged * s * s)) || (rc = t->val.alloc(ctx, t->nnzb * s * s)) ||
+        (rc = t->invdiag.alloc(ctx, n)) || (rc = t->rhs.alloc(ctx, n)) || (rc = t->x.alloc(ctx, n)) ||
+        (rc = t->fixed.alloc(ctx, n)) || (rc = t->fixval.alloc(ctx, n)))
+        return fail(rc);
+    AMIE_CUDA(cudaMemsetAsync(t->rhs.p, 0, n * 8, st));
+    AMIE_CUDA(cudaMemsetAsync(t->x.p, 0, n * 8, st));
+    AMIE_CUDA(cudaMemsetAsync(t->fixed.p, 0, n, st));
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    *out = t;
+    return AMIE_OK;
+}
+
+namespace amie {
+void release_solver_state(const amie_topo *t);
+}
+
+extern "C" amie_status amie_topology_destroy(amie_topo *t)
+{
+    if (!t) return AMIE_OK;
+    cudaSetDevice(t->ctx->device);
+    cudaStreamSynchronize(t->ctx->stream);
+    release_solver_state(t);
+    delete t;
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_topology_sizes(const amie_topo *t, uint32_t *n_rows, uint64_t *nnzb, uint64_t *n)
+{
+    if (!t) return AMIE_BAD_INPUT;
+    if (n_rows) *n_rows = t->n_rows;
+    if (nnzb) *nnzb = t->nnzb;
+    if (n) *n = t->n;
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_topology_pattern(const amie_topo *t, uint32_t *row_size, uint32_t *column_index)
+{
+    if (!t) return AMIE_BAD_INPUT;
+    cudaSetDevice(t->ctx->device);
+    cudaStream_t st = t->ctx->stream;
+    if (row_size) {
+        std::vector<uint32_t> rp(t->n_rows + 1);
+        AMIE_CUDA(cudaMemcpyAsync(rp.data(), t->row_ptr.p, rp.size() * 4, cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+        for (uint32_t k = 0; k < t->n_rows; k++) row_size[k] = rp[k + 1] - rp[k];
+    }
+    if (column_index) {
+        AMIE_CUDA(cudaMemcpyAsync(column_index, t->col.p, t->nnzb * 4, cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+    }
+    return AMIE_OK;
+}
+
+namespace amie {
+
+// Element matrices + gather on the topology's stream (no synchronisation).
+amie_status assemble_async(amie_topo *t)
+{
+    cudaStream_t st = t->ctx->stream;
+    MeshView m = mesh_view(t);
+    if (t->n_simple) {
+        if (t->dim == 2)
+            k_quad_simple<2><<<blocks_for(t->n_simple, 128), 128, 0, st>>>(m, t->simple_list.p, t->n_simple);
+        else
+            k_quad_simple<3><<<blocks_for(t->n_simple, 128), 128, 0, st>>>(m, t->simple_list.p, t->n_simple);
+        AMIE_LAUNCHED();
+    }
+    if (t->n_warp) {
+        if (t->dim == 2)
+            k_quad_warp<2><<<t->n_warp, 32, 0, st>>>(m, t->warp_list.p, t->n_warp);
+        else
+            k_quad_warp<3><<<t->n_warp, 32, 0, st>>>(m, t->warp_list.p, t->n_warp);
+        AMIE_LAUNCHED();
+    }
+    const double *sc = t->has_scale ? t->scale.p : nullptr;
+    if (t->s == 2)
+        k_gather<2><<<blocks_for(t->nnzb, 256), 256, 0, st>>>(t->nnzb, t->map_ptr.p, t->map.p, t->ke.p, t->blk_elem.p, sc,
+                                                             t->val.p);
+    else
+        k_gather<3><<<blocks_for(t->nnzb, 256), 256, 0, st>>>(t->nnzb, t->map_ptr.p, t->map.p, t->ke.p, t->blk_elem.p, sc,
+                                                             t->val.p);
+    AMIE_LAUNCHED();
+    AMIE_CUDA(cudaGetLastError());
+    AMIE_CUDA(cudaMemsetAsync(t->rhs.p, 0, t->n * 8, st));
+    t->assembled = true;
+    t->eliminated = false;
+    t->have32 = false;
+    return AMIE_OK;
+}
+
+// Inverse diagonal (and FP32 copies) of the current matrix.
+amie_status finalize_matrix_async(amie_topo *t, bool want32)
+{
+    cudaStream_t st = t->ctx->stream;
+    const uint64_t n = t->n;
+    float *inv32 = nullptr;
+    if (want32) {
+        if (!t->val32.p) AMIE_TRY(t->val32.alloc(t->ctx, t->nnzb * t->s * t->s));
+        if (!t->invdiag32.p) AMIE_TRY(t->invdiag32.alloc(t->ctx, n));
+        inv32 = t->invdiag32.p;
+    }
+    if (t->s == 2)
+        k_invdiag<2><<<blocks_for(n, 256), 256, 0, st>>>(t->n_rows, t->diag_pos.p, t->val.p, t->invdiag.p, inv32);
+    else
+        k_invdiag<3><<<blocks_for(n, 256), 256, 0, st>>>(t->n_rows, t->diag_pos.p, t->val.p, t->invdiag.p, inv32);
+    AMIE_LAUNCHED();
+    if (want32) {
+        k_to_f32<<<t->ctx->num_sms * 8, 256, 0, st>>>(t->nnzb * t->s * t->s, t->val.p, t->val32.p);
+        AMIE_LAUNCHED();
+        t->have32 = true;
+    }
+    AMIE_CUDA(cudaGetLastError());
+    return AMIE_OK;
+}
+
+amie_status dirichlet_async(amie_topo *t, uint32_t n_bc, const uint32_t *ids_dev, const double *vals_dev,
+                            const uint8_t *kinds_dev)
+{
+    cudaStream_t st = t->ctx->stream;
+    AMIE_CUDA(cudaMemsetAsync(t->fixed.p, 0, t->n, st));
+    if (n_bc) {
+        k_mark_fixed<<<blocks_for(n_bc, 256), 256, 0, st>>>(n_bc, ids_dev, vals_dev, kinds_dev, t->fixed.p, t->fixval.p);
+        AMIE_LAUNCHED();
+    }
+    if (t->s == 2)
+        k_dirichlet<2><<<blocks_for(t->n_rows, 128), 128, 0, st>>>(t->n_rows, t->row_ptr.p, t->col.p, t->val.p,
+                                                                 t->fixed.p, t->fixval.p, t->rhs.p);
+    else
+        k_dirichlet<3><<<blocks_for(t->n_rows, 128), 128, 0, st>>>(t->n_rows, t->row_ptr.p, t->col.p, t->val.p,
+                                                                 t->fixed.p, t->fixval.p, t->rhs.p);
+    AMIE_LAUNCHED();
+    if (n_bc && kinds_dev) {
+        k_add_forces<<<1, 32, 0, st>>>(n_bc, ids_dev, vals_dev, kinds_dev, t->rhs.p);
+        AMIE_LAUNCHED();
+    }
+    AMIE_CUDA(cudaGetLastError());
+    t->eliminated = true;
+    return AMIE_OK;
+}
+
+}  // namespace amie
+
+extern "C" amie_status amie_assemble(amie_topo *t)
+{
+    if (!t) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    AMIE_TRY(assemble_async(t));
+    AMIE_TRY(finalize_matrix_async(t, false));
+    AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_set_cscale(amie_topo *t, const double *cscale)
+{
+    if (!t || !cscale) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    if (!t->cscale.p) AMIE_TRY(t->cscale.alloc(t->ctx, t->n_elem));
+    AMIE_CUDA(cudaMemcpyAsync(t->cscale.p, cscale, (size_t)t->n_elem * 8, cudaMemcpyHostToDevice, t->ctx->stream));
+    t->has_cscale = true;
+    AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_element_matrices(const amie_topo *t, double *ke, uint64_t capacity)
+{
+    if (!t || !ke) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    const int s = t->s;
+    if (capacity < t->n_blocks_staged * s * s) {
+        set_error("capacity %llu < %llu", (unsigned long long)capacity,
+                  (unsigned long long)(t->n_blocks_staged * s * s));
+        return AMIE_BAD_INPUT;
+    }
+    std::vector<double> blocks(t->n_blocks_staged * s * s);
+    AMIE_CUDA(cudaMemcpyAsync(blocks.data(), t->ke.p, blocks.size() * 8, cudaMemcpyDeviceToHost, t->ctx->stream));
+    AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    uint64_t off = 0, boff = 0;
+    for (uint32_t e = 0; e < t->n_elem; e++) {
+        const uint32_t nf = t->h_dof_ptr[e + 1] - t->h_dof_ptr[e];
+        const uint32_t msz = nf * s;
+        for (uint32_t i = 0; i < nf; i++)
+            for (uint32_t j = 0; j < nf; j++)
+                for (int r = 0; r < s; r++)
+                    for (int c = 0; c < s; c++)
+                        ke[off + (uint64_t)(i * s + r) * msz + j * s + c] = blocks[(boff + i * nf + j) * s * s + r * s + c];
+        off += (uint64_t)msz * msz;
+        boff += (uint64_t)nf * nf;
+    }
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_apply_dirichlet(amie_topo *t, uint32_t n_bc, const uint32_t *ids, const double *values,
+                                            const uint8_t *kinds, const double *rhs0)
+{
+    if (!t || (n_bc && (!ids || !values))) return AMIE_BAD_INPUT;
+    if (!t->assembled) {
+        set_error("amie_apply_dirichlet before amie_assemble");
+        return AMIE_BAD_INPUT;
+    }
+    for (uint32_t i = 0; i < n_bc; i++)
+        if (ids[i] >= t->n) {
+            set_error("multiplier %u: id %u >= n %llu", i, ids[i], (unsigned long long)t->n);
+            return AMIE_BAD_INPUT;
+        }
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    cudaStream_t st = t->ctx->stream;
+    if (t->eliminated) {   // re-eliminating needs the original matrix
+        AMIE_TRY(assemble_async(t));
+    }
+    if (rhs0) AMIE_CUDA(cudaMemcpyAsync(t->rhs.p, rhs0, t->n * 8, cudaMemcpyHostToDevice, st));
+    else AMIE_CUDA(cudaMemsetAsync(t->rhs.p, 0, t->n * 8, st));
+    DevArray<uint32_t> d_ids;
+    DevArray<double> d_vals;
+    DevArray<uint8_t> d_kinds;
+    AMIE_TRY(upload(t->ctx, d_ids, ids, n_bc));
+    AMIE_TRY(upload(t->ctx, d_vals, values, n_bc));
+    if (kinds) AMIE_TRY(upload(t->ctx, d_kinds, kinds, n_bc));
+    AMIE_TRY(dirichlet_async(t, n_bc, d_ids.p, d_vals.p, kinds ? d_kinds.p : nullptr));
+    AMIE_TRY(finalize_matrix_async(t, false));
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_matrix_download(const amie_topo *t, double *array, double *rhs)
+{
+    if (!t) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    cudaStream_t st = t->ctx->stream;
+    if (array) {
+        const int s = t->s, cl = s + s % 2;
+        DevArray<double> out;
+        AMIE_TRY(out.alloc(t->ctx, t->nnzb * s * cl));
+        if (s == 2) k_to_amie_layout<2><<<blocks_for(t->nnzb, 256), 256, 0, st>>>(t->nnzb, t->val.p, out.p);
+        else k_to_amie_layout<3><<<blocks_for(t->nnzb, 256), 256, 0, st>>>(t->nnzb, t->val.p, out.p);
+        AMIE_LAUNCHED();
+        AMIE_CUDA(cudaMemcpyAsync(array, out.p, out.bytes(), cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+    }
+    if (rhs) {
+        AMIE_CUDA(cudaMemcpyAsync(rhs, t->rhs.p, t->n * 8, cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+    }
+    return AMIE_OK;
+}

@@ -1,0 +1,162 @@
+// internal.h -- shared definitions of the GB300 FE hot-path library.
+#pragma once
+
+#include "amie_gpu.h"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+namespace amie {
+
+constexpr int kSMs = 152;          // GB300: 2 dies x 76 SMs
+constexpr int kMaxFunctions = 32;  // shape + enrichment functions per element
+constexpr int kMaxGpWarpTile = 8;  // Gauss points staged per tile in the warp quadrature kernel
+
+void set_error(const char *fmt, ...);
+extern std::atomic<uint64_t> g_launches;
+
+#define AMIE_CUDA(call)                                                                     \
+    do {                                                                                    \
+        cudaError_t _e = (call);                                                            \
+        if (_e != cudaSuccess) {                                                            \
+            ::amie::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(_e)); \
+            return _e == cudaErrorMemoryAllocation ? AMIE_OOM : AMIE_CUDA_ERROR;             \
+        }                                                                                   \
+    } while (0)
+
+#define AMIE_TRY(expr)                       \
+    do {                                     \
+        amie_status _s = (expr);             \
+        if (_s != AMIE_OK) return _s;        \
+    } while (0)
+
+#define AMIE_LAUNCHED() (::amie::g_launches.fetch_add(1, std::memory_order_relaxed))
+
+// Device allocation tracked against the context's HBM budget.
+struct Ctx;
+amie_status dev_alloc(Ctx *ctx, void **p, size_t bytes);
+void dev_free(Ctx *ctx, void *p, size_t bytes);
+
+template <typename T>
+struct DevArray {
+    T *p = nullptr;
+    size_t n = 0;
+    Ctx *ctx = nullptr;
+    amie_status alloc(Ctx *c, size_t count)
+    {
+        release();
+        ctx = c;
+        n = count;
+        if (count == 0) return AMIE_OK;
+        return dev_alloc(c, (void **)&p, count * sizeof(T));
+    }
+    void release()
+    {
+        if (p) dev_free(ctx, p, n * sizeof(T));
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+    ~DevArray() { release(); }
+    DevArray() = default;
+    DevArray(const DevArray &) = delete;
+    DevArray &operator=(const DevArray &) = delete;
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t budget = 0;
+    std::atomic<uint64_t> allocated{0};
+    int verbose = 0;
+    int num_sms = kSMs;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double *h_scalars = nullptr;  // pinned scratch for solver control reads
+};
+
+// Device-side view of the element data used by the quadrature kernels.
+struct MeshView {
+    int dim, s, nv;
+    uint32_t n_elem;
+    const uint8_t *kind;
+    const uint32_t *dof_ptr;
+    const uint32_t *dof_ids;
+    const uint32_t *gp_ptr;
+    const double *gp;
+    const double *jinv;
+    const uint8_t *moved;
+    const double *jinv_gp;
+    const uint32_t *mat;
+    const double *cmat_table;
+    const double *cscale;
+    const uint32_t *enr_ptr;
+    const uint8_t *enr_type;
+    const uint8_t *enr_vertex;
+    const uint32_t *enr_data;
+    const int8_t *enr_jump;
+    const double *enr_grad;
+    const uint64_t *blk_off;  // first staged block of each element (in s*s blocks)
+    double *ke;               // staged element matrices: nf*nf blocks of s*s, row-major
+};
+
+// Block-sparse matrix on the device: CSR over block rows, s x s blocks row-major.
+template <typename T>
+struct BsrView {
+    uint32_t n_rows;
+    const uint32_t *row_ptr;
+    const uint32_t *col;
+    const T *val;
+};
+
+}  // namespace amie
+
+// Opaque handles of the C-ABI.
+struct amie_ctx : public amie::Ctx {};
+
+struct amie_topo {
+    amie_ctx *ctx = nullptr;
+    int dim = 0, s = 0, nv = 0;
+    uint32_t n_elem = 0, n_rows = 0, ndofmax = 0, n_mat = 0;
+    uint64_t nnzb = 0, n = 0, n_blocks_staged = 0, n_contrib = 0;
+    bool has_scale = false, has_cscale = false, has_moved = false;
+    std::vector<uint32_t> h_dof_ptr;   // host copy (element matrix export)
+
+    // element data
+    amie::DevArray<uint8_t> kind, moved, enr_type, enr_vertex;
+    amie::DevArray<uint32_t> dof_ptr, dof_ids, gp_ptr, mat, enr_ptr, enr_data;
+    amie::DevArray<double> gp, jinv, jinv_gp, cmat_table, cscale, scale, enr_grad;
+    amie::DevArray<int8_t> enr_jump;
+    amie::DevArray<uint64_t> blk_off;
+    amie::DevArray<uint32_t> simple_list, warp_list;   // elements per quadrature kernel
+    uint32_t n_simple = 0, n_warp = 0;
+
+    // staging + scatter map
+    amie::DevArray<double> ke;
+    amie::DevArray<uint32_t> map;        // staged block index per contribution, slot order
+    amie::DevArray<uint64_t> map_ptr;    // [nnzb+1]
+    amie::DevArray<uint32_t> blk_elem;   // staged block -> element (only with scale)
+
+    // pattern + matrix
+    amie::DevArray<uint32_t> row_ptr, col, diag_pos;
+    amie::DevArray<double> val;
+    amie::DevArray<float> val32;
+    amie::DevArray<double> invdiag;
+    amie::DevArray<float> invdiag32;
+    bool assembled = false, eliminated = false, have32 = false;
+    int spmv_group = 8;
+
+    // right-hand side, solution and solver work vectors
+    amie::DevArray<double> rhs, x, r, z, p, q, xc, rc, red;
+    amie::DevArray<float> r32, z32, p32, q32, d32;
+    amie::DevArray<uint8_t> fixed;
+    amie::DevArray<double> fixval;
+    amie::DevArray<double> scal;   // solver scalars
+    amie::DevArray<int32_t> flags; // solver control flags
+
+    double last_solve_s = 0;
+};

@@ -1,0 +1,403 @@
+// solver.cu -- host drivers of the device-resident solvers and the solve
+// entry points of the C-ABI.
+//
+//   AMIE_SOLVER_PCG_FP64   Jacobi-PCG in FP64, relative-residual stop, restarted
+//                          from the true residual b - A x if the recursive one drifted.
+//   AMIE_SOLVER_PCG_MIXED  FP64 iterative refinement: r = b - A x (FP64), inner
+//                          FP32 Jacobi-PCG on A d = r/|r| with FP32 SpMV, FP32
+//                          preconditioner and FP32 direction updates, then
+//                          x += |r| d accumulated in FP64.
+//   AMIE_SOLVER_AMIE_CG    ConjugateGradient::solve semantics (amie_cg.cu).
+#include "solver.cuh"
+
+#include <chrono>
+#include <cmath>
+#include <mutex>
+#include <unordered_map>
+
+namespace amie {
+
+amie_status assemble_async(amie_topo *t);
+amie_status finalize_matrix_async(amie_topo *t, bool want32);
+amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *st);
+
+struct SolverState {
+    int grid = 0;
+    DevArray<double> parts;       // 4 * grid
+    DevArray<PcgCtl> ctl;
+    PcgCtl *h_ctl = nullptr;      // pinned
+    cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
+    int graph_iters = 0;
+    ~SolverState()
+    {
+        if (graph64) cudaGraphExecDestroy(graph64);
+        if (graph32) cudaGraphExecDestroy(graph32);
+        if (h_ctl) cudaFreeHost(h_ctl);
+    }
+};
+
+static std::mutex g_state_mu;
+static std::unordered_map<const amie_topo *, SolverState *> g_states;
+
+SolverState *state_of(amie_topo *t)
+{
+    std::lock_guard<std::mutex> lk(g_state_mu);
+    auto it = g_states.find(t);
+    return it == g_states.end() ? nullptr : it->second;
+}
+
+void release_solver_state(const amie_topo *t)
+{
+    std::lock_guard<std::mutex> lk(g_state_mu);
+    auto it = g_states.find(t);
+    if (it != g_states.end()) {
+        delete it->second;
+        g_states.erase(it);
+    }
+}
+
+template <int S, typename T, typename F>
+void dispatch_group(int group, F &&f)
+{
+    switch (group) {
+    case 4: f(std::integral_constant<int, 4>()); break;
+    case 8: f(std::integral_constant<int, 8>()); break;
+    case 16: f(std::integral_constant<int, 16>()); break;
+    default: f(std::integral_constant<int, 32>()); break;
+    }
+}
+
+// Launch q = A p (+ partial p.q) for the topology's stride and lane group.
+template <typename T>
+void launch_spmv_pq(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, const PcgCtl *ctl, cudaStream_t st)
+{
+    auto go = [&](auto g) {
+        constexpr int G = decltype(g)::value;
+        if (t->s == 2) k_spmv_pq<2, G, T><<<grid, kVecThreads, 0, st>>>(v, part, ctl);
+        else k_spmv_pq<3, G, T><<<grid, kVecThreads, 0, st>>>(v, part, ctl);
+    };
+    dispatch_group<2, T>(t->spmv_group, go);
+    AMIE_LAUNCHED();
+}
+
+template <typename T>
+void launch_spmv(amie_topo *t, int grid, BsrView<T> A, const T *x, const T *b, T *y, double *part, cudaStream_t st)
+{
+    auto go = [&](auto g) {
+        constexpr int G = decltype(g)::value;
+        if (t->s == 2) k_spmv<2, G, T><<<grid, kVecThreads, 0, st>>>(A, x, b, y, part);
+        else k_spmv<3, G, T><<<grid, kVecThreads, 0, st>>>(A, x, b, y, part);
+    };
+    dispatch_group<2, T>(t->spmv_group, go);
+    AMIE_LAUNCHED();
+}
+
+BsrView<double> bsr64(amie_topo *t) { return BsrView<double>{t->n_rows, t->row_ptr.p, t->col.p, t->val.p}; }
+BsrView<float> bsr32(amie_topo *t) { return BsrView<float>{t->n_rows, t->row_ptr.p, t->col.p, t->val32.p}; }
+
+amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
+{
+    SolverState *s = state_of(t);
+    if (!s) {
+        s = new SolverState();
+        {
+            std::lock_guard<std::mutex> lk(g_state_mu);
+            g_states[t] = s;
+        }
+        // Grid: resident CTAs of the SpMV kernel on every SM (a multiple of the SM count).
+        int per_sm = 0;
+        auto occ = [&](auto g) {
+            constexpr int G = decltype(g)::value;
+            if (t->s == 2)
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv_pq<2, G, double>, kVecThreads, 0);
+            else
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv_pq<3, G, double>, kVecThreads, 0);
+        };
+        dispatch_group<2, double>(t->spmv_group, occ);
+        per_sm = std::max(1, std::min(per_sm, 8));
+        s->grid = t->ctx->num_sms * per_sm;
+        AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->grid));
+        AMIE_TRY(s->ctl.alloc(t->ctx, 1));
+        AMIE_CUDA(cudaMallocHost((void **)&s->h_ctl, sizeof(PcgCtl)));
+        const uint64_t n = t->n;
+        AMIE_TRY(t->r.alloc(t->ctx, n));
+        AMIE_TRY(t->z.alloc(t->ctx, n));
+        AMIE_TRY(t->p.alloc(t->ctx, n));
+        AMIE_TRY(t->q.alloc(t->ctx, n));
+    }
+    if (want32 && !t->r32.p) {
+        const uint64_t n = t->n;
+        AMIE_TRY(t->r32.alloc(t->ctx, n));
+        AMIE_TRY(t->z32.alloc(t->ctx, n));
+        AMIE_TRY(t->p32.alloc(t->ctx, n));
+        AMIE_TRY(t->q32.alloc(t->ctx, n));
+        AMIE_TRY(t->d32.alloc(t->ctx, n));
+    }
+    *out = s;
+    return AMIE_OK;
+}
+
+PcgParts parts_of(SolverState *s)
+{
+    PcgParts p;
+    p.pq = s->parts.p;
+    p.rz[0] = s->parts.p + s->grid;
+    p.rz[1] = s->parts.p + 2 * s->grid;
+    p.rr = s->parts.p + 3 * s->grid;
+    return p;
+}
+
+template <typename T>
+PcgVecs<T> vecs_of(amie_topo *t);
+template <>
+PcgVecs<double> vecs_of<double>(amie_topo *t)
+{
+    return PcgVecs<double>{bsr64(t), t->invdiag.p, t->x.p, t->r.p, t->z.p, t->p.p, t->q.p};
+}
+template <>
+PcgVecs<float> vecs_of<float>(amie_topo *t)
+{
+    return PcgVecs<float>{bsr32(t), t->invdiag32.p, t->d32.p, t->r32.p, t->z32.p, t->p32.p, t->q32.p};
+}
+
+constexpr int kGraphIters = 16;   // PCG iterations per graph launch (even: parity restarts at 0)
+
+template <typename T>
+amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
+{
+    if (*g) return AMIE_OK;
+    cudaStream_t st = t->ctx->stream;
+    PcgVecs<T> v = vecs_of<T>(t);
+    PcgParts parts = parts_of(s);
+    cudaGraph_t graph;
+    AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < kGraphIters; it++) {
+        const int parity = it & 1;
+        launch_spmv_pq<T>(t, s->grid, v, parts.pq, s->ctl.p, st);
+        k_update<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts, parity, s->ctl.p);
+        k_direction<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts, parity, s->ctl.p);
+        g_launches += 2;
+    }
+    AMIE_CUDA(cudaStreamEndCapture(st, &graph));
+    cudaError_t e = cudaGraphInstantiate(g, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        return AMIE_CUDA_ERROR;
+    }
+    return AMIE_OK;
+}
+
+double sum_host(const double *p, int n)
+{
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += p[i];
+    return s;
+}
+
+// Sum of the first `n` doubles of a device array (partials), synchronously.
+amie_status read_sum(amie_topo *t, const double *dev, int n, double *out)
+{
+    std::vector<double> h(n);
+    AMIE_CUDA(cudaMemcpyAsync(h.data(), dev, n * sizeof(double), cudaMemcpyDeviceToHost, t->ctx->stream));
+    AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    *out = sum_host(h.data(), n);
+    return AMIE_OK;
+}
+
+// One PCG run from the residual already in v.r; stops when r.r <= tol2 or after maxit iterations.
+template <typename T>
+amie_status run_pcg(amie_topo *t, SolverState *s, double tol2, int64_t maxit, int64_t *iters, double *rr_out)
+{
+    cudaStream_t st = t->ctx->stream;
+    PcgVecs<T> v = vecs_of<T>(t);
+    PcgParts parts = parts_of(s);
+    cudaGraphExec_t *g = sizeof(T) == 8 ? &s->graph64 : &s->graph32;
+    AMIE_TRY(graph_for<T>(t, s, g));
+    k_pcg_start<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts);
+    AMIE_LAUNCHED();
+    PcgCtl init{};
+    init.done = 0;
+    init.iterations = 0;
+    init.maxit = maxit;
+    init.tol2 = tol2;
+    *s->h_ctl = init;
+    AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
+    // The pinned copy is rewritten below only after this copy has completed.
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    while (true) {
+        AMIE_CUDA(cudaGraphLaunch(*g, st));
+        g_launches += 3 * kGraphIters;
+        AMIE_CUDA(cudaMemcpyAsync(s->h_ctl, s->ctl.p, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+        if (s->h_ctl->done) break;
+    }
+    *iters = s->h_ctl->iterations;
+    *rr_out = s->h_ctl->rr;
+    return AMIE_OK;
+}
+
+__global__ void k_scale_to_f32(uint64_t n, const double *r, double inv, float *r32, float *d32)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        r32[i] = (float)(r[i] * inv);
+        d32[i] = 0.0f;
+    }
+}
+
+__global__ void k_accumulate(uint64_t n, const float *d32, double scale, double *x)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        x[i] += scale * (double)d32[i];
+}
+
+__global__ void k_norm2_parts(uint64_t n, const double *v, double *part)
+{
+    __shared__ double sh[33];
+    double a = 0.0;
+    for (uint64_t i = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kVecThreads)
+        a += v[i] * v[i];
+    a = block_sum(a, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
+// r = b - A x in FP64; returns r.r.
+amie_status true_residual(amie_topo *t, SolverState *s, double *rr)
+{
+    launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->grid, t->ctx->stream);
+    AMIE_CUDA(cudaGetLastError());
+    return read_sum(t, s->parts.p + 3 * s->grid, s->grid, rr);
+}
+
+amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *st_out, bool mixed)
+{
+    SolverState *s = nullptr;
+    AMIE_TRY(ensure_state(t, mixed, &s));
+    if (mixed && !t->have32) AMIE_TRY(finalize_matrix_async(t, true));
+    cudaStream_t st = t->ctx->stream;
+    const double rtol = o && o->rtol > 0 ? o->rtol : 1e-10;
+    const int64_t maxit = o && o->maxit > 0 ? o->maxit : std::max<int64_t>(1000, (int64_t)t->n);
+    const double inner_rtol = o && o->inner_rtol > 0 ? o->inner_rtol : 1e-5;
+    k_norm2_parts<<<s->grid, kVecThreads, 0, st>>>(t->n, t->rhs.p, s->parts.p);
+    AMIE_LAUNCHED();
+    double bb = 0.0;
+    AMIE_TRY(read_sum(t, s->parts.p, s->grid, &bb));
+    const double bnorm = std::sqrt(bb);
+    st_out->iterations = 0;
+    st_out->refinements = 0;
+    if (bnorm == 0.0) {
+        AMIE_CUDA(cudaMemsetAsync(t->x.p, 0, t->n * 8, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+        st_out->relres = 0.0;
+        st_out->status = AMIE_OK;
+        return AMIE_OK;
+    }
+    double rr = 0.0;
+    AMIE_TRY(true_residual(t, s, &rr));
+    int64_t total = 0;
+    const double target2 = (rtol * bnorm) * (rtol * bnorm);
+    amie_status result = AMIE_NOT_CONVERGED;
+    for (int outer = 0; outer < 200; outer++) {
+        if (!(rr == rr)) { result = AMIE_NAN; break; }
+        if (rr <= target2) { result = AMIE_OK; break; }
+        if (total >= maxit) break;
+        int64_t it = 0;
+        double rr_in = 0.0;
+        if (!mixed) {
+            // recursive residual target a little below the true one: the true residual is re-checked
+            AMIE_TRY(run_pcg<double>(t, s, target2 * 0.25, maxit - total, &it, &rr_in));
+        } else {
+            const double norm = std::sqrt(rr);
+            k_scale_to_f32<<<s->grid, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / norm, t->r32.p, t->d32.p);
+            AMIE_LAUNCHED();
+            AMIE_TRY(run_pcg<float>(t, s, inner_rtol * inner_rtol, maxit - total, &it, &rr_in));
+            k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, norm, t->x.p);
+            AMIE_LAUNCHED();
+            st_out->refinements++;
+        }
+        total += it;
+        AMIE_TRY(true_residual(t, s, &rr));
+        if (!mixed && it == 0) break;
+    }
+    AMIE_CUDA(cudaGetLastError());
+    st_out->iterations = total;
+    st_out->relres = std::sqrt(rr) / bnorm;
+    st_out->status = result;
+    return AMIE_OK;
+}
+
+amie_status solve_dispatch(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *stats)
+{
+    if (!t->assembled) {
+        set_error("solve before amie_assemble");
+        return AMIE_BAD_INPUT;
+    }
+    const int solver = o ? o->solver : AMIE_SOLVER_PCG_FP64;
+    auto t0 = std::chrono::steady_clock::now();
+    amie_status rc;
+    if (solver == AMIE_SOLVER_PCG_FP64) rc = solve_pcg(t, o, stats, false);
+    else if (solver == AMIE_SOLVER_PCG_MIXED) rc = solve_pcg(t, o, stats, true);
+    else if (solver == AMIE_SOLVER_AMIE_CG) rc = amie_cg_solve(t, o, stats);
+    else {
+        set_error("unknown solver %d", solver);
+        return AMIE_BAD_INPUT;
+    }
+    AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    t->last_solve_s = stats->seconds;
+    return rc;
+}
+
+}  // namespace amie
+
+using namespace amie;
+
+extern "C" amie_status amie_solve_resident(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *stats)
+{
+    if (!t) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    amie_solve_stats local{};
+    amie_solve_stats *sp = stats ? stats : &local;
+    if (!(o && o->use_x0)) AMIE_CUDA(cudaMemsetAsync(t->x.p, 0, t->n * 8, t->ctx->stream));
+    AMIE_TRY(solve_dispatch(t, o, sp));
+    return (amie_status)sp->status;
+}
+
+extern "C" amie_status amie_solve(amie_topo *t, const amie_solve_opts *o, double *x_inout, amie_solve_stats *stats)
+{
+    if (!t || !x_inout) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    cudaStream_t st = t->ctx->stream;
+    if (o && o->use_x0) AMIE_CUDA(cudaMemcpyAsync(t->x.p, x_inout, t->n * 8, cudaMemcpyHostToDevice, st));
+    else AMIE_CUDA(cudaMemsetAsync(t->x.p, 0, t->n * 8, st));
+    amie_solve_stats local{};
+    amie_solve_stats *sp = stats ? stats : &local;
+    AMIE_TRY(solve_dispatch(t, o, sp));
+    AMIE_CUDA(cudaMemcpyAsync(x_inout, t->x.p, t->n * 8, cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    return (amie_status)sp->status;
+}
+
+extern "C" amie_status amie_solution_download(const amie_topo *t, double *x)
+{
+    if (!t || !x) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    AMIE_CUDA(cudaMemcpyAsync(x, t->x.p, t->n * 8, cudaMemcpyDeviceToHost, t->ctx->stream));
+    AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_spmv(amie_topo *t, const double *x, double *y)
+{
+    if (!t || !x || !y) return AMIE_BAD_INPUT;
+    if (!t->assembled) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    SolverState *s = nullptr;
+    AMIE_TRY(ensure_state(t, false, &s));
+    cudaStream_t st = t->ctx->stream;
+    AMIE_CUDA(cudaMemcpyAsync(t->p.p, x, t->n * 8, cudaMemcpyHostToDevice, st));
+    launch_spmv<double>(t, s->grid, bsr64(t), t->p.p, nullptr, t->q.p, nullptr, st);
+    AMIE_CUDA(cudaMemcpyAsync(y, t->q.p, t->n * 8, cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    return AMIE_OK;
+}
