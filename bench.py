@@ -1,0 +1,481 @@
+"""Benchmark of the GB300 FE hot path: element stiffness -> block-sparse
+scatter -> Dirichlet elimination -> Jacobi-PCG (FP32 inner / FP64 refinement).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config cfg1|cfg0|cfg2] [--solver mixed|fp64]
+
+Workload (default, the configuration the headline metric is quoted on):
+cfg1 -- 2D quadratic (P2) triangles, ~1.2 M DOF, 4000 seeded non-overlapping
+inclusions (truncated power-law radii, exponent -2.5, 0.1-2 mm, E 60 GPa in a
+25 GPa matrix), a seeded straight crack of length 0.3 x width with Heaviside
+enrichment of the cut elements, tip branch functions on the tip element
+(512 Monte-Carlo Gauss points), bottom fixed, top displaced 1e-5 m.  Seeded
+synthetic data (workloads.py) stands in for the reference's mesher.
+
+One step = element stiffness quadrature + atomic-free scatter + Dirichlet
+elimination + solve to relative residual 1e-10, with the element data resident
+in HBM.  value = DOF x PCG iterations / step time (whole job: summed over
+ranks, max time over ranks).  Inputs (matrix, vectors) exceed the 129 MB L2.
+
+Multi-GPU: the path does not shard (one solve per GPU); N ranks run N
+independent replicas (weak scaling).
+
+--impl reference times the CPU restatement of the reference path
+(oracle/amie_oracle.cpp, Kahan SpMV / dots as ConjugateGradient::solve) on all
+host threads, on the same workload, each step a bounded sample of PCG
+iterations.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for sub in ("xfem-amie_gb300", "oracle"):
+    p = os.path.join(REPO, sub)
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+import amie_mesh as am  # noqa: E402
+import workloads as W  # noqa: E402
+
+METRIC = "DOF-iterations/s (element stiffness + scatter + Dirichlet + Jacobi-PCG to relative residual 1e-10)"
+UNIT = "DOF-iterations/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg1", choices=["cfg0", "cfg1", "cfg2"])
+    ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--rtol", type=float, default=1e-10)
+    ap.add_argument("--size", type=int, default=0, help="override the mesh resolution (cells per side)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
+    ap.add_argument("--serve", type=int, default=256, help="serving-mix requests (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ workloads
+
+def make_workload(cfg: str, size: int = 0):
+    if cfg == "cfg1":
+        N = size or 387
+        m, bcs, meta = W.cracked_square(N, L=0.1, order=2, n_inclusions=4000 if N >= 200 else 400, seed=2024)
+        name = "cfg1: P2 triangles, 4000 power-law inclusions, Heaviside crack 0.3 L"
+    elif cfg == "cfg0":
+        N = size or 141
+        m, bcs, meta = W.inclusion_square(N, L=0.04, order=1, n_inclusions=300, seed=2024)
+        name = "cfg0: P1 triangles, 300 inclusions"
+    else:
+        N = size or 64
+        m, bcs, meta = W.voxel_cube(N, seed=2024)
+        name = "cfg2: 64^3 voxels x 6 linear tetrahedra, lognormal E"
+    meta["cells_per_side"] = N
+    return m, bcs, meta, name
+
+
+def mesh_bytes(m: am.MeshData) -> int:
+    tot = 0
+    for k in ("kind", "dof_ptr", "dof_ids", "gp_ptr", "gp", "jinv", "moved", "jinv_gp", "mat", "cmat_table",
+              "cscale", "scale", "enr_ptr", "enr_type", "enr_vertex", "enr_data", "enr_jump", "enr_grad"):
+        a = getattr(m, k)
+        if a is not None:
+            tot += a.nbytes
+    return tot
+
+
+def spmv_bytes(nnzb: int, n_rows: int, s: int, w: int) -> int:
+    """Algorithmic bytes of one block SpMV: blocks + column indices + row pointers + x read + y write."""
+    return nnzb * (s * s * w + 4) + 4 * (n_rows + 1) + 2 * n_rows * s * w
+
+
+def load_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel_key: str):
+    """DRAM bytes per launch of the kernel from the committed ncu summary, if any."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(kernel_key)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.remove(self.path)
+        if not rows:
+            return None
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ distributed
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allreduce_max(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU legs
+
+def cpu_pcg_sample(stride, rs, ci, arr, rhs, seconds: float):
+    """DOF-iterations/s of the oracle's PCG (Kahan SpMV and dots) over a bounded sample."""
+    import oracle as O
+    n = len(rhs)
+    t0 = time.perf_counter()
+    O.pcg(stride, rs, ci, arr, rhs, rtol=1e-30, maxit=5)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    iters = int(max(5, min(2000, 5 * seconds / dt)))
+    t0 = time.perf_counter()
+    _, it, _, _ = O.pcg(stride, rs, ci, arr, rhs, rtol=1e-30, maxit=iters)
+    dt = time.perf_counter() - t0
+    return n * it / dt, it, dt
+
+
+def cpu_assembly(m, bcs):
+    import oracle as O
+    t0 = time.perf_counter()
+    R = O.assemble(m, *bcs)
+    return R, time.perf_counter() - t0
+
+
+def run_reference(args, world, rank, dist):
+    """--impl reference: the CPU restatement of the reference path on the host cores."""
+    if rank != 0:
+        return 0
+    import oracle as O
+    O.build()
+    m, bcs, meta, name = make_workload(args.config, args.size)
+    R, t_asm = cpu_assembly(m, bcs)
+    n = len(R["rhs"])
+    stride = m.stride
+    vals = []
+    per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_pcg_sample(stride, R["row_size"], R["column_index"], R["array"], R["rhs"], 1.0)
+    samples = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        v, it, dt = cpu_pcg_sample(stride, R["row_size"], R["column_index"], R["array"], R["rhs"], per_step)
+        vals.append(v)
+        samples.append((it, dt))
+    total_t = time.perf_counter() - t_all
+    value = float(np.mean(vals))
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": name, "n_dof": int(n), "nnzb": int(len(R["column_index"])), **_cfg_meta(meta)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
+                         "sample": f"{samples[0][0]} Jacobi-PCG iterations (Kahan SpMV/dots) per step on the "
+                                   f"assembled {n}-DOF matrix; CPU assembly {t_asm:.2f} s untimed"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def _cfg_meta(meta):
+    keep = ("n_elem", "n_nodes", "n_inclusions", "n_cut", "n_enriched", "order", "cells_per_side")
+    return {k: (int(v) if isinstance(v, (np.integer, int)) else v) for k, v in meta.items() if k in keep}
+
+
+# ------------------------------------------------------------------ GPU leg
+
+def run_ours(args, world, rank, local, dist):
+    import amie_gpu as G
+    import build as gpu_build
+    gpu_build.build()
+    m, bcs, meta, name = make_workload(args.config, args.size)
+    ctx = G.Context(local)
+    solver = G.SOLVER_PCG_MIXED if args.solver == "mixed" else G.SOLVER_PCG_FP64
+    topo = G.Topology(ctx, m)
+    topo.assemble()
+    topo.apply_dirichlet(*bcs)
+    n = topo.n
+
+    def step(sv=solver, rtol=args.rtol):
+        ctx.timer_start()
+        topo.assemble()                       # quadrature + gather + stored Dirichlet elimination
+        st = topo.solve_resident(sv, rtol=rtol)
+        ms = ctx.timer_stop()
+        return ms, st
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    barrier(dist)
+    launches0 = G.kernel_launches()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_wall = time.perf_counter()
+    times, iters, stats = [], [], []
+    for _ in range(args.steps):
+        ms, st = step()
+        times.append(ms)
+        iters.append(st["iterations"])
+        stats.append(st)
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    launches = G.kernel_launches() - launches0
+    barrier(dist)
+    t_local = sum(times) / 1e3
+    t_max = allreduce_max(dist, t_local)
+    dof_it = allreduce_sum(dist, float(n) * sum(iters))
+    value = dof_it / t_max
+    x_mixed = topo.solution()
+
+    # FP64 plain path on the same matrix: throughput and the reference solution for the error statement
+    ms64, st64 = step(G.SOLVER_PCG_FP64, args.rtol)
+    x64 = topo.solution()
+    ms_tight, st_tight = step(G.SOLVER_PCG_FP64, 1e-12)
+    x_tight = topo.solution()
+    node_dofs = slice(0, meta.get("n_nodes", n // m.stride) * m.stride)
+    err_mixed = float(np.abs(x_mixed[node_dofs] - x_tight[node_dofs]).max() / np.abs(x_tight[node_dofs]).max())
+    err_fp64 = float(np.abs(x64[node_dofs] - x_tight[node_dofs]).max() / np.abs(x_tight[node_dofs]).max())
+    fp64_value = n * st64["iterations"] / (ms64 / 1e3)
+
+    # assembly alone (quadrature + gather + elimination) and solve-only rates
+    ctx.timer_start()
+    topo.assemble()
+    ms_asm = ctx.timer_stop()
+
+    # dominant kernel: block SpMV of the inner solve (FP32 for mixed, FP64 otherwise)
+    prec = 32 if solver == G.SOLVER_PCG_MIXED else 64
+    w = prec // 8
+    ms_spmv = topo.profile_spmv(prec, 50)
+    ms_spmv64 = topo.profile_spmv(64, 50)
+    peak, peak_kind = load_peaks()
+    alg = spmv_bytes(topo.nnzb, topo.n_rows, m.stride, w)
+    alg64 = spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 8)
+    achieved = alg / (ms_spmv / 1e3) / 1e9
+    achieved64 = alg64 / (ms_spmv64 / 1e3) / 1e9
+    traffic = load_traffic(f"{args.config}_spmv{prec}")
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if solver == G.SOLVER_PCG_MIXED else "f64", "data": "synthetic (seeded)",
+        "config": {"workload": name, "solver": args.solver, "rtol": args.rtol, "n_dof": int(n),
+                   "nnzb": int(topo.nnzb), "block": f"{m.stride}x{m.stride}",
+                   "l2": "inputs larger than L2 (matrix + vectors > 129 MB)", "parallelism": f"replicas x{world}",
+                   **_cfg_meta(meta)},
+        "solve": {"iterations": iters, "refinements": [s["refinements"] for s in stats],
+                  "relres": [s["relres"] for s in stats], "ms_per_step": times,
+                  "err_vs_fp64_1e-12": err_mixed},
+        "fp64": {"value": fp64_value, "iterations": st64["iterations"], "ms": ms64, "relres": st64["relres"],
+                 "err_vs_fp64_1e-12": err_fp64},
+        "mixed_vs_fp64_dof_it": value / world / fp64_value if solver == G.SOLVER_PCG_MIXED else 1.0,
+        "mixed_vs_fp64_solve_time": ms64 / (t_local * 1e3 / args.steps) if solver == G.SOLVER_PCG_MIXED else 1.0,
+        "assembly_ms": ms_asm,
+        "roofline": {"bound": "hbm", "kernel": f"k_spmv_pq<{m.stride},{topo_group(topo)},{'float' if w == 4 else 'double'}>",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic, "alg_bytes_per_launch": alg,
+                     "ms_per_launch": ms_spmv},
+        "roofline_fp64_spmv": {"achieved": achieved64, "frac": achieved64 / peak, "alg_bytes_per_launch": alg64,
+                               "ms_per_launch": ms_spmv64},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "wall_s_timed": wall,
+    }
+
+    # end to end through the public API with host buffers: upload + pattern + assemble + elimination + solve + download
+    if not args.no_e2e:
+        e2e_ms, e2e_it = [], []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            tp = G.Topology(ctx, m)
+            tp.assemble()
+            tp.apply_dirichlet(*bcs)
+            xs, st = tp.solve(solver, rtol=args.rtol)
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            e2e_it.append(st["iterations"])
+            tp.close()
+        e2e_t = allreduce_max(dist, e2e_ms[-1] / 1e3)
+        e2e_dof_it = allreduce_sum(dist, float(n) * e2e_it[-1])
+        h2d = mesh_bytes(m) + sum(a.nbytes for a in bcs)
+        result["e2e"] = {"value": e2e_dof_it / e2e_t, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                         "d2h_bytes_per_step": int(n * 8), "ms": e2e_ms[-1]}
+
+    # serving mix (config 4): p50 / p99 latency next to throughput
+    if args.serve > 0:
+        result["serving"] = run_serving(ctx, args.serve, args.serve_rate, solver)
+
+    # CPU baseline: the oracle port on this machine's host cores, bounded sample, rank 0 at N = 1
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle as O
+        O.build()
+        rs, ci = topo.pattern()
+        arr, rhs = topo.matrix()
+        v_cpu, it_cpu, dt_cpu = cpu_pcg_sample(m.stride, rs, ci, arr, rhs, args.cpu_seconds)
+        result["cpu_baseline"] = {"value": v_cpu, "unit": UNIT, "cores": O.threads(), "kind": "port",
+                                  "sample": f"{it_cpu} Jacobi-PCG iterations (Kahan SpMV/dots) on the same "
+                                            f"{n}-DOF matrix, {dt_cpu:.1f} s"}
+    topo.close()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(result))
+    return 0
+
+
+def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, pool: int = 32):
+    """Config-4 serving mix: Poisson arrivals of independent homogenisation solves
+    (log-uniform 2k-200k DOF, inclusion fraction U[0.2, 0.6]) into the
+    continuous-batching server.  Returns p50/p99 latency and solves/s."""
+    import amie_gpu as G
+    meshes, arrivals, which = W.serving_mix(n_requests, rate, seed=seed, pool=pool)
+    srv = G.Server(ctx, solver=solver, rtol=1e-10)
+    # warm the server (graph, first allocations) with one request
+    t = srv.submit(meshes[0][0], *meshes[0][1])
+    srv.drain(60.0)
+    srv.poll(t, want_x=False)
+    tickets = []
+    t0 = time.perf_counter()
+    for k in range(n_requests):
+        delay = arrivals[k] - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        m, bcs, _ = meshes[which[k]]
+        tickets.append(srv.submit(m, *bcs))
+    srv.drain(600.0)
+    wall = time.perf_counter() - t0
+    lat, statuses, dofs, iters = [], [], [], []
+    for k, tk in enumerate(tickets):
+        r = srv.poll(tk, want_x=False)
+        if r is None:
+            continue
+        res, _ = r
+        lat.append(res["latency_s"])
+        statuses.append(res["status"])
+        dofs.append(res["n"])
+        iters.append(res["iterations"])
+    srv.stop()
+    lat = np.array(lat)
+    ok = int(sum(1 for s in statuses if s == G.AMIE_OK))
+    return {"requests": n_requests, "completed_ok": ok, "rate_req_s": rate, "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "solves_per_s": ok / wall, "wall_s": wall,
+            "mean_dof": float(np.mean(dofs)) if dofs else 0.0, "mean_iterations": float(np.mean(iters)) if iters else 0.0,
+            "distinct_microstructures": pool,
+            "solver": "mixed" if solver == G.SOLVER_PCG_MIXED else "fp64"}
+
+
+def topo_group(topo):
+    avg = topo.nnzb / max(1, topo.n_rows)
+    return 4 if avg <= 4.5 else 8 if avg <= 9 else 16 if avg <= 18 else 32
+
+
+def main():
+    args = parse_args()
+    world, rank, local, dist = dist_setup(args.gpus)
+    try:
+        if args.impl == "reference":
+            return run_reference(args, world, rank, dist)
+        return run_ours(args, world, rank, local, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -160,7 +160,9 @@ AMIE_API amie_status amie_element_matrices(const amie_topo *topo, double *ke, ui
 /* Dirichlet elimination of Assembly::setBoundaryConditions
  * (solvers/assembly.cpp:125-283) for multipliers set by Assembly::setPointAlong
  * (solvers/assembly.cpp:1590) or SET_FORCE_*.  rhs0: initial force vector
- * [n] or NULL (zero). */
+ * [n] or NULL (zero).  The multipliers stay on the device: every later
+ * amie_assemble (a damage step, a new material factor) scatters and
+ * eliminates again, as make_final does. */
 AMIE_API amie_status amie_apply_dirichlet(amie_topo *topo, uint32_t n_bc, const uint32_t *ids, const double *values,
                                  const uint8_t *kinds, const double *rhs0);
 
@@ -224,6 +226,18 @@ AMIE_API amie_status amie_cancel(amie_server *srv, uint64_t ticket);
 /* Runs the server loop until every submitted request is finished or timeout_s elapses. */
 AMIE_API amie_status amie_server_drain(amie_server *srv, double timeout_s);
 AMIE_API amie_status amie_server_stop(amie_server *srv);
+
+/* ------------------------------------------------------------------ timing
+ * Device time on the context's stream (CUDA events) between start and stop;
+ * stop synchronises the stream.  No counterpart in the reference, which
+ * prints wall times only (solvers/assembly.cpp:1851-1853). */
+AMIE_API amie_status amie_timer_start(amie_ctx *ctx);
+AMIE_API amie_status amie_timer_stop(amie_ctx *ctx, double *ms);
+/* Average device duration of the block SpMV kernel with its fused dot product
+ * (one PCG iteration's q = A p) over `reps` back-to-back launches on the current
+ * matrix; precision 64 (FP64 values) or 32 (FP32 values).  Used to report the
+ * kernel's achieved bandwidth against the HBM roofline. */
+AMIE_API amie_status amie_profile_spmv(amie_topo *topo, int32_t precision, int32_t reps, double *ms_per_launch);
 
 /* Number of kernels this library has launched (process-wide counter). */
 AMIE_API uint64_t amie_kernel_launches(void);

@@ -144,6 +144,25 @@ def test_pcg_mixed(golden_topos, name):
     assert rel(x[s], xo[s]) <= max(NODE_TOL.get(name, 1e-8), 1e-8)
 
 
+AMIE_U_TOL = {"voxel_t4": 1e-6}
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_amie_cg_semantics(golden_topos, name):
+    """ConjugateGradient::solve semantics: the reference's iteration count and displacements."""
+    import amie_gpu
+    d, m, t = golden_topos[name]
+    ids, vals, kinds = am.golden_bcs(d)
+    t.assemble()
+    t.apply_dirichlet(ids, vals, kinds)
+    x, st = t.solve(amie_gpu.SOLVER_AMIE_CG, eps=float(d["epsilon"][0]), nssor=int(d["nssor"][0]))
+    assert abs(st["iterations"] - int(d["cg_iterations"][0])) <= 3
+    assert rel(x, d["u"]) <= AMIE_U_TOL.get(name, 1e-9)
+    xo, ito, rc = O.cg_amie(m.stride, d["row_size"], d["column_index"], d["array"], d["rhs"],
+                            eps=float(d["epsilon"][0]), nssor=int(d["nssor"][0]))
+    assert abs(st["iterations"] - ito) <= 3
+
+
 def test_solve_is_deterministic(golden_topos):
     import amie_gpu
     d, m, t = golden_topos["incl_p2"]
@@ -208,9 +227,9 @@ def test_nan_rhs_reports_nan(gpu_ctx):
     m = am.from_golden(d, "tabulated")
     t = amie_gpu.Topology(gpu_ctx, m)
     t.assemble()
-    rhs0 = np.zeros(t.n)
-    rhs0[7] = np.nan
     ids, vals, kinds = am.golden_bcs(d)
+    rhs0 = np.zeros(t.n)
+    rhs0[np.setdiff1d(np.arange(t.n), ids)[0]] = np.nan   # a free DOF: elimination keeps it
     t.apply_dirichlet(ids, vals, kinds, rhs0=rhs0)
     with pytest.raises(amie_gpu.AmieError) as ei:
         t.solve(amie_gpu.SOLVER_PCG_FP64)

@@ -32,7 +32,8 @@ EXPORTED = [
     "amie_topology_destroy", "amie_topology_sizes", "amie_topology_pattern", "amie_assemble", "amie_set_cscale",
     "amie_element_matrices", "amie_apply_dirichlet", "amie_matrix_download", "amie_spmv", "amie_solve",
     "amie_solve_resident", "amie_solution_download", "amie_server_start", "amie_submit", "amie_poll",
-    "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches",
+    "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
+    "amie_timer_stop", "amie_profile_spmv",
 ]
 
 
@@ -140,6 +141,15 @@ class Context:
         check(lib().amie_ctx_create(C.byref(_Config(device, hbm_budget_bytes, verbose)), C.byref(self.ptr)),
               "amie_ctx_create")
 
+    def timer_start(self):
+        check(lib().amie_timer_start(self.ptr), "amie_timer_start")
+
+    def timer_stop(self) -> float:
+        """Milliseconds of device time on the context's stream since timer_start."""
+        ms = C.c_double()
+        check(lib().amie_timer_stop(self.ptr, C.byref(ms)), "amie_timer_stop")
+        return ms.value
+
     def close(self):
         if self.ptr:
             lib().amie_ctx_destroy(self.ptr)
@@ -238,6 +248,68 @@ class Topology:
         x = np.zeros(self.n, np.float64)
         check(lib().amie_solution_download(self.ptr, _p(x)), "amie_solution_download")
         return x
+
+    def profile_spmv(self, precision: int = 64, reps: int = 20) -> float:
+        """Average device milliseconds of one q = A p (+ p.q) launch."""
+        ms = C.c_double()
+        check(lib().amie_profile_spmv(self.ptr, C.c_int32(precision), C.c_int32(reps), C.byref(ms)),
+              "amie_profile_spmv")
+        return ms.value
+
+
+class Server:
+    """Continuous-batching solve server (amie_server_* of the C-ABI)."""
+
+    def __init__(self, ctx: Context, solver=SOLVER_PCG_MIXED, rtol=1e-10, hbm_budget_bytes=0, max_slots=0):
+        self.ctx = ctx
+        self.ptr = C.c_void_p()
+        cfg = ServerConfig(solver, rtol, hbm_budget_bytes, max_slots, 0)
+        check(lib().amie_server_start(ctx.ptr, C.byref(cfg), C.byref(self.ptr)), "amie_server_start")
+        self._keep = {}
+        self._n = {}
+
+    def submit(self, m: am.MeshData, bc_ids, bc_values, bc_kinds=None, x0=None) -> int:
+        ms = mesh_struct(m)
+        ids = np.ascontiguousarray(bc_ids, np.uint32)
+        vals = np.ascontiguousarray(bc_values, np.float64)
+        kinds = None if bc_kinds is None else np.ascontiguousarray(bc_kinds, np.uint8)
+        x0a = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+        req = Request(C.cast(C.pointer(ms), C.c_void_p), len(ids), _p(ids), _p(vals), _p(kinds), _p(x0a))
+        t = C.c_uint64()
+        check(lib().amie_submit(self.ptr, C.byref(req), C.byref(t)), "amie_submit")
+        self._n[t.value] = (int(max(m.ndofmax, int(m.dof_ids.max()) + 1)) * m.stride)
+        return t.value
+
+    def poll(self, ticket: int, want_x: bool = True):
+        """None while running; else (result dict, solution or None)."""
+        res = Result()
+        x = np.zeros(self._n.get(ticket, 0), np.float64) if want_x else None
+        rc = lib().amie_poll(self.ptr, C.c_uint64(ticket), C.byref(res), _p(x) if want_x else None)
+        if rc == AMIE_NOT_READY:
+            return None
+        if rc not in (AMIE_OK, AMIE_CANCELLED):
+            check(rc, "amie_poll")
+        d = {k: getattr(res, k) for k, _ in Result._fields_}
+        if x is not None and res.n:
+            x = x[:res.n]
+        return d, x
+
+    def cancel(self, ticket: int):
+        check(lib().amie_cancel(self.ptr, C.c_uint64(ticket)), "amie_cancel")
+
+    def drain(self, timeout_s: float = 0.0) -> int:
+        return int(lib().amie_server_drain(self.ptr, C.c_double(timeout_s)))
+
+    def stop(self):
+        if self.ptr:
+            lib().amie_server_stop(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
 
 
 class Assembly:

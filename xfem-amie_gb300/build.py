@@ -17,7 +17,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libamie_gpu.so")
-SOURCES = ["common.cu", "assemble.cu", "solver.cu", "amie_cg.cu", "server.cu"]
+SOURCES = ["common.cu", "assemble.cu", "solver.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I", os.path.join(REPO, "include"), "-I", CSRC]
@@ -58,6 +58,22 @@ def build(force: bool = False, extra=()) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr[-4000:]}")
     return LIB
+
+
+def build_cpp_test() -> str:
+    """The C++ driver of gpu::Assembly used by tests/test_cpp_assembly.py."""
+    lib = build()
+    exe = os.path.join(BUILD, "test_gpu_assembly")
+    srcs = [os.path.join(HERE, "host", "gpu_assembly.cpp"), os.path.join(REPO, "tests", "cpp", "test_gpu_assembly.cpp")]
+    if os.path.exists(exe) and all(os.path.getmtime(s) < os.path.getmtime(exe) for s in srcs + [lib]):
+        return exe
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-I", os.path.join(REPO, "include"), "-I", os.path.join(HERE, "host"), *srcs,
+           "-L", HERE, "-lamie_gpu", f"-Wl,-rpath,{HERE}", "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed:\n{r.stderr[-4000:]}")
+    return exe
 
 
 if __name__ == "__main__":

@@ -896,11 +896,24 @@ amie_status dirichlet_async(amie_topo *t, uint32_t n_bc, const uint32_t *ids_dev
 
 }  // namespace amie
 
+namespace amie {
+
+// Elimination with the stored multipliers (after a fresh gather).
+amie_status reapply_dirichlet_async(amie_topo *t)
+{
+    cudaStream_t st = t->ctx->stream;
+    if (t->has_rhs0) AMIE_CUDA(cudaMemcpyAsync(t->rhs.p, t->rhs0.p, t->n * 8, cudaMemcpyDeviceToDevice, st));
+    return dirichlet_async(t, t->n_bc, t->bc_ids.p, t->bc_vals.p, t->has_bc_kinds ? t->bc_kinds.p : nullptr);
+}
+
+}  // namespace amie
+
 extern "C" amie_status amie_assemble(amie_topo *t)
 {
     if (!t) return AMIE_BAD_INPUT;
     AMIE_CUDA(cudaSetDevice(t->ctx->device));
     AMIE_TRY(assemble_async(t));
+    if (t->bc_set) AMIE_TRY(reapply_dirichlet_async(t));
     AMIE_TRY(finalize_matrix_async(t, false));
     AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
     return AMIE_OK;
@@ -963,15 +976,17 @@ extern "C" amie_status amie_apply_dirichlet(amie_topo *t, uint32_t n_bc, const u
     if (t->eliminated) {   // re-eliminating needs the original matrix
         AMIE_TRY(assemble_async(t));
     }
-    if (rhs0) AMIE_CUDA(cudaMemcpyAsync(t->rhs.p, rhs0, t->n * 8, cudaMemcpyHostToDevice, st));
+    AMIE_CUDA(cudaStreamSynchronize(st));   // the stored multipliers may be replaced below
+    t->n_bc = n_bc;
+    AMIE_TRY(upload(t->ctx, t->bc_ids, ids, n_bc));
+    AMIE_TRY(upload(t->ctx, t->bc_vals, values, n_bc));
+    t->has_bc_kinds = kinds != nullptr;
+    if (kinds) AMIE_TRY(upload(t->ctx, t->bc_kinds, kinds, n_bc));
+    t->has_rhs0 = rhs0 != nullptr;
+    if (rhs0) AMIE_TRY(upload(t->ctx, t->rhs0, rhs0, t->n));
     else AMIE_CUDA(cudaMemsetAsync(t->rhs.p, 0, t->n * 8, st));
-    DevArray<uint32_t> d_ids;
-    DevArray<double> d_vals;
-    DevArray<uint8_t> d_kinds;
-    AMIE_TRY(upload(t->ctx, d_ids, ids, n_bc));
-    AMIE_TRY(upload(t->ctx, d_vals, values, n_bc));
-    if (kinds) AMIE_TRY(upload(t->ctx, d_kinds, kinds, n_bc));
-    AMIE_TRY(dirichlet_async(t, n_bc, d_ids.p, d_vals.p, kinds ? d_kinds.p : nullptr));
+    t->bc_set = true;
+    AMIE_TRY(reapply_dirichlet_async(t));
     AMIE_TRY(finalize_matrix_async(t, false));
     AMIE_CUDA(cudaStreamSynchronize(st));
     return AMIE_OK;

@@ -155,6 +155,14 @@ struct amie_topo {
     amie::DevArray<float> r32, z32, p32, q32, d32;
     amie::DevArray<uint8_t> fixed;
     amie::DevArray<double> fixval;
+    // Dirichlet / force multipliers and initial forces of the last
+    // amie_apply_dirichlet; re-applied by every amie_assemble (make_final does
+    // scatter + setBoundaryConditions in one call, solvers/assembly.cpp:803-816).
+    amie::DevArray<uint32_t> bc_ids;
+    amie::DevArray<double> bc_vals, rhs0;
+    amie::DevArray<uint8_t> bc_kinds;
+    uint32_t n_bc = 0;
+    bool bc_set = false, has_rhs0 = false, has_bc_kinds = false;
     amie::DevArray<double> scal;   // solver scalars
     amie::DevArray<int32_t> flags; // solver control flags
 

@@ -1,0 +1,834 @@
+// server.cuh -- continuous-batching solve server, included by solver.cu.
+//
+// Requests (independent meshes: microstructure or damage-step solves of
+// uneven size) are admitted while others run, as slots and the HBM budget
+// allow.  Admission (upload, pattern + scatter map, element matrices, gather,
+// Dirichlet elimination) runs on its own stream, overlapping the solves.
+// Every admitted solve keeps its matrix, scatter map and warm-start vector on
+// the device.  All solves in the batch advance together: one CUDA graph holds
+// kBatchIters Jacobi-PCG iterations over every active slot, each kernel
+// covering all slots through a CTA -> slot map (CTAs split between slots in
+// proportion to their size, so each slot's reductions are its own CTAs'
+// partials: deterministic, and the same alone and in a mix).  A slot whose
+// inner solve has converged stops doing work inside the graph; between graph
+// launches the host refines it in FP64 (mixed precision) or retires it.
+// There is no device-side waiting anywhere: the host decides between launches.
+#pragma once
+
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <thread>
+
+namespace amie {
+
+constexpr int kBatchIters = 16;
+
+// Device view of one slot.
+struct SlotDesc {
+    BsrView<float> A32;      // inner matrix (FP32 values) -- or FP64 below
+    BsrView<double> A64;
+    const float *dinv32;
+    const double *dinv64;
+    float *d32, *r32, *z32, *p32, *q32;   // inner vectors (mixed)
+    double *x64, *r64, *z64, *p64, *q64;  // FP64 vectors
+    uint64_t n;
+    int32_t c0, c1;          // CTA range in the batch grid
+    int32_t active;          // 1 = iterate
+    int32_t mixed;
+};
+
+struct SlotCtl {
+    int32_t done;            // inner run finished (converged or capped)
+    int32_t pad;
+    int64_t iterations;      // inner iterations of the current run
+    int64_t maxit;
+    double tol2;
+    double rr;
+};
+
+__device__ __forceinline__ double slot_sum(const double *parts, int c0, int c1, double *sh)
+{
+    double v = 0.0;
+    for (int i = c0 + threadIdx.x; i < c1; i += kVecThreads) v += parts[i];
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) sh[32] = v;
+    __syncthreads();
+    const double r = sh[32];
+    __syncthreads();
+    return r;
+}
+
+template <typename T>
+__device__ __forceinline__ BsrView<T> slot_A(const SlotDesc &d);
+template <>
+__device__ __forceinline__ BsrView<float> slot_A<float>(const SlotDesc &d) { return d.A32; }
+template <>
+__device__ __forceinline__ BsrView<double> slot_A<double>(const SlotDesc &d) { return d.A64; }
+
+template <typename T>
+struct SlotVecs {
+    const T *dinv;
+    T *x, *r, *z, *p, *q;
+};
+template <typename T>
+__device__ __forceinline__ SlotVecs<T> slot_vecs(const SlotDesc &d);
+template <>
+__device__ __forceinline__ SlotVecs<float> slot_vecs<float>(const SlotDesc &d)
+{
+    return SlotVecs<float>{d.dinv32, d.d32, d.r32, d.z32, d.p32, d.q32};
+}
+template <>
+__device__ __forceinline__ SlotVecs<double> slot_vecs<double>(const SlotDesc &d)
+{
+    return SlotVecs<double>{d.dinv64, d.x64, d.r64, d.z64, d.p64, d.q64};
+}
+
+// Batched kernel A: q = A p per slot, partial p.q per CTA.
+template <typename T, int G>
+__global__ void __launch_bounds__(kVecThreads) kb_spmv_pq(const SlotDesc *slots, const int16_t *cta_slot,
+                                                          const SlotCtl *ctl, double *part_pq)
+{
+    __shared__ double sh[33];
+    const int s = cta_slot[blockIdx.x];
+    if (s < 0) return;
+    const SlotDesc d = slots[s];
+    if (!d.active || ctl[s].done) return;
+    constexpr int RPB = kVecThreads / G;
+    const int lane = threadIdx.x % G;
+    const BsrView<T> A = slot_A<T>(d);
+    const SlotVecs<T> v = slot_vecs<T>(d);
+    const int lc = blockIdx.x - d.c0, nc = d.c1 - d.c0;
+    double dot = 0.0;
+    for (uint32_t base = lc * RPB; base < A.n_rows; base += nc * RPB) {
+        const uint32_t row = base + threadIdx.x / G;
+        const bool valid = row < A.n_rows;
+        T acc[2];
+        row_spmv<2, G, T>(A, v.p, row, valid, lane, acc);
+        if (valid && lane == 0) {
+            v.q[(uint64_t)row * 2] = acc[0];
+            v.q[(uint64_t)row * 2 + 1] = acc[1];
+            dot += (double)acc[0] * (double)v.p[(uint64_t)row * 2] + (double)acc[1] * (double)v.p[(uint64_t)row * 2 + 1];
+        }
+    }
+    dot = block_sum(dot, sh);
+    if (threadIdx.x == 0) part_pq[blockIdx.x] = dot;
+}
+
+// Batched kernel B: per-slot alpha, update, partials r.z and r.r.
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) kb_update(const SlotDesc *slots, const int16_t *cta_slot, SlotCtl *ctl,
+                                                         const double *part_pq, double *part_rz0, double *part_rz1,
+                                                         double *part_rr, int parity)
+{
+    __shared__ double sh[33];
+    const int s = cta_slot[blockIdx.x];
+    if (s < 0) return;
+    const SlotDesc d = slots[s];
+    if (!d.active || ctl[s].done) return;
+    double *rz_new = parity ? part_rz1 : part_rz0;
+    const double *rz_old = parity ? part_rz0 : part_rz1;
+    const double pq = slot_sum(part_pq, d.c0, d.c1, sh);
+    const double rz = slot_sum(rz_old, d.c0, d.c1, sh);
+    const double alpha = pq != 0.0 ? rz / pq : 0.0;
+    const T a = (T)alpha;
+    const SlotVecs<T> v = slot_vecs<T>(d);
+    const int lc = blockIdx.x - d.c0, nc = d.c1 - d.c0;
+    double drz = 0.0, drr = 0.0;
+    for (uint64_t i = (uint64_t)lc * kVecThreads + threadIdx.x; i < d.n; i += (uint64_t)nc * kVecThreads) {
+        const T ri = v.r[i] - a * v.q[i];
+        v.x[i] += a * v.p[i];
+        v.r[i] = ri;
+        const T zi = ri * v.dinv[i];
+        v.z[i] = zi;
+        drz += (double)ri * (double)zi;
+        drr += (double)ri * (double)ri;
+    }
+    drz = block_sum(drz, sh);
+    drr = block_sum(drr, sh);
+    if (threadIdx.x == 0) {
+        rz_new[blockIdx.x] = drz;
+        part_rr[blockIdx.x] = drr;
+        if (blockIdx.x == d.c0) ctl[s].iterations += 1;
+    }
+}
+
+// Batched kernel C: per-slot stop test, beta, p = z + beta p.
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) kb_direction(const SlotDesc *slots, const int16_t *cta_slot, SlotCtl *ctl,
+                                                            const double *part_rz0, const double *part_rz1,
+                                                            const double *part_rr, int parity)
+{
+    __shared__ double sh[33];
+    const int s = cta_slot[blockIdx.x];
+    if (s < 0) return;
+    const SlotDesc d = slots[s];
+    if (!d.active || ctl[s].done) return;
+    const double *rz_new = parity ? part_rz1 : part_rz0;
+    const double *rz_old = parity ? part_rz0 : part_rz1;
+    const double rzn = slot_sum(rz_new, d.c0, d.c1, sh);
+    const double rzo = slot_sum(rz_old, d.c0, d.c1, sh);
+    const double rr = slot_sum(part_rr, d.c0, d.c1, sh);
+    const bool stop = rr <= ctl[s].tol2 || ctl[s].iterations >= ctl[s].maxit || !(rr == rr);
+    if (stop) {
+        if (blockIdx.x == d.c0 && threadIdx.x == 0) {
+            ctl[s].done = 1;
+            ctl[s].rr = rr;
+        }
+        return;
+    }
+    const T bt = (T)(rzo != 0.0 ? rzn / rzo : 0.0);
+    const SlotVecs<T> v = slot_vecs<T>(d);
+    const int lc = blockIdx.x - d.c0, nc = d.c1 - d.c0;
+    for (uint64_t i = (uint64_t)lc * kVecThreads + threadIdx.x; i < d.n; i += (uint64_t)nc * kVecThreads)
+        v.p[i] = v.z[i] + bt * v.p[i];
+}
+
+// Start of an inner run of one slot: z = D^-1 r, p = z, partials r.z -> rz[1], r.r.
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) kb_start(SlotDesc d, double *part_rz1, double *part_rr)
+{
+    __shared__ double sh[33];
+    const SlotVecs<T> v = slot_vecs<T>(d);
+    const int nc = d.c1 - d.c0;
+    double drz = 0.0, drr = 0.0;
+    for (uint64_t i = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x; i < d.n; i += (uint64_t)nc * kVecThreads) {
+        const T ri = v.r[i];
+        const T zi = ri * v.dinv[i];
+        v.z[i] = zi;
+        v.p[i] = zi;
+        drz += (double)ri * (double)zi;
+        drr += (double)ri * (double)ri;
+    }
+    drz = block_sum(drz, sh);
+    drr = block_sum(drr, sh);
+    if (threadIdx.x == 0) {
+        part_rz1[d.c0 + blockIdx.x] = drz;
+        part_rr[d.c0 + blockIdx.x] = drr;
+    }
+}
+
+}  // namespace amie
+
+// ------------------------------------------------------------------ host side
+
+struct amie_server {
+    amie_ctx *ctx = nullptr;        // solve stream
+    amie_ctx *adm = nullptr;        // admission stream
+    amie_server_config cfg{};
+    bool mixed = true;
+    int grid = 0, group = 8;
+    uint64_t budget = 0;
+    std::atomic<uint64_t> in_use{0};
+
+    struct Req {
+        uint64_t ticket;
+        // deep copies of the request arrays
+        std::vector<uint8_t> kind, moved, enr_type, enr_vertex, bc_kinds;
+        std::vector<uint32_t> dof_ptr, dof_ids, gp_ptr, mat, enr_ptr, enr_data, bc_ids;
+        std::vector<double> gp, jinv, jinv_gp, cmat, cscale, scale, enr_grad, bc_vals, x0;
+        std::vector<int8_t> enr_jump;
+        amie_mesh mesh{};
+        uint64_t footprint = 0;
+        double t_submit = 0, t_admit = 0, t_done = 0;
+        amie_topo *topo = nullptr;
+        int slot = -1;
+        double bnorm = 0, rnorm = 0;
+        int64_t iterations = 0;
+        int refinements = 0;
+        amie_status status = AMIE_NOT_READY;
+        bool cancelled = false;
+        std::vector<double> x;   // result
+        double relres = 0;
+    };
+
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Req *> pending;
+    std::map<uint64_t, Req *> all;
+    uint64_t next_ticket = 1;
+    bool running = false, stop_flag = false;
+    std::thread worker;
+
+    // batch state
+    std::vector<Req *> slot_req;                 // per slot
+    amie::DevArray<amie::SlotDesc> d_slots;
+    amie::DevArray<amie::SlotCtl> d_ctl;
+    amie::DevArray<int16_t> d_cta_slot;
+    amie::DevArray<double> d_parts;              // pq | rz0 | rz1 | rr, grid each
+    amie::SlotDesc *h_slots = nullptr;           // pinned
+    amie::SlotCtl *h_ctl = nullptr;              // pinned
+    int16_t *h_cta_slot = nullptr;               // pinned
+    cudaGraphExec_t graph = nullptr;
+    std::string error;
+};
+
+namespace amie {
+
+inline double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+template <typename T>
+static void copy_vec(std::vector<T> &dst, const T *src, size_t n)
+{
+    if (src) dst.assign(src, src + n);
+    else dst.clear();
+}
+
+// Device bytes a request needs: staged element blocks, pattern keys and sort
+// scratch, matrix (FP64 + FP32), scatter map, vectors, element data.
+static uint64_t request_footprint(const amie_mesh &m)
+{
+    uint64_t blocks = 0;
+    for (uint32_t e = 0; e < m.n_elem; e++) {
+        const uint64_t nf = m.dof_ptr[e + 1] - m.dof_ptr[e];
+        blocks += nf * nf;
+    }
+    const uint64_t s2 = (uint64_t)m.stride * m.stride;
+    const uint64_t rows = m.ndofmax ? m.ndofmax : 1;
+    const uint64_t n = rows * m.stride;
+    return blocks * (s2 * 8 + 48) + blocks * (s2 * 12 + 8) + n * 8 * 16 + (uint64_t)m.n_elem * 64 +
+           (uint64_t)m.gp_ptr[m.n_elem] * 64 + (16u << 20);
+}
+
+struct ServerOps {
+    static amie_status fail_req(amie_server *srv, amie_server::Req *r, amie_status st)
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        r->status = st;
+        r->t_done = now_s();
+        srv->cv.notify_all();
+        return AMIE_OK;
+    }
+
+    static amie_status read_sum_on(cudaStream_t st, const double *dev, int n, double *out)
+    {
+        std::vector<double> h(n);
+        AMIE_CUDA(cudaMemcpyAsync(h.data(), dev, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+        double s = 0.0;
+        for (int i = 0; i < n; i++) s += h[i];
+        *out = s;
+        return AMIE_OK;
+    }
+
+    // Upload + pattern + element matrices + gather + elimination on the admission stream,
+    // then the initial FP64 residual.
+    static amie_status admit(amie_server *srv, amie_server::Req *r)
+    {
+        amie_topo *t = nullptr;
+        AMIE_TRY(amie_topology_build(srv->adm, &r->mesh, &t));
+        r->topo = t;
+        if (t->s != 2) {
+            set_error("the server batches 2D meshes only");
+            return AMIE_BAD_INPUT;
+        }
+        AMIE_TRY(amie_assemble(t));
+        const uint8_t *kinds = r->bc_kinds.empty() ? nullptr : r->bc_kinds.data();
+        AMIE_TRY(amie_apply_dirichlet(t, (uint32_t)r->bc_ids.size(), r->bc_ids.data(), r->bc_vals.data(), kinds,
+                                      nullptr));
+        SolverState *s = nullptr;
+        AMIE_TRY(ensure_state(t, srv->mixed, &s));
+        if (srv->mixed) AMIE_TRY(finalize_matrix_async(t, true));
+        cudaStream_t st = srv->adm->stream;
+        if (!r->x0.empty() && r->x0.size() == t->n)
+            AMIE_CUDA(cudaMemcpyAsync(t->x.p, r->x0.data(), t->n * 8, cudaMemcpyHostToDevice, st));
+        else
+            AMIE_CUDA(cudaMemsetAsync(t->x.p, 0, t->n * 8, st));
+        k_norm2_parts<<<s->grid, kVecThreads, 0, st>>>(t->n, t->rhs.p, s->parts.p);
+        AMIE_LAUNCHED();
+        double bb = 0.0, rr = 0.0;
+        AMIE_TRY(read_sum_on(st, s->parts.p, s->grid, &bb));
+        launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->grid, st);
+        AMIE_TRY(read_sum_on(st, s->parts.p + 3 * s->grid, s->grid, &rr));
+        r->bnorm = std::sqrt(bb);
+        r->rnorm = std::sqrt(rr);
+        return AMIE_OK;
+    }
+
+    // CTA allocator over the batch grid: first fit of `count` contiguous CTAs.
+    static int alloc_ctas(amie_server *srv, int count)
+    {
+        int run = 0;
+        for (int c = 0; c < srv->grid; c++) {
+            run = srv->h_cta_slot[c] < 0 ? run + 1 : 0;
+            if (run == count) return c - count + 1;
+        }
+        return -1;
+    }
+
+    static int ctas_for(uint64_t n_rows)
+    {
+        const uint64_t per = (uint64_t)(kVecThreads / 8) * 8;   // 8 row passes of 32 rows
+        return (int)std::max<uint64_t>(1, std::min<uint64_t>(128, (n_rows + per - 1) / per));
+    }
+
+    static void fill_desc(amie_server *srv, int slot, amie_topo *t, int c0, int c1)
+    {
+        SlotDesc &d = srv->h_slots[slot];
+        d.A64 = bsr64(t);
+        d.A32 = t->val32.p ? bsr32(t) : BsrView<float>{t->n_rows, t->row_ptr.p, t->col.p, nullptr};
+        d.dinv32 = t->invdiag32.p;
+        d.dinv64 = t->invdiag.p;
+        d.d32 = t->d32.p; d.r32 = t->r32.p; d.z32 = t->z32.p; d.p32 = t->p32.p; d.q32 = t->q32.p;
+        d.x64 = t->x.p; d.r64 = t->r.p; d.z64 = t->z.p; d.p64 = t->p.p; d.q64 = t->q.p;
+        d.n = t->n;
+        d.c0 = c0;
+        d.c1 = c1;
+        d.active = 1;
+        d.mixed = srv->mixed ? 1 : 0;
+    }
+
+    // Start (or restart) the inner run of a slot from its FP64 residual r64 (norm rnorm).
+    static amie_status start_inner(amie_server *srv, int slot, amie_server::Req *r)
+    {
+        cudaStream_t st = srv->ctx->stream;
+        amie_topo *t = r->topo;
+        const SlotDesc &d = srv->h_slots[slot];
+        const int nc = d.c1 - d.c0;
+        double *pq = srv->d_parts.p, *rz1 = srv->d_parts.p + 2 * srv->grid, *rr = srv->d_parts.p + 3 * srv->grid;
+        (void)pq;
+        SlotCtl c{};
+        c.done = 0;
+        c.iterations = 0;
+        const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
+        c.maxit = std::max<int64_t>(1, maxit - r->iterations);
+        if (srv->mixed) {
+            k_scale_to_f32<<<nc, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / r->rnorm, t->r32.p, t->d32.p);
+            kb_start<float><<<nc, kVecThreads, 0, st>>>(d, rz1, rr);
+            const double inner = 1e-5;
+            c.tol2 = inner * inner;
+        } else {
+            kb_start<double><<<nc, kVecThreads, 0, st>>>(d, rz1, rr);
+            const double target = srv->cfg.rtol * r->bnorm;
+            c.tol2 = 0.25 * target * target;
+        }
+        g_launches += 2;
+        srv->h_ctl[slot] = c;
+        AMIE_CUDA(cudaMemcpyAsync(srv->d_ctl.p + slot, srv->h_ctl + slot, sizeof(SlotCtl), cudaMemcpyHostToDevice, st));
+        AMIE_CUDA(cudaMemcpyAsync(srv->d_slots.p + slot, srv->h_slots + slot, sizeof(SlotDesc), cudaMemcpyHostToDevice, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+        return AMIE_OK;
+    }
+
+    static amie_status join(amie_server *srv, amie_server::Req *r)
+    {
+        int slot = -1;
+        for (size_t i = 0; i < srv->slot_req.size(); i++)
+            if (!srv->slot_req[i]) { slot = (int)i; break; }
+        if (slot < 0) return AMIE_NOT_READY;
+        const int count = ctas_for(r->topo->n_rows);
+        const int c0 = alloc_ctas(srv, count);
+        if (c0 < 0) return AMIE_NOT_READY;
+        for (int c = c0; c < c0 + count; c++) srv->h_cta_slot[c] = (int16_t)slot;
+        srv->slot_req[slot] = r;
+        r->slot = slot;
+        fill_desc(srv, slot, r->topo, c0, c0 + count);
+        cudaStream_t st = srv->ctx->stream;
+        AMIE_CUDA(cudaMemcpyAsync(srv->d_cta_slot.p, srv->h_cta_slot, srv->grid * sizeof(int16_t), cudaMemcpyHostToDevice, st));
+        if (r->rnorm <= srv->cfg.rtol * r->bnorm || r->bnorm == 0.0) {   // already converged (warm start)
+            srv->h_slots[slot].active = 0;
+            AMIE_CUDA(cudaMemcpyAsync(srv->d_slots.p + slot, srv->h_slots + slot, sizeof(SlotDesc), cudaMemcpyHostToDevice, st));
+            AMIE_CUDA(cudaStreamSynchronize(st));
+            return retire(srv, r, AMIE_OK);
+        }
+        return start_inner(srv, slot, r);
+    }
+
+    static amie_status retire(amie_server *srv, amie_server::Req *r, amie_status result)
+    {
+        cudaStream_t st = srv->ctx->stream;
+        amie_topo *t = r->topo;
+        if (t && result != AMIE_CANCELLED) {
+            r->x.resize(t->n);
+            AMIE_CUDA(cudaMemcpyAsync(r->x.data(), t->x.p, t->n * 8, cudaMemcpyDeviceToHost, st));
+            AMIE_CUDA(cudaStreamSynchronize(st));
+        }
+        if (r->slot >= 0) {
+            const int slot = r->slot;
+            for (int c = 0; c < srv->grid; c++)
+                if (srv->h_cta_slot[c] == slot) srv->h_cta_slot[c] = -1;
+            srv->h_slots[slot].active = 0;
+            AMIE_CUDA(cudaMemcpyAsync(srv->d_slots.p + slot, srv->h_slots + slot, sizeof(SlotDesc), cudaMemcpyHostToDevice, st));
+            AMIE_CUDA(cudaMemcpyAsync(srv->d_cta_slot.p, srv->h_cta_slot, srv->grid * sizeof(int16_t), cudaMemcpyHostToDevice, st));
+            AMIE_CUDA(cudaStreamSynchronize(st));
+            srv->slot_req[slot] = nullptr;
+            r->slot = -1;
+        }
+        if (t) {
+            amie_topology_destroy(t);
+            r->topo = nullptr;
+        }
+        srv->in_use -= r->footprint;
+        std::lock_guard<std::mutex> lk(srv->mu);
+        r->status = result;
+        r->relres = r->bnorm > 0 ? r->rnorm / r->bnorm : 0.0;
+        r->t_done = now_s();
+        srv->cv.notify_all();
+        return AMIE_OK;
+    }
+
+    // A slot's inner run is finished: FP64 refinement step / true residual, then retire or restart.
+    static amie_status advance(amie_server *srv, int slot)
+    {
+        amie_server::Req *r = srv->slot_req[slot];
+        amie_topo *t = r->topo;
+        cudaStream_t st = srv->ctx->stream;
+        SolverState *s = state_of(t);
+        const SlotCtl &c = srv->h_ctl[slot];
+        r->iterations += c.iterations;
+        if (srv->mixed) {
+            k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, r->rnorm, t->x.p);
+            AMIE_LAUNCHED();
+            r->refinements++;
+        }
+        double rr = 0.0;
+        launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->grid, st);
+        AMIE_TRY(read_sum_on(st, s->parts.p + 3 * s->grid, s->grid, &rr));
+        r->rnorm = std::sqrt(rr);
+        const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
+        if (!(rr == rr)) return retire(srv, r, AMIE_NAN);
+        if (r->rnorm <= srv->cfg.rtol * r->bnorm) return retire(srv, r, AMIE_OK);
+        if (r->iterations >= maxit || r->refinements > 100) return retire(srv, r, AMIE_NOT_CONVERGED);
+        return start_inner(srv, slot, r);
+    }
+
+    static amie_status capture(amie_server *srv)
+    {
+        cudaStream_t st = srv->ctx->stream;
+        double *pq = srv->d_parts.p, *rz0 = pq + srv->grid, *rz1 = pq + 2 * srv->grid, *rr = pq + 3 * srv->grid;
+        cudaGraph_t g;
+        AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < kBatchIters; it++) {
+            const int parity = it & 1;
+            if (srv->mixed) {
+                kb_spmv_pq<float, 8><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, pq);
+                kb_update<float><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, pq, rz0, rz1, rr, parity);
+                kb_direction<float><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, rz0, rz1, rr, parity);
+            } else {
+                kb_spmv_pq<double, 8><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, pq);
+                kb_update<double><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, pq, rz0, rz1, rr, parity);
+                kb_direction<double><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, rz0, rz1, rr, parity);
+            }
+        }
+        AMIE_CUDA(cudaStreamEndCapture(st, &g));
+        cudaError_t e = cudaGraphInstantiate(&srv->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+            return AMIE_CUDA_ERROR;
+        }
+        return AMIE_OK;
+    }
+
+    static bool any_active(amie_server *srv)
+    {
+        for (auto *r : srv->slot_req)
+            if (r) return true;
+        return false;
+    }
+
+    static void loop(amie_server *srv)
+    {
+        cudaSetDevice(srv->ctx->device);
+        std::vector<amie_server::Req *> admitted;
+        while (true) {
+            // 1. batch iterations in flight on the solve stream
+            const bool active = any_active(srv);
+            if (active) {
+                cudaGraphLaunch(srv->graph, srv->ctx->stream);
+                g_launches += 3 * kBatchIters;
+                cudaMemcpyAsync(srv->h_ctl, srv->d_ctl.p, srv->slot_req.size() * sizeof(SlotCtl), cudaMemcpyDeviceToHost,
+                                srv->ctx->stream);
+                cudaEventRecord(srv->ctx->ev1, srv->ctx->stream);
+            }
+            // 2. admission, overlapping the batch on the device
+            std::vector<amie_server::Req *> to_admit;
+            {
+                std::unique_lock<std::mutex> lk(srv->mu);
+                if (!active && srv->pending.empty() && admitted.empty()) {
+                    if (srv->stop_flag) break;
+                    srv->cv.wait_for(lk, std::chrono::milliseconds(2));
+                    continue;
+                }
+                size_t free_slots = 0;
+                for (auto *r : srv->slot_req)
+                    if (!r) free_slots++;
+                while (!srv->pending.empty() && to_admit.size() + admitted.size() < free_slots) {
+                    amie_server::Req *r = srv->pending.front();
+                    if (r->cancelled) {
+                        srv->pending.pop_front();
+                        r->status = AMIE_CANCELLED;
+                        r->t_done = now_s();
+                        continue;
+                    }
+                    if (r->footprint > srv->budget) {   // can never fit
+                        srv->pending.pop_front();
+                        r->status = AMIE_OOM;
+                        r->t_done = now_s();
+                        continue;
+                    }
+                    if (srv->in_use + r->footprint > srv->budget) break;   // wait for memory
+                    srv->pending.pop_front();
+                    srv->in_use += r->footprint;
+                    to_admit.push_back(r);
+                }
+                srv->cv.notify_all();
+            }
+            for (auto *r : to_admit) {
+                r->t_admit = now_s();
+                amie_status st = admit(srv, r);
+                if (st != AMIE_OK) {
+                    if (r->topo) {
+                        amie_topology_destroy(r->topo);
+                        r->topo = nullptr;
+                    }
+                    srv->in_use -= r->footprint;
+                    fail_req(srv, r, st);
+                } else {
+                    admitted.push_back(r);
+                }
+            }
+            // 3. batch results
+            if (active) {
+                cudaEventSynchronize(srv->ctx->ev1);
+                for (size_t i = 0; i < srv->slot_req.size(); i++) {
+                    amie_server::Req *r = srv->slot_req[i];
+                    if (!r) continue;
+                    if (r->cancelled) { retire(srv, r, AMIE_CANCELLED); continue; }
+                    if (srv->h_ctl[i].done) advance(srv, (int)i);
+                }
+            }
+            // 4. join admitted requests
+            std::vector<amie_server::Req *> waiting;
+            for (auto *r : admitted) {
+                amie_status st = join(srv, r);
+                if (st == AMIE_NOT_READY) waiting.push_back(r);
+                else if (st != AMIE_OK) fail_req(srv, r, st);
+            }
+            admitted.swap(waiting);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) {
+                srv->error = cudaGetErrorString(e);
+                std::lock_guard<std::mutex> lk(srv->mu);
+                for (auto &kv : srv->all)
+                    if (kv.second->status == AMIE_NOT_READY) kv.second->status = AMIE_CUDA_ERROR;
+                srv->cv.notify_all();
+                break;
+            }
+        }
+    }
+};
+
+}  // namespace amie
+
+extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config *cfg, amie_server **out)
+{
+    using namespace amie;
+    if (!ctx || !out) return AMIE_BAD_INPUT;
+    *out = nullptr;
+    AMIE_CUDA(cudaSetDevice(ctx->device));
+    amie_server *srv = new amie_server();
+    srv->ctx = ctx;
+    amie_server_config c{AMIE_SOLVER_PCG_MIXED, 1e-10, 0, 256, kBatchIters};
+    if (cfg) c = *cfg;
+    if (c.rtol <= 0) c.rtol = 1e-10;
+    if (c.max_slots <= 0) c.max_slots = 256;
+    c.max_slots = std::min(c.max_slots, 1024);
+    c.iters_per_launch = kBatchIters;
+    if (c.solver != AMIE_SOLVER_PCG_MIXED && c.solver != AMIE_SOLVER_PCG_FP64) {
+        delete srv;
+        set_error("server solver must be PCG_FP64 or PCG_MIXED");
+        return AMIE_BAD_INPUT;
+    }
+    srv->cfg = c;
+    srv->mixed = c.solver == AMIE_SOLVER_PCG_MIXED;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    srv->budget = c.hbm_budget_bytes ? c.hbm_budget_bytes : (uint64_t)(0.9 * free_b);
+    srv->grid = std::max(ctx->num_sms * 8, c.max_slots);
+    amie_config ac{ctx->device, 0, 0};
+    amie_status rc = amie_ctx_create(&ac, &srv->adm);
+    if (rc != AMIE_OK) {
+        delete srv;
+        return rc;
+    }
+    auto fail = [&](amie_status s) {
+        amie_ctx_destroy(srv->adm);
+        delete srv;
+        return s;
+    };
+    srv->slot_req.assign(c.max_slots, nullptr);
+    if ((rc = srv->d_slots.alloc(ctx, c.max_slots)) || (rc = srv->d_ctl.alloc(ctx, c.max_slots)) ||
+        (rc = srv->d_cta_slot.alloc(ctx, srv->grid)) || (rc = srv->d_parts.alloc(ctx, 4 * (size_t)srv->grid)))
+        return fail(rc);
+    if (cudaMallocHost((void **)&srv->h_slots, c.max_slots * sizeof(SlotDesc)) != cudaSuccess ||
+        cudaMallocHost((void **)&srv->h_ctl, c.max_slots * sizeof(SlotCtl)) != cudaSuccess ||
+        cudaMallocHost((void **)&srv->h_cta_slot, srv->grid * sizeof(int16_t)) != cudaSuccess)
+        return fail(AMIE_OOM);
+    std::memset(srv->h_slots, 0, c.max_slots * sizeof(SlotDesc));
+    std::memset(srv->h_ctl, 0, c.max_slots * sizeof(SlotCtl));
+    for (int i = 0; i < srv->grid; i++) srv->h_cta_slot[i] = -1;
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(srv->d_slots.p, srv->h_slots, c.max_slots * sizeof(SlotDesc), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(srv->d_ctl.p, srv->h_ctl, c.max_slots * sizeof(SlotCtl), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(srv->d_cta_slot.p, srv->h_cta_slot, srv->grid * sizeof(int16_t), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(srv->d_parts.p, 0, 4 * (size_t)srv->grid * 8, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(AMIE_CUDA_ERROR);
+    if ((rc = ServerOps::capture(srv)) != AMIE_OK) return fail(rc);
+    srv->running = true;
+    srv->worker = std::thread(ServerOps::loop, srv);
+    *out = srv;
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_submit(amie_server *srv, const amie_request *req, uint64_t *ticket)
+{
+    using namespace amie;
+    if (!srv || !req || !req->mesh || !ticket) return AMIE_BAD_INPUT;
+    const amie_mesh &m = *req->mesh;
+    if (m.n_elem == 0 || !m.dof_ptr || !m.kind || !m.gp_ptr) return AMIE_BAD_INPUT;
+    auto *r = new amie_server::Req();
+    const uint32_t E = m.n_elem;
+    const uint64_t ngp = m.gp_ptr[E];
+    const uint32_t nenr = m.enr_ptr ? m.enr_ptr[E] : 0;
+    const int d = m.dim;
+    const int nv = d == 2 ? 3 : 6;
+    copy_vec(r->kind, m.kind, E);
+    copy_vec(r->dof_ptr, m.dof_ptr, E + 1);
+    copy_vec(r->dof_ids, m.dof_ids, m.dof_ptr[E]);
+    copy_vec(r->gp_ptr, m.gp_ptr, E + 1);
+    copy_vec(r->gp, m.gp, ngp * (d + 1));
+    copy_vec(r->jinv, m.jinv, (size_t)E * d * d);
+    copy_vec(r->moved, m.moved, m.moved ? E : 0);
+    copy_vec(r->jinv_gp, m.jinv_gp, m.jinv_gp ? ngp * d * d : 0);
+    copy_vec(r->mat, m.mat, E);
+    copy_vec(r->cmat, m.cmat_table, (size_t)m.n_mat * nv * nv);
+    copy_vec(r->cscale, m.cscale, m.cscale ? E : 0);
+    copy_vec(r->scale, m.scale, m.scale ? E : 0);
+    if (m.enr_ptr) {
+        copy_vec(r->enr_ptr, m.enr_ptr, E + 1);
+        copy_vec(r->enr_type, m.enr_type, nenr);
+        copy_vec(r->enr_vertex, m.enr_vertex, nenr);
+        copy_vec(r->enr_data, m.enr_data, nenr);
+        copy_vec(r->enr_jump, m.enr_jump, m.enr_jump ? m.n_enr_gp : 0);
+        copy_vec(r->enr_grad, m.enr_grad, m.enr_grad ? m.n_enr_gp * d : 0);
+    }
+    copy_vec(r->bc_ids, req->bc_ids, req->n_bc);
+    copy_vec(r->bc_vals, req->bc_values, req->n_bc);
+    copy_vec(r->bc_kinds, req->bc_kinds, req->bc_kinds ? req->n_bc : 0);
+    r->mesh = m;
+    r->mesh.kind = r->kind.data();
+    r->mesh.dof_ptr = r->dof_ptr.data();
+    r->mesh.dof_ids = r->dof_ids.data();
+    r->mesh.gp_ptr = r->gp_ptr.data();
+    r->mesh.gp = r->gp.empty() ? nullptr : r->gp.data();
+    r->mesh.jinv = r->jinv.data();
+    r->mesh.moved = r->moved.empty() ? nullptr : r->moved.data();
+    r->mesh.jinv_gp = r->jinv_gp.empty() ? nullptr : r->jinv_gp.data();
+    r->mesh.mat = r->mat.data();
+    r->mesh.cmat_table = r->cmat.data();
+    r->mesh.cscale = r->cscale.empty() ? nullptr : r->cscale.data();
+    r->mesh.scale = r->scale.empty() ? nullptr : r->scale.data();
+    if (m.enr_ptr) {
+        r->mesh.enr_ptr = r->enr_ptr.data();
+        r->mesh.enr_type = r->enr_type.data();
+        r->mesh.enr_vertex = r->enr_vertex.data();
+        r->mesh.enr_data = r->enr_data.data();
+        r->mesh.enr_jump = r->enr_jump.empty() ? nullptr : r->enr_jump.data();
+        r->mesh.enr_grad = r->enr_grad.empty() ? nullptr : r->enr_grad.data();
+    }
+    uint32_t max_id = 0;
+    for (uint32_t k : r->dof_ids) max_id = std::max(max_id, k);
+    if (!r->mesh.ndofmax) r->mesh.ndofmax = max_id + 1;
+    if (req->x0) r->x0.assign(req->x0, req->x0 + (size_t)std::max(r->mesh.ndofmax, max_id + 1) * m.stride);
+    r->footprint = request_footprint(r->mesh);
+    r->t_submit = now_s();
+    std::lock_guard<std::mutex> lk(srv->mu);
+    r->ticket = srv->next_ticket++;
+    srv->all[r->ticket] = r;
+    srv->pending.push_back(r);
+    srv->cv.notify_all();
+    *ticket = r->ticket;
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_poll(amie_server *srv, uint64_t ticket, amie_result *res, double *x)
+{
+    if (!srv) return AMIE_BAD_INPUT;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->all.find(ticket);
+    if (it == srv->all.end()) return AMIE_BAD_INPUT;
+    amie_server::Req *r = it->second;
+    if (r->status == AMIE_NOT_READY) return AMIE_NOT_READY;
+    if (res) {
+        res->status = r->status;
+        res->iterations = r->iterations;
+        res->relres = r->relres;
+        res->latency_s = r->t_done - r->t_submit;
+        res->queue_s = (r->t_admit > 0 ? r->t_admit : r->t_done) - r->t_submit;
+        res->n = r->x.size();
+    }
+    if (x && !r->x.empty()) std::memcpy(x, r->x.data(), r->x.size() * sizeof(double));
+    return r->status == AMIE_CANCELLED ? AMIE_CANCELLED : AMIE_OK;
+}
+
+extern "C" amie_status amie_cancel(amie_server *srv, uint64_t ticket)
+{
+    if (!srv) return AMIE_BAD_INPUT;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->all.find(ticket);
+    if (it == srv->all.end()) return AMIE_BAD_INPUT;
+    it->second->cancelled = true;
+    srv->cv.notify_all();
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_server_drain(amie_server *srv, double timeout_s)
+{
+    if (!srv) return AMIE_BAD_INPUT;
+    const double t_end = amie::now_s() + (timeout_s > 0 ? timeout_s : 1e30);
+    std::unique_lock<std::mutex> lk(srv->mu);
+    while (true) {
+        bool busy = false;
+        for (auto &kv : srv->all)
+            if (kv.second->status == AMIE_NOT_READY) { busy = true; break; }
+        if (!busy) return AMIE_OK;
+        if (amie::now_s() >= t_end) return AMIE_TIMEOUT;
+        srv->cv.wait_for(lk, std::chrono::milliseconds(5));
+    }
+}
+
+extern "C" amie_status amie_server_stop(amie_server *srv)
+{
+    if (!srv) return AMIE_OK;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->stop_flag = true;
+        for (auto *r : srv->pending) r->cancelled = true;
+        for (auto *r : srv->slot_req)
+            if (r) r->cancelled = true;
+        srv->cv.notify_all();
+    }
+    if (srv->worker.joinable()) srv->worker.join();
+    cudaSetDevice(srv->ctx->device);
+    cudaStreamSynchronize(srv->ctx->stream);
+    for (auto &kv : srv->all) {
+        if (kv.second->topo) amie_topology_destroy(kv.second->topo);
+        delete kv.second;
+    }
+    if (srv->graph) cudaGraphExecDestroy(srv->graph);
+    if (srv->h_slots) cudaFreeHost(srv->h_slots);
+    if (srv->h_ctl) cudaFreeHost(srv->h_ctl);
+    if (srv->h_cta_slot) cudaFreeHost(srv->h_cta_slot);
+    srv->d_slots.release();
+    srv->d_ctl.release();
+    srv->d_cta_slot.release();
+    srv->d_parts.release();
+    amie_ctx_destroy(srv->adm);
+    delete srv;
+    return AMIE_OK;
+}

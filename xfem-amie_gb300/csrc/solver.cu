@@ -326,6 +326,15 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
     return AMIE_OK;
 }
 
+}  // namespace amie
+
+// The AMIE_CG control block starts with the same `done` flag as PcgCtl, so the
+// SpMV kernel's early exit works with either.
+#include "amie_cg.cuh"
+#include "server.cuh"
+
+namespace amie {
+
 amie_status solve_dispatch(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *stats)
 {
     if (!t->assembled) {
@@ -384,6 +393,52 @@ extern "C" amie_status amie_solution_download(const amie_topo *t, double *x)
     AMIE_CUDA(cudaSetDevice(t->ctx->device));
     AMIE_CUDA(cudaMemcpyAsync(x, t->x.p, t->n * 8, cudaMemcpyDeviceToHost, t->ctx->stream));
     AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_timer_start(amie_ctx *ctx)
+{
+    if (!ctx) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(ctx->device));
+    AMIE_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_timer_stop(amie_ctx *ctx, double *ms)
+{
+    if (!ctx || !ms) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(ctx->device));
+    AMIE_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    AMIE_CUDA(cudaEventSynchronize(ctx->ev1));
+    float f = 0.0f;
+    AMIE_CUDA(cudaEventElapsedTime(&f, ctx->ev0, ctx->ev1));
+    *ms = f;
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_t reps, double *ms_per_launch)
+{
+    if (!t || !ms_per_launch || reps <= 0 || (precision != 32 && precision != 64)) return AMIE_BAD_INPUT;
+    if (!t->assembled) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    SolverState *s = nullptr;
+    AMIE_TRY(ensure_state(t, precision == 32, &s));
+    if (precision == 32 && !t->have32) AMIE_TRY(finalize_matrix_async(t, true));
+    cudaStream_t st = t->ctx->stream;
+    // p = 1 keeps the inputs defined; the kernel's cost does not depend on the values
+    if (precision == 64) AMIE_CUDA(cudaMemsetAsync(t->p.p, 0, t->n * 8, st));
+    else AMIE_CUDA(cudaMemsetAsync(t->p32.p, 0, t->n * 4, st));
+    PcgParts parts = parts_of(s);
+    for (int i = 0; i <= reps; i++) {   // launch 0 is a warm-up
+        if (i == 1) AMIE_CUDA(cudaEventRecord(t->ctx->ev0, st));
+        if (precision == 64) launch_spmv_pq<double>(t, s->grid, vecs_of<double>(t), parts.pq, nullptr, st);
+        else launch_spmv_pq<float>(t, s->grid, vecs_of<float>(t), parts.pq, nullptr, st);
+    }
+    AMIE_CUDA(cudaEventRecord(t->ctx->ev1, st));
+    AMIE_CUDA(cudaEventSynchronize(t->ctx->ev1));
+    float f = 0.0f;
+    AMIE_CUDA(cudaEventElapsedTime(&f, t->ctx->ev0, t->ctx->ev1));
+    *ms_per_launch = (double)f / reps;
     return AMIE_OK;
 }
 

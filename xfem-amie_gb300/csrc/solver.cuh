@@ -119,13 +119,16 @@ __device__ __forceinline__ void load_x(const T *__restrict__ x, uint32_t c, T xv
 }
 
 // y = A x over a group of G lanes per block row; acc in the precision of T.
-// Returns, in lane 0 of each group, the row's S outputs.
+// Returns, in lane 0 of each group, the row's S outputs.  Every lane of the
+// warp must call this (the group reduction shuffles over the full warp); a
+// lane whose row is past the end passes valid = false and contributes zero.
 template <int S, int G, typename T>
-__device__ __forceinline__ void row_spmv(const BsrView<T> &A, const T *__restrict__ x, uint32_t row, int lane, T acc[S])
+__device__ __forceinline__ void row_spmv(const BsrView<T> &A, const T *__restrict__ x, uint32_t row, bool valid,
+                                         int lane, T acc[S])
 {
 #pragma unroll
     for (int r = 0; r < S; r++) acc[r] = T(0);
-    const uint32_t b = __ldg(A.row_ptr + row), e = __ldg(A.row_ptr + row + 1);
+    const uint32_t b = valid ? __ldg(A.row_ptr + row) : 0u, e = valid ? __ldg(A.row_ptr + row + 1) : 0u;
     for (uint32_t p = b + lane; p < e; p += G) {
         T blk[S * S], xv[S];
         load_block<S, T>(A.val, p, blk);
@@ -150,10 +153,13 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv_pq(PcgVecs<T> v, double *p
     constexpr int RPB = kVecThreads / G;
     const int lane = threadIdx.x % G;
     double dot = 0.0;
-    for (uint32_t row = blockIdx.x * RPB + threadIdx.x / G; row < v.A.n_rows; row += gridDim.x * RPB) {
+    // the trip count depends on the CTA only, so every lane of a warp reaches the shuffles
+    for (uint32_t base = blockIdx.x * RPB; base < v.A.n_rows; base += gridDim.x * RPB) {
+        const uint32_t row = base + threadIdx.x / G;
+        const bool valid = row < v.A.n_rows;
         T acc[S];
-        row_spmv<S, G, T>(v.A, v.p, row, lane, acc);
-        if (lane == 0) {
+        row_spmv<S, G, T>(v.A, v.p, row, valid, lane, acc);
+        if (valid && lane == 0) {
 #pragma unroll
             for (int r = 0; r < S; r++) {
                 v.q[(uint64_t)row * S + r] = acc[r];
@@ -173,10 +179,12 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv(BsrView<T> A, const T *x, 
     constexpr int RPB = kVecThreads / G;
     const int lane = threadIdx.x % G;
     double dot = 0.0;
-    for (uint32_t row = blockIdx.x * RPB + threadIdx.x / G; row < A.n_rows; row += gridDim.x * RPB) {
+    for (uint32_t base = blockIdx.x * RPB; base < A.n_rows; base += gridDim.x * RPB) {
+        const uint32_t row = base + threadIdx.x / G;
+        const bool valid = row < A.n_rows;
         T acc[S];
-        row_spmv<S, G, T>(A, x, row, lane, acc);
-        if (lane == 0) {
+        row_spmv<S, G, T>(A, x, row, valid, lane, acc);
+        if (valid && lane == 0) {
 #pragma unroll
             for (int r = 0; r < S; r++) {
                 const T yv = b ? b[(uint64_t)row * S + r] - acc[r] : acc[r];
