@@ -155,9 +155,11 @@ amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_sta
     const int nssor = o ? o->nssor : 32;
     const double realeps = std::max(1e-12, eps);
     const int64_t Maxit = o && o->maxit > 0 ? o->maxit : (int64_t)(n / 2);
-    double *part_a = s->parts.p;            // rr / generic
-    double *part_rz = s->parts.p + grid;
-    double *part_pq = s->parts.p + 2 * grid;
+    // partial buffers: pq | rz (inner loop) | rz of the restart step (k_pcg_start) | norms
+    const PcgParts parts0 = parts_of(s);
+    double *part_pq = parts0.pq;
+    double *part_rz = parts0.rz[0];
+    double *part_a = parts0.rr;
     double *x = t->x.p, *r = t->r.p, *z = t->z.p, *p = t->p.p, *q = t->q.p, *xc = t->xc.p, *rc = t->rc.p;
     double *xmin = t->red.p;
     const BsrView<double> A = bsr64(t);
@@ -254,12 +256,19 @@ amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_sta
         *hctl = c;
         AMIE_CUDA(cudaMemcpyAsync(dctl.p, hctl, sizeof(AmieCtl), cudaMemcpyHostToDevice, st));
         AMIE_CUDA(cudaStreamSynchronize(st));
-        while (true) {
+        // host watchdog: localnit <= n, so the device finishes within n / kAmieGraphIters + 2 launches
+        const int64_t max_launches = (int64_t)(n / kAmieGraphIters) + 2;
+        for (int64_t launch = 0;; launch++) {
             AMIE_CUDA(cudaGraphLaunch(gexec, st));
             g_launches += 4 * kAmieGraphIters;
             AMIE_CUDA(cudaMemcpyAsync(hctl, dctl.p, sizeof(AmieCtl), cudaMemcpyDeviceToHost, st));
             AMIE_CUDA(cudaStreamSynchronize(st));
             if (hctl->done) break;
+            if (launch >= max_launches) {
+                set_error("CG control block stalled: localnit %lld, nit %lld", (long long)hctl->localnit,
+                          (long long)hctl->nit);
+                return AMIE_TIMEOUT;
+            }
         }
         nit = hctl->nit;
         last_rho = hctl->last_rho;

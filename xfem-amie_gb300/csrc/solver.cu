@@ -225,12 +225,21 @@ amie_status run_pcg(amie_topo *t, SolverState *s, double tol2, int64_t maxit, in
     AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
     // The pinned copy is rewritten below only after this copy has completed.
     AMIE_CUDA(cudaStreamSynchronize(st));
-    while (true) {
+    // Host watchdog: the device sets `done` by maxit at the latest, so more
+    // launches than maxit / kGraphIters + 2 mean the control block is not advancing.
+    const int64_t max_launches = maxit / kGraphIters + 2;
+    for (int64_t launch = 0;; launch++) {
         AMIE_CUDA(cudaGraphLaunch(*g, st));
         g_launches += 3 * kGraphIters;
         AMIE_CUDA(cudaMemcpyAsync(s->h_ctl, s->ctl.p, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
         AMIE_CUDA(cudaStreamSynchronize(st));
         if (s->h_ctl->done) break;
+        if (launch >= max_launches) {
+            set_error("PCG control block stalled: %lld launches, iterations %lld, maxit %lld, rr %g, tol2 %g",
+                      (long long)launch, (long long)s->h_ctl->iterations, (long long)s->h_ctl->maxit,
+                      s->h_ctl->rr, s->h_ctl->tol2);
+            return AMIE_TIMEOUT;
+        }
     }
     *iters = s->h_ctl->iterations;
     *rr_out = s->h_ctl->rr;
@@ -310,7 +319,10 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
             const double norm = std::sqrt(rr);
             k_scale_to_f32<<<s->grid, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / norm, t->r32.p, t->d32.p);
             AMIE_LAUNCHED();
-            AMIE_TRY(run_pcg<float>(t, s, inner_rtol * inner_rtol, maxit - total, &it, &rr_in));
+            // reduce by inner_rtol, or by less when that is all the outer target still needs
+            const double need = 0.3 * rtol * bnorm / norm;
+            const double inner = std::min(0.5, std::max(inner_rtol, need));
+            AMIE_TRY(run_pcg<float>(t, s, inner * inner, maxit - total, &it, &rr_in));
             k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, norm, t->x.p);
             AMIE_LAUNCHED();
             st_out->refinements++;

@@ -207,7 +207,8 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     if (ctl->done) return;
     const int nparts = gridDim.x;
     const double pq = sum_parts(parts.pq, nparts, sh);
-    const double rz = sum_parts(parts.rz[parity ^ 1], nparts, sh);
+    double *const rz_new_parts = parity ? parts.rz[1] : parts.rz[0];   // select, not a local-memory index
+    const double rz = sum_parts(parity ? parts.rz[0] : parts.rz[1], nparts, sh);
     const double alpha = pq != 0.0 ? rz / pq : 0.0;
     const T a = (T)alpha;
     double drz = 0.0, drr = 0.0;
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     drz = block_sum(drz, sh);
     drr = block_sum(drr, sh);
     if (threadIdx.x == 0) {
-        parts.rz[parity][blockIdx.x] = drz;
+        rz_new_parts[blockIdx.x] = drz;
         parts.rr[blockIdx.x] = drr;
         if (blockIdx.x == 0) {
             ctl->alpha = alpha;
@@ -239,8 +240,8 @@ __global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_
     __shared__ double sh[33];
     if (ctl->done) return;
     const int nparts = gridDim.x;
-    const double rz_new = sum_parts(parts.rz[parity], nparts, sh);
-    const double rz_old = sum_parts(parts.rz[parity ^ 1], nparts, sh);
+    const double rz_new = sum_parts(parity ? parts.rz[1] : parts.rz[0], nparts, sh);
+    const double rz_old = sum_parts(parity ? parts.rz[0] : parts.rz[1], nparts, sh);
     const double rr = sum_parts(parts.rr, nparts, sh);
     const int64_t it = ctl->iterations;   // written by the previous kernel
     const bool stop = rr <= ctl->tol2 || it >= ctl->maxit || !(rr == rr);

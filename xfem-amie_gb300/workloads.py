@@ -270,10 +270,10 @@ def cracked_square(N, L=0.1, order=2, n_inclusions=4000, E_matrix=25e9, E_inc=60
             gpy = vy[e, 1] + pts[:, 0] * (vy[e, 2] - vy[e, 1]) + pts[:, 1] * (vy[e, 0] - vy[e, 1])
             Hg = H(gpx, gpy)
         else:
-            rule = P2_PTS if order == 2 else np.array([[0.333333333333333, 0.333333333333333]])
-            gpx_ = vx[e, 1] + rule[:, 0] * (vx[e, 2] - vx[e, 1]) + rule[:, 1] * (vx[e, 0] - vx[e, 1])
-            gpy_ = vy[e, 1] + rule[:, 0] * (vy[e, 2] - vy[e, 1]) + rule[:, 1] * (vy[e, 0] - vy[e, 1])
-            Hg = H(gpx_, gpy_)
+            # an element the crack does not cut lies on one side of it: H is its centroid's
+            # value at every Gauss point of the element's default rule
+            n_rule = 4 if order == 2 else 1
+            Hg = np.full(n_rule, int(H(np.array([gx[e]]), np.array([gy[e]]))[0]))
         ids = list(conn[e])
         for k in range(3):
             nid = int(vert_ids[e, k])
