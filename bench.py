@@ -67,7 +67,10 @@ def parse_args():
     ap.add_argument("--serve", type=int, default=256, help="serving-mix requests (0 = skip)")
     ap.add_argument("--profile", action="store_true", help="assemble once and launch the SpMV kernels a few times "
                                                            "(for an ncu capture), print their timings, exit")
+    ap.add_argument("--launch-list", action="store_true", help="run exactly one step without warm-up (for an ncu "
+                                                               "launch list), print its timing, exit")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--damage-steps", type=int, default=60, help="config-3 damage-loop load steps (0 = skip)")
     return ap.parse_args()
 
 
@@ -296,6 +299,16 @@ def run_ours(args, world, rank, local, dist):
     topo.assemble()
     topo.apply_dirichlet(*bcs)
     n = topo.n
+    if args.launch_list:
+        # exactly one step (assembly + elimination + solve), for an ncu launch list of a step
+        ctx.timer_start()
+        topo.assemble()
+        st = topo.solve_resident(solver, rtol=args.rtol)
+        ms = ctx.timer_stop()
+        print(json.dumps({"launch_list": name, "n_dof": int(n), "ms": ms, **st}))
+        topo.close()
+        ctx.close()
+        return 0
     if args.profile:
         # few launches for an ncu capture: 2 FP32 and 2 FP64 SpMV(+dot) launches after one assembly
         ms32 = topo.profile_spmv(32, 1)
@@ -413,6 +426,9 @@ def run_ours(args, world, rank, local, dist):
     # serving mix (config 4): p50 / p99 latency next to throughput
     if args.serve > 0:
         result["serving"] = run_serving(ctx, args.serve, args.serve_rate, solver)
+    # damage loop (config 3)
+    if args.damage_steps > 0:
+        result["damage_loop"] = run_damage_loop(ctx, solver, args.damage_steps)
 
     # CPU baseline: the oracle port on this machine's host cores, bounded sample, rank 0 at N = 1
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -470,6 +486,35 @@ def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, p
             "mean_dof": float(np.mean(dofs)) if dofs else 0.0, "mean_iterations": float(np.mean(iters)) if iters else 0.0,
             "distinct_microstructures": pool,
             "solver": "mixed" if solver == G.SOLVER_PCG_MIXED else "fp64"}
+
+
+def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 6e-5):
+    """Config-3 loop: notched beam in three-point bending, P1, ~250k DOF, E 35 GPa;
+    each load step updates the scalar damage on the device from the last
+    solution (Mazars equivalent strain, eps0 = 1e-4, exponential softening),
+    re-integrates (1 - d) C, eliminates the new imposed deflection and solves
+    warm-started from the previous displacement (all device-resident)."""
+    import amie_gpu as G
+    m, bcs_at, meta = W.notched_beam()
+    topo = G.Topology(ctx, m)
+    topo.assemble()
+    iters, changed = [], []
+    ctx.timer_start()
+    for k in range(1, steps + 1):
+        if k > 1:
+            nc, _ = topo.damage_step(eps0=1e-4, softening=3000.0, d_max=0.999, want_damage=False)
+            changed.append(nc)
+        topo.apply_dirichlet(*bcs_at(deflection_max * k / steps))   # scatter (1-d) C + elimination
+        st = topo.solve_resident(solver, rtol=1e-10, use_x0=k > 1)
+        iters.append(st["iterations"])
+    ms = ctx.timer_stop()
+    _, dmg = topo.damage_step(eps0=1e-4, softening=3000.0, d_max=0.999)
+    topo.close()
+    n = meta["n_dof"]
+    return {"steps": steps, "n_dof": int(n), "ms_total": ms, "ms_per_step": ms / steps,
+            "iterations_total": int(sum(iters)), "dof_iterations_per_s": n * sum(iters) / (ms / 1e3),
+            "damaged_elements": int((dmg > 0).sum()), "max_damage": float(dmg.max()),
+            "elements_changed_last_step": int(changed[-1]) if changed else 0}
 
 
 def topo_group(topo):

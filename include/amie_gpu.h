@@ -227,6 +227,30 @@ AMIE_API amie_status amie_cancel(amie_server *srv, uint64_t ticket);
 AMIE_API amie_status amie_server_drain(amie_server *srv, double timeout_s);
 AMIE_API amie_status amie_server_stop(amie_server *srv);
 
+/* ------------------------------------------------------------------ fields and damage
+ * Per-element strain (Voigt, engineering shear: xx yy xy in 2D, xx yy zz yz xz xy
+ * in 3D) and stress (C_eff strain) from the device-resident solution, averaged
+ * over the element's Gauss points with their weights
+ * (FeatureTree::strainFromDisplacements / stressFromDisplacements,
+ * features/features.cpp:4223, 3424).  strain, stress: [n_elem * nv] host arrays or NULL. */
+AMIE_API amie_status amie_element_fields(amie_topo *topo, double *strain, double *stress);
+
+/* One explicit scalar-damage update from the current solution
+ * (StiffnessAndFracture::step, physics/stiffness_and_fracture.cpp:81-90): Mazars
+ * equivalent strain eq = |<eps>_+| of the principal strains
+ * (physics/fracturecriteria/mazars.cpp:153), d = 1 - (eps0/eq) exp(-B (eq - eps0))
+ * above eps0, irreversible, capped at d_max; the factor on C becomes base (1 - d),
+ * so the next amie_assemble integrates (1 - d) C (isotropiclineardamage.cpp:39-46).
+ * 2D meshes.  n_changed: elements whose damage grew by more than change_tol. */
+typedef struct amie_damage_params {
+    double eps0;
+    double softening;    /* B */
+    double d_max;
+    double change_tol;
+} amie_damage_params;
+AMIE_API amie_status amie_damage_step(amie_topo *topo, const amie_damage_params *params, uint32_t *n_changed,
+                                      double *damage_out);
+
 /* ------------------------------------------------------------------ timing
  * Device time on the context's stream (CUDA events) between start and stop;
  * stop synchronises the stream.  No counterpart in the reference, which

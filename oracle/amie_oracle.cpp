@@ -227,6 +227,85 @@ extern "C" int oracle_element_matrices(const oracle_mesh *m, const uint64_t *ke_
     return bad ? -2 : 0;
 }
 
+extern "C" int oracle_element_fields(const oracle_mesh *m, const double *u, double *strain, double *stress)
+{
+    const int dim = m->dim;
+    const int nv = dim == 2 ? 3 : 6;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < (int64_t)m->n_elem; e++) {
+        const int kind = m->kind[e];
+        const int nshape = shape_count(kind);
+        const uint32_t e0 = m->enr_ptr ? m->enr_ptr[e] : 0, e1 = m->enr_ptr ? m->enr_ptr[e + 1] : 0;
+        const int nf = nshape + (int)(e1 - e0);
+        const double *Je = m->jinv + (size_t)e * dim * dim;
+        const uint32_t g0 = m->gp_ptr[e], g1 = m->gp_ptr[e + 1];
+        std::vector<double> pts, wts;
+        if (g1 > g0) {
+            for (uint32_t g = g0; g < g1; g++) {
+                for (int c = 0; c < dim; c++) pts.push_back(m->gp[(size_t)g * (dim + 1) + c]);
+                wts.push_back(m->gp[(size_t)g * (dim + 1) + dim]);
+            }
+        } else {
+            Rule r = default_rule(kind);
+            for (int g = 0; g < r.n; g++) {
+                for (int c = 0; c < dim; c++) pts.push_back(r.p[g][c]);
+                wts.push_back(r.w[g] / det(dim, Je));
+            }
+        }
+        const bool moved = m->moved && m->moved[e] && g1 > g0;
+        double eps[6] = {0, 0, 0, 0, 0, 0}, wsum = 0;
+        for (size_t g = 0; g < wts.size(); g++) {
+            double sg[6][3];
+            shape_grad(kind, &pts[g * dim], sg);
+            const double *J = moved ? m->jinv_gp + (size_t)(g0 + g) * dim * dim : Je;
+            double eg[6] = {0, 0, 0, 0, 0, 0};
+            for (int f = 0; f < nf; f++) {
+                double lg[3] = {0, 0, 0};
+                if (f < nshape) {
+                    for (int c = 0; c < dim; c++) lg[c] = sg[f][c];
+                } else {
+                    const uint32_t fj = e0 + (f - nshape);
+                    const size_t off = (size_t)m->enr_data[fj] + g;
+                    if (m->enr_type[fj] == ORACLE_ENR_HEAVISIDE) {
+                        lg[0] = P1_GRAD[m->enr_vertex[fj]][0] * m->enr_jump[off];
+                        lg[1] = P1_GRAD[m->enr_vertex[fj]][1] * m->enr_jump[off];
+                    } else {
+                        for (int c = 0; c < dim; c++) lg[c] = m->enr_grad[off * dim + c];
+                    }
+                }
+                double d[3] = {0, 0, 0};
+                for (int r = 0; r < dim; r++)
+                    for (int c = 0; c < dim; c++) d[r] += lg[c] * J[r * dim + c];
+                const double *x = u + (size_t)m->dof_ids[m->dof_ptr[e] + f] * dim;
+                if (dim == 2) {
+                    eg[0] += d[0] * x[0];
+                    eg[1] += d[1] * x[1];
+                    eg[2] += d[1] * x[0] + d[0] * x[1];
+                } else {
+                    eg[0] += d[0] * x[0];
+                    eg[1] += d[1] * x[1];
+                    eg[2] += d[2] * x[2];
+                    eg[3] += d[2] * x[1] + d[1] * x[2];
+                    eg[4] += d[2] * x[0] + d[0] * x[2];
+                    eg[5] += d[1] * x[0] + d[0] * x[1];
+                }
+            }
+            for (int k = 0; k < nv; k++) eps[k] += wts[g] * eg[k];
+            wsum += wts[g];
+        }
+        const double cs = m->cscale ? m->cscale[e] : 1.0;
+        const double *C = m->cmat_table + (size_t)m->mat[e] * nv * nv;
+        for (int k = 0; k < nv; k++) eps[k] /= wsum;
+        for (int k = 0; k < nv; k++) {
+            double s = 0;
+            for (int l = 0; l < nv; l++) s += C[k * nv + l] * eps[l];
+            strain[(size_t)e * nv + k] = eps[k];
+            stress[(size_t)e * nv + k] = cs * s;
+        }
+    }
+    return 0;
+}
+
 extern "C" int oracle_pattern(const oracle_mesh *m, uint32_t *n_rows, uint64_t *nnzb, uint32_t *row_size,
                               uint32_t *column_index)
 {

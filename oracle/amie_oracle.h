@@ -93,6 +93,12 @@ int oracle_pcg(int32_t stride, uint32_t n_rows, const uint32_t *row_size, const 
                const double *array, const double *b, double *x, double rtol, int64_t maxit,
                int64_t *iterations, double *relres);
 
+/* Per-element strain (Voigt, engineering shear) averaged over the element's Gauss
+ * points with their weights, and stress = cscale C strain, from displacements u
+ * (FeatureTree::strainFromDisplacements / stressFromDisplacements,
+ * features/features.cpp:4223, 3424).  strain, stress: [n_elem * nv]. */
+int oracle_element_fields(const oracle_mesh *m, const double *u, double *strain, double *stress);
+
 /* Number of OpenMP threads the oracle uses (for reporting). */
 int oracle_threads(void);
 

@@ -127,6 +127,17 @@ def pcg(stride, rs, ci, arr, b, x0=None, rtol=1e-10, maxit=100000):
     return x, int(it.value), float(rr.value), int(rc)
 
 
+def element_fields(m, u):
+    """(strain, stress) per element, Voigt, from displacements u."""
+    nv = m.nv
+    eps = np.zeros(m.n_elem * nv)
+    sig = np.zeros(m.n_elem * nv)
+    st = _mesh_struct(m)
+    u = np.ascontiguousarray(u, np.float64)
+    lib().oracle_element_fields(C.byref(st), _p(u), _p(eps), _p(sig))
+    return eps.reshape(-1, nv), sig.reshape(-1, nv)
+
+
 def assemble(m, bc_ids, bc_values, bc_kinds, rhs0=None):
     """Full host pipeline: K_e -> pattern -> Kahan scatter -> Dirichlet."""
     off, ke = element_matrices(m)

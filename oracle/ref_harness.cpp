@@ -300,6 +300,15 @@ int run_2d(const std::string &which, Out &o, std::map<std::string, std::string> 
         new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, BOTTOM),
         new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM),
         new BoundingBoxDefinedBoundaryCondition(SET_ALONG_ETA, TOP, disp)};
+    if (which == "plate") {
+        // examples/main_check_behaviour.cpp with examples/test/test_stiffness.ini:
+        // 10 x 10 mm plate, E = 10 GPa, nu = 0.2, 1 MPa imposed as a stress on TOP;
+        // the reference's known answer is strain_yy * 1e3 = 0.1, stress_yy / 1e6 = 1
+        // (examples/test/check_behaviour_test_stiffness_base).
+        bcs = {new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM),
+               new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, BOTTOM_LEFT),
+               new BoundingBoxDefinedBoundaryCondition(SET_STRESS_ETA, TOP, getd(kv, "stress", 1e6))};
+    }
     F.setSamplingNumber(sampling);
     if (order == 2) F.setOrder(QUADRATIC);
 
@@ -394,7 +403,7 @@ int main(int argc, char **argv)
     auto kv = parse_kv(argc, argv, 3);
     Out o(argv[2]);
     if (!o.f) return 3;
-    if (which == "incl" || which == "crack") return run_2d(which, o, kv);
+    if (which == "incl" || which == "crack" || which == "plate") return run_2d(which, o, kv);
     if (which == "voxel") return run_voxel(o, kv);
     std::fprintf(stderr, "unknown case %s\n", which.c_str());
     return 2;

@@ -34,6 +34,9 @@ CASES = {
     # straight Heaviside-enriched crack of length 0.3*width, P1 and P2
     "crack_p1": ("crack", ["sampling=16", "order=1", "E=25e9"]),
     "crack_p2": ("crack", ["sampling=10", "order=2", "E=25e9"]),
+    # known-answer test of examples/test/test_stiffness.ini: 10 mm plate, 1 MPa imposed
+    # stress on TOP (force multipliers), E = 10 GPa -> strain_yy = 1e-4 everywhere
+    "plate": ("plate", ["size=0.01", "E=10e9", "nu=0.2", "sampling=4"]),
     # config-2 style: voxel file -> 6 linear tets per voxel, 16 lognormal phases,
     # uniaxial imposed strain 1e-4
     "voxel_t4": ("voxel", ["n=6", "nphase=16", "seed=5", "strain=1e-4"]),

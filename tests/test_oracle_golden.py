@@ -78,6 +78,19 @@ def test_cg_amie_matches_reference(name):
     assert rel(x, d["u"]) <= U_TOL.get(name, 1e-9)
 
 
+def test_plate_known_answer():
+    """examples/test/check_behaviour_test_stiffness_base: strain_yy * 1e3 = 0.1 and
+    stress_yy / 1e6 = 1 for the 1 MPa plate, in every element (the reference's
+    solve stops at an absolute tolerance: 1e-7 relative here)."""
+    d = load_golden("plate")
+    m = am.from_golden(d, "tabulated")
+    eps, sig = O.element_fields(m, d["u"])
+    assert np.allclose(eps[:, 1] * 1e3, 0.1, rtol=1e-7)
+    assert np.allclose(sig[:, 1] / 1e6, 1.0, rtol=1e-7)
+    assert np.allclose(eps[:, 0], -0.2e-4, rtol=1e-6)
+    assert np.abs(eps[:, 2]).max() < 1e-11
+
+
 def test_pcg_reaches_tight_residual():
     d = load_golden("incl_p1")
     x, it, rr, rc = O.pcg(2, d["row_size"], d["column_index"], d["array"], d["rhs"], rtol=1e-12)

@@ -33,8 +33,13 @@ EXPORTED = [
     "amie_element_matrices", "amie_apply_dirichlet", "amie_matrix_download", "amie_spmv", "amie_solve",
     "amie_solve_resident", "amie_solution_download", "amie_server_start", "amie_submit", "amie_poll",
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
-    "amie_timer_stop", "amie_profile_spmv",
+    "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step",
 ]
+
+
+class DamageParams(C.Structure):
+    _fields_ = [("eps0", C.c_double), ("softening", C.c_double), ("d_max", C.c_double),
+                ("change_tol", C.c_double)]
 
 
 class AmieError(RuntimeError):
@@ -248,6 +253,22 @@ class Topology:
         x = np.zeros(self.n, np.float64)
         check(lib().amie_solution_download(self.ptr, _p(x)), "amie_solution_download")
         return x
+
+    def element_fields(self):
+        """(strain, stress) per element, Voigt, from the device solution."""
+        nv = self.mesh.nv
+        eps = np.zeros(self.mesh.n_elem * nv, np.float64)
+        sig = np.zeros(self.mesh.n_elem * nv, np.float64)
+        check(lib().amie_element_fields(self.ptr, _p(eps), _p(sig)), "amie_element_fields")
+        return eps.reshape(-1, nv), sig.reshape(-1, nv)
+
+    def damage_step(self, eps0=1e-4, softening=5000.0, d_max=0.9999, change_tol=1e-6, want_damage=True):
+        """One damage update from the device solution; returns (elements changed, damage or None)."""
+        prm = DamageParams(eps0, softening, d_max, change_tol)
+        n = C.c_uint32()
+        d = np.zeros(self.mesh.n_elem, np.float64) if want_damage else None
+        check(lib().amie_damage_step(self.ptr, C.byref(prm), C.byref(n), _p(d)), "amie_damage_step")
+        return n.value, d
 
     def profile_spmv(self, precision: int = 64, reps: int = 20) -> float:
         """Average device milliseconds of one q = A p (+ p.q) launch."""

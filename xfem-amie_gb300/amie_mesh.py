@@ -177,9 +177,21 @@ def from_golden(d, enrichment: str = "auto") -> MeshData:
     return m
 
 
+# LagrangeMultiplierType values (solvers/assembly.h:36-96): the force types are
+# added to the right-hand side after elimination, GENERAL and
+# SET_PROPORTIONAL_DISPLACEMENT are not supported, every other type is an
+# eliminated displacement (solvers/assembly.cpp:163-169).
+LM_FORCE_TYPES = (34, 35, 36, 37)          # SET_FORCE_XI, _ETA, _ZETA, _INDEXED_AXIS
+LM_UNSUPPORTED = (0, 23)                   # GENERAL, SET_PROPORTIONAL_DISPLACEMENT
+
+
 def golden_bcs(d):
-    """Dirichlet multipliers of a fixture: (ids, values, kinds)."""
+    """Multipliers of a fixture as (ids, values, kinds), sorted by id as make_final sorts them."""
     ids = d["bc_ids"].astype(np.uint32)
     vals = d["bc_values"].astype(np.float64)
-    kinds = np.zeros(len(ids), np.uint8)   # SET_ALONG_* / FIX_ALONG_* -> displacement
-    return ids, vals, kinds
+    types = d["bc_types"].astype(np.int64)
+    if np.isin(types, LM_UNSUPPORTED).any():
+        raise ValueError("GENERAL / proportional multipliers are not supported")
+    kinds = np.where(np.isin(types, LM_FORCE_TYPES), BC_FORCE, BC_DISPLACEMENT).astype(np.uint8)
+    order = np.argsort(ids, kind="stable")
+    return ids[order], vals[order], kinds[order]

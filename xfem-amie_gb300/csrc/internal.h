@@ -155,6 +155,7 @@ struct amie_topo {
     amie::DevArray<float> r32, z32, p32, q32, d32;
     amie::DevArray<uint8_t> fixed;
     amie::DevArray<double> fixval;
+    amie::DevArray<double> strain, damage, cscale_base;   // field recovery and damage loop
     // Dirichlet / force multipliers and initial forces of the last
     // amie_apply_dirichlet; re-applied by every amie_assemble (make_final does
     // scatter + setBoundaryConditions in one call, solvers/assembly.cpp:803-816).

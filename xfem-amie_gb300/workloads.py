@@ -461,6 +461,58 @@ def serving_mix(n_requests, rate, dof_min=2000, dof_max=200000, seed=7, pool=64)
     return meshes, arrivals, which
 
 
+def notched_beam(nx=706, ny=176, Lx=0.4, Ly=0.1, notch_w=0.02, notch_h=0.002, E=35e9, nu=0.2, seed=3,
+                 jitter=0.1):
+    """Config-3 family: 400 x 100 mm beam, P1 triangles, a 20 x 2 mm notch at the
+    bottom of midspan (elements inside removed, as a VoidForm feature leaves them
+    without stiffness; orphan nodes renumbered away), three-point bending:
+    bottom-left corner fixed in x and y, bottom-right corner fixed in y, the top
+    midspan node displaced downwards (the load of each step is a multiplier value)."""
+    rng = np.random.default_rng(seed)
+    hx, hy = Lx / nx, Ly / ny
+    M = nx + 1
+    I, J = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), indexing="xy")
+    x = (I * hx).astype(np.float64).ravel()
+    y = (J * hy).astype(np.float64).ravel()
+    inner = ((I > 0) & (J > 0) & (I < nx) & (J < ny)).ravel()
+    x[inner] += rng.uniform(-jitter, jitter, inner.sum()) * hx
+    y[inner] += rng.uniform(-jitter, jitter, inner.sum()) * hy
+    ci, cj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    ci, cj = ci.ravel(), cj.ravel()
+    a = cj * M + ci
+    b = a + 1
+    c = a + M + 1
+    d = a + M
+    conn = np.concatenate([np.stack([c, a, b], 1), np.stack([d, a, c], 1)])
+    cx = x[conn].mean(1)
+    cy = y[conn].mean(1)
+    keep = ~((np.abs(cx - Lx / 2) < notch_w / 2) & (cy < notch_h))
+    conn = conn[keep]
+    used = np.unique(conn)
+    remap = np.full(len(x), -1, np.int64)
+    remap[used] = np.arange(len(used))
+    conn = remap[conn].astype(np.uint32)
+    x, y = x[used], y[used]
+    vx, vy = x[conn], y[conn]
+    Jinv, _ = _tri_jinv(vx, vy)
+    E_count = len(conn)
+    m = am.MeshData(dim=2, stride=2, kind=np.full(E_count, am.TRI3, np.uint8),
+                    dof_ptr=(np.arange(E_count + 1) * 3).astype(np.uint32), dof_ids=conn.ravel(),
+                    gp_ptr=np.zeros(E_count + 1, np.uint32), gp=np.zeros(0), jinv=Jinv.reshape(-1),
+                    mat=np.zeros(E_count, np.uint32), cmat_table=plane_stress(E, nu).reshape(-1), ndofmax=len(x))
+    tol = 1e-12
+    left = int(np.nonzero((np.abs(x) < tol) & (np.abs(y) < tol))[0][0])
+    right = int(np.nonzero((np.abs(x - Lx) < tol) & (np.abs(y) < tol))[0][0])
+    top = int(np.argmin(np.abs(x - Lx / 2) + 10 * np.abs(y - Ly)))
+    meta = dict(n_nodes=len(x), n_elem=E_count, n_dof=2 * len(x), load_node=top)
+
+    def bcs(deflection):
+        ids = np.array(sorted([2 * left, 2 * left + 1, 2 * right + 1, 2 * top + 1]), np.uint32)
+        vals = np.array([-deflection if i == 2 * top + 1 else 0.0 for i in ids])
+        return ids, vals, np.zeros(len(ids), np.uint8)
+    return m, bcs, meta
+
+
 def voxel_cube(nv=64, E_median=30e9, sigma_log=0.4, nu=0.2, strain=1e-4, seed=1, size=1e-4):
     """Config-2 family: n^3 voxels, 6 linear tetrahedra per voxel with the corner
     choice of VoxelFilter::read (filters/voxelfilter.cpp:352-400), lognormal E per
