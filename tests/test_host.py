@@ -42,6 +42,18 @@ def test_python_binding_lists_every_symbol():
     assert sorted(amie_gpu.EXPORTED) == declared_functions()
 
 
+def test_amie_bridge_compiles_against_reference_headers():
+    """The AMIE-side adapter (xfem-amie_gb300/host/amie_bridge.cpp) compiles
+    against the reference's own headers where the reference tree is present."""
+    import subprocess
+    oracle_dir = os.path.join(REPO, "oracle")
+    has = subprocess.run(["make", "-s", "-C", oracle_dir, "has-ref"], capture_output=True, text=True).stdout.strip()
+    if has != "yes":
+        pytest.skip("reference tree not present")
+    r = subprocess.run(["make", "-s", "-C", oracle_dir, "bridge"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
 def test_mesh_validation_and_offsets():
     d = load_golden("crack_p2")
     m = am.from_golden(d, "auto")
