@@ -185,6 +185,27 @@ AMIE_API amie_status amie_solve(amie_topo *topo, const amie_solve_opts *opts, do
 AMIE_API amie_status amie_solve_resident(amie_topo *topo, const amie_solve_opts *opts, amie_solve_stats *stats);
 AMIE_API amie_status amie_solution_download(const amie_topo *topo, double *x);
 
+/* Jacobi-PCG (FP64, relative-residual stop) on a block-CSR matrix the caller
+ * already holds in device memory, without allocating any device memory.  No
+ * counterpart in the reference.  For callers that cannot call cudaMalloc at
+ * solve time: code running during a CUDA graph capture that forbids
+ * allocation, applications whose own pool owns all device memory, real-time
+ * loops that cannot take an allocation's implicit synchronisation.
+ *   Matrix: row_ptr_dev [n_rows+1], col_dev [nnzb], val_dev [nnzb*s*s] (s x s
+ *   blocks row-major, this library's device layout), b_dev, x_dev [n_rows*s];
+ *   x_dev is the warm start if use_x0, the solution on return.  stream: a
+ *   cudaStream_t, or NULL for the default stream.
+ *   Limit: n_rows * stride <= 262144 scalar DOFs; larger systems return
+ *   AMIE_BAD_INPUT.  The work vectors live in one static device array of about
+ *   10.5 MB that every GPU loading this library reserves until exit.
+ *   The first call on a device looks up that array's device address (set-up);
+ *   make that first call before any stream capture.  Every call shares the
+ *   array, so calls that overlap on the GPU race. */
+AMIE_API amie_status amie_pcg_solve_noalloc(int32_t stride, uint32_t n_rows, const uint32_t *row_ptr_dev,
+                                            const uint32_t *col_dev, const double *val_dev, const double *b_dev,
+                                            double *x_dev, double rtol, int64_t maxit, int32_t use_x0, void *stream,
+                                            amie_solve_stats *stats);
+
 /* ------------------------------------------------------------------ serving
  * Continuous-batching solve server: independent meshes (microstructure or
  * damage-step solves) are admitted while others run, as free HBM allows; all

@@ -33,7 +33,7 @@ EXPORTED = [
     "amie_element_matrices", "amie_apply_dirichlet", "amie_matrix_download", "amie_spmv", "amie_solve",
     "amie_solve_resident", "amie_solution_download", "amie_server_start", "amie_submit", "amie_poll",
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
-    "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step",
+    "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step", "amie_pcg_solve_noalloc",
 ]
 
 
