@@ -155,11 +155,11 @@ amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_sta
     const int nssor = o ? o->nssor : 32;
     const double realeps = std::max(1e-12, eps);
     const int64_t Maxit = o && o->maxit > 0 ? o->maxit : (int64_t)(n / 2);
-    // partial buffers: pq | rz (inner loop) | rz of the restart step (k_pcg_start) | norms
+    // partial buffers: pq | rz (restart step and inner loop) | rr (restart step) | norms
     const PcgParts parts0 = parts_of(s);
     double *part_pq = parts0.pq;
-    double *part_rz = parts0.rz[0];
-    double *part_a = parts0.rr;
+    double *part_rz = parts0.rz;
+    double *part_a = parts0.spare;
     double *x = t->x.p, *r = t->r.p, *z = t->z.p, *p = t->p.p, *q = t->q.p, *xc = t->xc.p, *rc = t->rc.p;
     double *xmin = t->red.p;
     const BsrView<double> A = bsr64(t);
@@ -188,7 +188,7 @@ amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_sta
         for (int it = 0; it < kAmieGraphIters; it++) {
             k_amie_precond<<<grid, kVecThreads, 0, st>>>(n, t->invdiag.p, r, z, part_rz, dctl.p);
             k_amie_direction<<<grid, kVecThreads, 0, st>>>(n, z, p, part_rz, dctl.p);
-            launch_spmv_pq<double>(t, grid, v, part_pq, reinterpret_cast<const PcgCtl *>(dctl.p), st);
+            launch_spmv_pq<double>(t, grid, v, part_pq, &dctl.p->done, nullptr, st);
             k_amie_update<<<grid, kVecThreads, 0, st>>>(n, x, r, xc, rc, p, q, part_rz, part_pq, dctl.p);
         }
         AMIE_CUDA(cudaStreamEndCapture(st, &graph));
@@ -235,11 +235,12 @@ amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_sta
         if (err0 < realeps) { result = AMIE_OK; break; }
         // z = D^-1 r, p = z, q = A p
         PcgParts parts = parts_of(s);
-        k_pcg_start<double><<<grid, kVecThreads, 0, st>>>(v, n, parts);   // z, p; r.z -> rz[1]
+        AMIE_CUDA(cudaMemsetAsync(s->ctl.p, 0, sizeof(PcgCtl), st));
+        k_pcg_start<double><<<grid, kVecThreads, 0, st>>>(v, n, parts, s->ctl.p);   // z, p; partial r.z
         AMIE_LAUNCHED();
-        launch_spmv_pq<double>(t, grid, v, part_pq, nullptr, st);
+        launch_spmv_pq<double>(t, grid, v, part_pq, nullptr, nullptr, st);
         double last_rho = 0.0, pq = 0.0;
-        AMIE_TRY(read_sum(t, parts.rz[1], grid, &last_rho));
+        AMIE_TRY(read_sum(t, parts.rz, grid, &last_rho));
         AMIE_TRY(read_sum(t, part_pq, grid, &pq));
         if (std::fabs(pq) < 1e-12 * last_rho) { result = AMIE_OK; break; }
         k_amie_first_update<<<grid, kVecThreads, 0, st>>>(n, last_rho / pq, x, r, xc, rc, p, q);

@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 
 #include "element.cuh"
@@ -643,7 +644,12 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
 
     // rows ~ blocks per row -> lanes per block row in the SpMV
     const double avg = (double)t->nnzb / t->n_rows;
-    t->spmv_group = avg <= 4.5 ? 4 : avg <= 9 ? 8 : avg <= 18 ? 16 : 32;
+    t->spmv_group = avg <= 4.5 ? 2 : avg <= 9 ? 2 : avg <= 18 ? 4 : 8;
+    // tuning override for measurements: AMIE_SPMV_GROUP = 1, 2, 4, 8, 16 or 32 lanes per block row
+    if (const char *g = std::getenv("AMIE_SPMV_GROUP")) {
+        const int v = std::atoi(g);
+        if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16 || v == 32) t->spmv_group = v;
+    }
 
     // matrix, vectors and staging
     const uint64_t n = t->n;

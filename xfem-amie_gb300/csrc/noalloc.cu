@@ -111,9 +111,9 @@ amie_status noalloc_solve(const NoAllocDevice &dev, uint32_t n_rows, const uint3
     const int grid = std::min(dev.num_sms * 4, kNoAllocMaxCtas);
     PcgParts pp;
     pp.pq = parts;
-    pp.rz[0] = parts + kNoAllocMaxCtas;
-    pp.rz[1] = parts + 2 * kNoAllocMaxCtas;
-    pp.rr = parts + 3 * kNoAllocMaxCtas;
+    pp.rz = parts + kNoAllocMaxCtas;
+    pp.rr = parts + 2 * kNoAllocMaxCtas;
+    pp.spare = parts + 3 * kNoAllocMaxCtas;
     uint32_t nnzb = 0;
     AMIE_CUDA(cudaMemcpyAsync(&nnzb, row_ptr + n_rows, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     AMIE_CUDA(cudaStreamSynchronize(st));
@@ -125,10 +125,10 @@ amie_status noalloc_solve(const NoAllocDevice &dev, uint32_t n_rows, const uint3
     k_noalloc_invdiag<S><<<(n_rows + 255) / 256, 256, 0, st>>>(n_rows, row_ptr, col, val, dinv);
     AMIE_LAUNCHED();
     if (!use_x0) AMIE_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), st));
-    k_noalloc_norm2<<<grid, kVecThreads, 0, st>>>(n, b, pp.rr);
+    k_noalloc_norm2<<<grid, kVecThreads, 0, st>>>(n, b, pp.spare);
     AMIE_LAUNCHED();
     double bb = 0.0;
-    AMIE_TRY(host_sum(pp.rr, grid, st, &bb));
+    AMIE_TRY(host_sum(pp.spare, grid, st, &bb));
     const double bnorm = std::sqrt(bb);
     stats->iterations = 0;
     stats->refinements = 0;
@@ -142,10 +142,10 @@ amie_status noalloc_solve(const NoAllocDevice &dev, uint32_t n_rows, const uint3
     auto residual = [&](double *rr) -> amie_status {   // r = b - A x, returns r.r
         with_group<S>(group, [&](auto g) {
             constexpr int G = decltype(g)::value;
-            k_spmv<S, G, double><<<grid, kVecThreads, 0, st>>>(A, x, b, r, pp.rr);
+            k_spmv<S, G, double><<<grid, kVecThreads, 0, st>>>(A, x, b, r, pp.spare);
         });
         AMIE_LAUNCHED();
-        return host_sum(pp.rr, grid, st, rr);
+        return host_sum(pp.spare, grid, st, rr);
     };
     double rr = 0.0;
     AMIE_TRY(residual(&rr));
@@ -157,23 +157,22 @@ amie_status noalloc_solve(const NoAllocDevice &dev, uint32_t n_rows, const uint3
         if (!(rr == rr)) { result = AMIE_NAN; break; }
         if (rr <= target2) { result = AMIE_OK; break; }
         if (total >= maxit) break;
-        k_pcg_start<double><<<grid, kVecThreads, 0, st>>>(v, n, pp);
-        AMIE_LAUNCHED();
-        PcgCtl c{};
+        PcgCtl c{};   // done = 0, ticket = 0, iterations = 0
         c.maxit = maxit - total;
         c.tol2 = 0.25 * target2;
         AMIE_CUDA(cudaMemcpyAsync(ctl, &c, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
+        k_pcg_start<double><<<grid, kVecThreads, 0, st>>>(v, n, pp, ctl);
+        AMIE_LAUNCHED();
         const int64_t max_rounds = c.maxit / kCheck + 2;
         PcgCtl h{};
         for (int64_t round = 0;; round++) {
             for (int it = 0; it < kCheck; it++) {
-                const int parity = it & 1;
                 with_group<S>(group, [&](auto g) {
                     constexpr int G = decltype(g)::value;
-                    k_spmv_pq<S, G, double><<<grid, kVecThreads, 0, st>>>(v, pp.pq, ctl);
+                    k_spmv_pq<S, G, double><<<grid, kVecThreads, 0, st>>>(v, pp.pq, &ctl->done, ctl);
                 });
-                k_update<double><<<grid, kVecThreads, 0, st>>>(v, n, pp, parity, ctl);
-                k_direction<double><<<grid, kVecThreads, 0, st>>>(v, n, pp, parity, ctl);
+                k_update<double><<<grid, kVecThreads, 0, st>>>(v, n, pp, ctl);
+                k_direction<double><<<grid, kVecThreads, 0, st>>>(v, n, ctl);
                 g_launches += 3;
             }
             AMIE_CUDA(cudaMemcpyAsync(&h, ctl, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));

@@ -104,8 +104,9 @@ __global__ void __launch_bounds__(kVecThreads) kb_spmv_pq(const SlotDesc *slots,
     for (uint32_t base = lc * RPB; base < A.n_rows; base += nc * RPB) {
         const uint32_t row = base + threadIdx.x / G;
         const bool valid = row < A.n_rows;
+        const uint32_t rb = valid ? __ldg(A.row_ptr + row) : 0u, re = valid ? __ldg(A.row_ptr + row + 1) : 0u;
         T acc[2];
-        row_spmv<2, G, T>(A, v.p, row, valid, lane, acc);
+        row_spmv<2, G, T>(A, v.p, rb, re, lane, acc);
         if (valid && lane == 0) {
             v.q[(uint64_t)row * 2] = acc[0];
             v.q[(uint64_t)row * 2 + 1] = acc[1];

@@ -60,6 +60,8 @@ template <int S, typename T, typename F>
 void dispatch_group(int group, F &&f)
 {
     switch (group) {
+    case 1: f(std::integral_constant<int, 1>()); break;
+    case 2: f(std::integral_constant<int, 2>()); break;
     case 4: f(std::integral_constant<int, 4>()); break;
     case 8: f(std::integral_constant<int, 8>()); break;
     case 16: f(std::integral_constant<int, 16>()); break;
@@ -67,14 +69,16 @@ void dispatch_group(int group, F &&f)
     }
 }
 
-// Launch q = A p (+ partial p.q) for the topology's stride and lane group.
+// Launch q = A p (+ partial p.q) for the topology's stride and lane group;
+// `done` (nullable) stops it, `fin` (nullable) receives pq and alpha.
 template <typename T>
-void launch_spmv_pq(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, const PcgCtl *ctl, cudaStream_t st)
+void launch_spmv_pq(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, const int32_t *done, PcgCtl *fin,
+                    cudaStream_t st)
 {
     auto go = [&](auto g) {
         constexpr int G = decltype(g)::value;
-        if (t->s == 2) k_spmv_pq<2, G, T><<<grid, kVecThreads, 0, st>>>(v, part, ctl);
-        else k_spmv_pq<3, G, T><<<grid, kVecThreads, 0, st>>>(v, part, ctl);
+        if (t->s == 2) k_spmv_pq<2, G, T><<<grid, kVecThreads, 0, st>>>(v, part, done, fin);
+        else k_spmv_pq<3, G, T><<<grid, kVecThreads, 0, st>>>(v, part, done, fin);
     };
     dispatch_group<2, T>(t->spmv_group, go);
     AMIE_LAUNCHED();
@@ -141,9 +145,9 @@ PcgParts parts_of(SolverState *s)
 {
     PcgParts p;
     p.pq = s->parts.p;
-    p.rz[0] = s->parts.p + s->grid;
-    p.rz[1] = s->parts.p + 2 * s->grid;
-    p.rr = s->parts.p + 3 * s->grid;
+    p.rz = s->parts.p + s->grid;
+    p.rr = s->parts.p + 2 * s->grid;
+    p.spare = s->parts.p + 3 * s->grid;
     return p;
 }
 
@@ -160,7 +164,7 @@ PcgVecs<float> vecs_of<float>(amie_topo *t)
     return PcgVecs<float>{bsr32(t), t->invdiag32.p, t->d32.p, t->r32.p, t->z32.p, t->p32.p, t->q32.p};
 }
 
-constexpr int kGraphIters = 16;   // PCG iterations per graph launch (even: parity restarts at 0)
+constexpr int kGraphIters = 16;   // PCG iterations per graph launch
 
 template <typename T>
 amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
@@ -172,12 +176,11 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     cudaGraph_t graph;
     AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int it = 0; it < kGraphIters; it++) {
-        const int parity = it & 1;
-        launch_spmv_pq<T>(t, s->grid, v, parts.pq, s->ctl.p, st);
-        k_update<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts, parity, s->ctl.p);
-        k_direction<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts, parity, s->ctl.p);
-        g_launches += 2;
+        launch_spmv_pq<T>(t, s->grid, v, parts.pq, &s->ctl.p->done, s->ctl.p, st);
+        k_update<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts, s->ctl.p);
+        k_direction<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, s->ctl.p);
     }
+    g_launches -= kGraphIters;   // captured, not launched: counted per graph launch
     AMIE_CUDA(cudaStreamEndCapture(st, &graph));
     cudaError_t e = cudaGraphInstantiate(g, graph, 0);
     cudaGraphDestroy(graph);
@@ -214,15 +217,16 @@ amie_status run_pcg(amie_topo *t, SolverState *s, double tol2, int64_t maxit, in
     PcgParts parts = parts_of(s);
     cudaGraphExec_t *g = sizeof(T) == 8 ? &s->graph64 : &s->graph32;
     AMIE_TRY(graph_for<T>(t, s, g));
-    k_pcg_start<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts);
-    AMIE_LAUNCHED();
     PcgCtl init{};
     init.done = 0;
+    init.ticket = 0;
     init.iterations = 0;
     init.maxit = maxit;
     init.tol2 = tol2;
     *s->h_ctl = init;
     AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
+    k_pcg_start<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts, s->ctl.p);   // rz, rr into the control block
+    AMIE_LAUNCHED();
     // The pinned copy is rewritten below only after this copy has completed.
     AMIE_CUDA(cudaStreamSynchronize(st));
     // Host watchdog: the device sets `done` by maxit at the latest, so more
@@ -443,8 +447,8 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     PcgParts parts = parts_of(s);
     for (int i = 0; i <= reps; i++) {   // launch 0 is a warm-up
         if (i == 1) AMIE_CUDA(cudaEventRecord(t->ctx->ev0, st));
-        if (precision == 64) launch_spmv_pq<double>(t, s->grid, vecs_of<double>(t), parts.pq, nullptr, st);
-        else launch_spmv_pq<float>(t, s->grid, vecs_of<float>(t), parts.pq, nullptr, st);
+        if (precision == 64) launch_spmv_pq<double>(t, s->grid, vecs_of<double>(t), parts.pq, nullptr, nullptr, st);
+        else launch_spmv_pq<float>(t, s->grid, vecs_of<float>(t), parts.pq, nullptr, nullptr, st);
     }
     AMIE_CUDA(cudaEventRecord(t->ctx->ev1, st));
     AMIE_CUDA(cudaEventSynchronize(t->ctx->ev1));
