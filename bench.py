@@ -59,8 +59,11 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg1", choices=["cfg0", "cfg1", "cfg2"])
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--inner-rtol", type=float, default=0.0,
+                    help="mixed: FP32 residual reduction between FP64 residual replacements (0 = library default)")
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--size", type=int, default=0, help="override the mesh resolution (cells per side)")
+    ap.add_argument("--reps", type=int, default=1, help="--profile: timed SpMV launches per precision")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
@@ -311,9 +314,9 @@ def run_ours(args, world, rank, local, dist):
         return 0
     if args.profile:
         # few launches for an ncu capture: 2 FP32 and 2 FP64 SpMV(+dot) launches after one assembly
-        ms32 = topo.profile_spmv(32, 1)
-        ms64 = topo.profile_spmv(64, 1)
-        print(json.dumps({"profile": name, "n_dof": int(n), "nnzb": int(topo.nnzb), "ms_spmv32": ms32,
+        ms32 = topo.profile_spmv(32, args.reps)
+        ms64 = topo.profile_spmv(64, args.reps)
+        print(json.dumps({"profile": name, "n_dof": int(n), "nnzb": int(topo.nnzb), "reps": args.reps, "ms_spmv32": ms32,
                           "ms_spmv64": ms64, "alg_bytes32": spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 4),
                           "alg_bytes64": spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 8)}))
         topo.close()
@@ -323,7 +326,7 @@ def run_ours(args, world, rank, local, dist):
     def step(sv=solver, rtol=args.rtol):
         ctx.timer_start()
         topo.assemble()                       # quadrature + gather + stored Dirichlet elimination
-        st = topo.solve_resident(sv, rtol=rtol)
+        st = topo.solve_resident(sv, rtol=rtol, inner_rtol=args.inner_rtol)
         ms = ctx.timer_stop()
         return ms, st
 
@@ -518,8 +521,7 @@ def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 6
 
 
 def topo_group(topo):
-    avg = topo.nnzb / max(1, topo.n_rows)
-    return 4 if avg <= 4.5 else 8 if avg <= 9 else 16 if avg <= 18 else 32
+    return topo.spmv_lanes()
 
 
 def main():

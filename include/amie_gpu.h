@@ -112,7 +112,8 @@ typedef struct amie_solve_opts {
     double eps;                  /* AMIE_CG absolute tolerance (Assembly::setEpsilon); default 1e-10 */
     int32_t nssor;               /* AMIE_CG smoothing sweeps (Assembly::setSSORIterations); default 32 */
     int64_t maxit;               /* iteration cap; <= 0 = reference default n/2 (AMIE_CG) / 20 n (PCG) */
-    double inner_rtol;           /* MIXED: FP32 inner solve reduction per refinement step; default 1e-5 */
+    double inner_rtol;           /* MIXED: FP32 residual reduction between two FP64 residual replacements
+                                    (reliable updates); <= 0 = default 0.1 */
     int32_t use_x0;              /* 1 = start from x_inout (Assembly::extrapolate warm start) */
 } amie_solve_opts;
 
@@ -140,6 +141,10 @@ AMIE_API amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh, a
 AMIE_API amie_status amie_topology_destroy(amie_topo *topo);
 /* n_rows = block rows, nnzb = stored blocks, n = n_rows * stride scalar DOFs. */
 AMIE_API amie_status amie_topology_sizes(const amie_topo *topo, uint32_t *n_rows, uint64_t *nnzb, uint64_t *n);
+/* Lanes per block row the block SpMV uses for this topology (1, 2, 4, 8, 16 or 32),
+ * chosen from the blocks per row at topology build.  No reference counterpart:
+ * a kernel-configuration query for reports. */
+AMIE_API amie_status amie_topology_spmv_lanes(const amie_topo *topo, int32_t *lanes);
 /* row_size [n_rows] and column_index [nnzb] of CoordinateIndexedSparseMatrix
  * (sparse/sparse_matrix.h:129-179). */
 AMIE_API amie_status amie_topology_pattern(const amie_topo *topo, uint32_t *row_size, uint32_t *column_index);

@@ -34,6 +34,7 @@ EXPORTED = [
     "amie_solve_resident", "amie_solution_download", "amie_server_start", "amie_submit", "amie_poll",
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
     "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step", "amie_pcg_solve_noalloc",
+    "amie_topology_spmv_lanes",
 ]
 
 
@@ -191,6 +192,11 @@ class Topology:
         except Exception:
             pass
 
+    def spmv_lanes(self):
+        g = C.c_int32()
+        check(lib().amie_topology_spmv_lanes(self.ptr, C.byref(g)), "amie_topology_spmv_lanes")
+        return g.value
+
     def pattern(self):
         rs = np.zeros(self.n_rows, np.uint32)
         ci = np.zeros(self.nnzb, np.uint32)
@@ -233,7 +239,7 @@ class Topology:
         return y
 
     def solve(self, solver=SOLVER_PCG_FP64, rtol=1e-10, x0=None, maxit=0, eps=1e-10, nssor=32,
-              inner_rtol=1e-5, accept=(AMIE_OK,)):
+              inner_rtol=0.0, accept=(AMIE_OK,)):
         x = np.zeros(self.n, np.float64) if x0 is None else np.array(x0, np.float64, copy=True)
         opts = SolveOpts(solver, rtol, eps, nssor, maxit, inner_rtol, 1 if x0 is not None else 0)
         st = SolveStats()
@@ -241,7 +247,7 @@ class Topology:
         check(rc, "amie_solve", ok=accept)
         return x, st.as_dict()
 
-    def solve_resident(self, solver=SOLVER_PCG_FP64, rtol=1e-10, maxit=0, inner_rtol=1e-5, use_x0=False,
+    def solve_resident(self, solver=SOLVER_PCG_FP64, rtol=1e-10, maxit=0, inner_rtol=0.0, use_x0=False,
                        accept=(AMIE_OK,)):
         opts = SolveOpts(solver, rtol, 1e-10, 32, maxit, inner_rtol, 1 if use_x0 else 0)
         st = SolveStats()

@@ -139,6 +139,7 @@ amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_sta
 {
     SolverState *s = nullptr;
     AMIE_TRY(ensure_state(t, false, &s));
+    AMIE_TRY(ensure_sell(t, true, false));
     cudaStream_t st = t->ctx->stream;
     const uint64_t n = t->n;
     const int grid = s->grid;

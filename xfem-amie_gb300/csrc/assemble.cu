@@ -391,6 +391,45 @@ __global__ void k_to_amie_layout(uint64_t nnzb, const double *val, double *out)
 
 inline unsigned blocks_for(uint64_t n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// SELL slots of one slice per warp: block index (kSellNone for padding) and column.
+__global__ void k_sell_fill(uint32_t n_rows, uint32_t n_slices, const uint32_t *perm, const uint64_t *slice_ptr,
+                            const uint32_t *row_ptr, const uint32_t *col, uint32_t *sell_blk, uint32_t *sell_col)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t sl = warp; sl < n_slices; sl += n_warps) {
+        const uint32_t row = perm[sl * 32 + lane];
+        const uint32_t b = row < n_rows ? row_ptr[row] : 0u, e = row < n_rows ? row_ptr[row + 1] : 0u;
+        const uint64_t g0 = slice_ptr[sl];
+        const uint32_t len = (uint32_t)((slice_ptr[sl + 1] - g0) >> 5);
+        for (uint32_t j = 0; j < len; j++) {
+            const uint64_t slot = g0 + (uint64_t)j * 32 + lane;
+            const bool real = b + j < e;
+            sell_blk[slot] = real ? b + j : kSellNone;
+            sell_col[slot] = real ? col[b + j] : (row < n_rows ? row : 0u);
+        }
+    }
+}
+
+// Copy of the BSR values (row-major s x s blocks) into the chunked SELL layout.
+template <int S, typename T>
+__global__ void k_to_sell(uint64_t n_slots, const uint32_t *sell_blk, const double *val, T *out)
+{
+    constexpr int V = kSellVec<S, T>;
+    for (uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots;
+         slot += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t blk = sell_blk[slot];
+        T *group = out + (slot & ~uint64_t(31)) * (S * S);
+        const uint32_t lane = (uint32_t)(slot & 31);
+#pragma unroll
+        for (int c = 0; c < S * S; c++) {
+            const double v = blk != kSellNone ? val[(uint64_t)blk * (S * S) + c] : 0.0;
+            group[32 * V * (c / V) + V * lane + c % V] = (T)v;
+        }
+    }
+}
+
 template <typename T>
 amie_status upload(amie_ctx *ctx, DevArray<T> &d, const T *h, size_t n)
 {
@@ -644,11 +683,50 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
 
     // rows ~ blocks per row -> lanes per block row in the SpMV
     const double avg = (double)t->nnzb / t->n_rows;
-    t->spmv_group = avg <= 4.5 ? 2 : avg <= 9 ? 2 : avg <= 18 ? 4 : 8;
-    // tuning override for measurements: AMIE_SPMV_GROUP = 1, 2, 4, 8, 16 or 32 lanes per block row
+    t->spmv_group = avg <= 12 ? 1 : avg <= 24 ? 2 : 4;
+    // tuning overrides for measurements: AMIE_SPMV_GROUP = 1, 2, 4, 8, 16 or 32 lanes per
+    // block row (block-CSR kernel); AMIE_SELL_VARIANT = 0..5 (SELL kernel loop, see amie_topo)
     if (const char *g = std::getenv("AMIE_SPMV_GROUP")) {
         const int v = std::atoi(g);
         if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16 || v == 32) t->spmv_group = v;
+    }
+    if (const char *g = std::getenv("AMIE_SELL_VARIANT")) {
+        const int v = std::atoi(g);
+        if (v >= 0 && v <= 5) t->sell_variant = v;
+    }
+
+    // SELL-32-sigma structure: rows sorted by length inside windows, slices of 32
+    {
+        std::vector<uint32_t> h_rp(t->n_rows + 1);
+        AMIE_CUDA(cudaMemcpyAsync(h_rp.data(), t->row_ptr.p, h_rp.size() * 4, cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));
+        t->n_slices = (t->n_rows + 31) / 32;
+        std::vector<uint32_t> perm((size_t)t->n_slices * 32, t->n_rows);
+        std::vector<uint64_t> sptr(t->n_slices + 1, 0);
+        for (uint32_t w0 = 0; w0 < t->n_rows; w0 += kSellSigma) {
+            const uint32_t w1 = std::min<uint32_t>(t->n_rows, w0 + kSellSigma);
+            for (uint32_t r = w0; r < w1; r++) perm[r] = r;
+            std::stable_sort(perm.begin() + w0, perm.begin() + w1, [&](uint32_t a, uint32_t b) {
+                return h_rp[a + 1] - h_rp[a] > h_rp[b + 1] - h_rp[b];
+            });
+        }
+        for (uint32_t sl = 0; sl < t->n_slices; sl++) {
+            uint32_t len = 0;
+            for (uint32_t l = 0; l < 32; l++) {
+                const uint32_t r = perm[(size_t)sl * 32 + l];
+                if (r < t->n_rows) len = std::max(len, h_rp[r + 1] - h_rp[r]);
+            }
+            sptr[sl + 1] = sptr[sl] + 32ull * len;
+        }
+        t->n_slots = sptr[t->n_slices];
+        if ((rc = upload(ctx, t->sell_perm, perm.data(), perm.size())) ||
+            (rc = upload(ctx, t->sell_ptr, sptr.data(), sptr.size())) ||
+            (rc = t->sell_blk.alloc(ctx, t->n_slots)) || (rc = t->sell_col.alloc(ctx, t->n_slots)))
+            return fail(rc);
+        k_sell_fill<<<t->ctx->num_sms * 8, 256, 0, st>>>(t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p,
+                                                         t->row_ptr.p, t->col.p, t->sell_blk.p, t->sell_col.p);
+        g_launches += 1;
+        AMIE_CUDA(cudaGetLastError());
     }
 
     // matrix, vectors and staging
@@ -685,6 +763,13 @@ extern "C" amie_status amie_topology_sizes(const amie_topo *t, uint32_t *n_rows,
     if (n_rows) *n_rows = t->n_rows;
     if (nnzb) *nnzb = t->nnzb;
     if (n) *n = t->n;
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_topology_spmv_lanes(const amie_topo *t, int32_t *lanes)
+{
+    if (!t || !lanes) return AMIE_BAD_INPUT;
+    *lanes = t->spmv_group;
     return AMIE_OK;
 }
 
@@ -748,6 +833,8 @@ amie_status finalize_matrix_async(amie_topo *t, bool want32)
 {
     cudaStream_t st = t->ctx->stream;
     const uint64_t n = t->n;
+    t->sell64_ok = false;
+    t->sell32_ok = false;
     float *inv32 = nullptr;
     if (want32) {
         if (!t->val32.p) AMIE_TRY(t->val32.alloc(t->ctx, t->nnzb * t->s * t->s));
@@ -763,6 +850,29 @@ amie_status finalize_matrix_async(amie_topo *t, bool want32)
         k_to_f32<<<t->ctx->num_sms * 8, 256, 0, st>>>(t->nnzb * t->s * t->s, t->val.p, t->val32.p);
         AMIE_LAUNCHED();
         t->have32 = true;
+    }
+    AMIE_CUDA(cudaGetLastError());
+    return AMIE_OK;
+}
+
+// SELL values of the current matrix in FP64 and/or FP32 (allocated on first use).
+amie_status ensure_sell(amie_topo *t, bool want64, bool want32)
+{
+    cudaStream_t st = t->ctx->stream;
+    const int g = t->ctx->num_sms * 8;
+    if (want64 && !t->sell64_ok) {
+        if (!t->sell_val.p) AMIE_TRY(t->sell_val.alloc(t->ctx, t->n_slots * t->s * t->s));
+        if (t->s == 2) k_to_sell<2, double><<<g, 256, 0, st>>>(t->n_slots, t->sell_blk.p, t->val.p, t->sell_val.p);
+        else k_to_sell<3, double><<<g, 256, 0, st>>>(t->n_slots, t->sell_blk.p, t->val.p, t->sell_val.p);
+        AMIE_LAUNCHED();
+        t->sell64_ok = true;
+    }
+    if (want32 && !t->sell32_ok) {
+        if (!t->sell_val32.p) AMIE_TRY(t->sell_val32.alloc(t->ctx, t->n_slots * t->s * t->s));
+        if (t->s == 2) k_to_sell<2, float><<<g, 256, 0, st>>>(t->n_slots, t->sell_blk.p, t->val.p, t->sell_val32.p);
+        else k_to_sell<3, float><<<g, 256, 0, st>>>(t->n_slots, t->sell_blk.p, t->val.p, t->sell_val32.p);
+        AMIE_LAUNCHED();
+        t->sell32_ok = true;
     }
     AMIE_CUDA(cudaGetLastError());
     return AMIE_OK;

@@ -113,6 +113,28 @@ struct BsrView {
     const T *val;
 };
 
+// Sliced-ELL copy of a block-CSR matrix (SELL-32-sigma): block rows are
+// sorted by length (descending, stable) inside windows of kSellSigma rows and
+// cut into slices of 32; slice k holds 32 rows padded to its longest row, its
+// slots stored j-major (slot = slice_ptr[k] + 32 j + lane) so a warp reads the
+// j-th block of its 32 rows from one contiguous run.  Values of the 32 blocks
+// of one j are stored in chunks of kSellVec<S,T> components: component c of
+// lane l at val[32*S*S*(group) + 32*V*(c / V) + V*l + c % V].  Padding slots
+// have zero values and the row's own column (no effect on the result).
+constexpr uint32_t kSellSigma = 1024;
+constexpr uint32_t kSellNone = 0xffffffffu;
+template <int S, typename T>
+constexpr int kSellVec = S == 2 ? int(16 / sizeof(T)) : 1;
+
+template <typename T>
+struct SellView {
+    uint32_t n_rows, n_slices;
+    const uint32_t *perm;        // [32 * n_slices] block row of each lane (n_rows = padding)
+    const uint64_t *slice_ptr;   // [n_slices + 1] first slot of each slice
+    const uint32_t *col;         // [slots] block column
+    const T *val;                // [slots * S * S] chunked as above
+};
+
 }  // namespace amie
 
 // Opaque handles of the C-ABI.
@@ -149,6 +171,18 @@ struct amie_topo {
     amie::DevArray<float> invdiag32;
     bool assembled = false, eliminated = false, have32 = false;
     int spmv_group = 8;
+    // SELL-32-sigma copy used by the solver SpMV (values converted on demand
+    // after each change of the matrix)
+    amie::DevArray<uint32_t> sell_perm, sell_col, sell_blk;   // sell_blk: BSR block per slot or kSellNone
+    amie::DevArray<uint64_t> sell_ptr;
+    amie::DevArray<double> sell_val;
+    amie::DevArray<float> sell_val32;
+    uint32_t n_slices = 0;
+    uint64_t n_slots = 0;
+    bool sell64_ok = false, sell32_ok = false;
+    // SELL SpMV loop: 0 = 4 slots per step, 1 = 8, 2 = 2 pipelined, 3 = 4 pipelined,
+    // 4 / 5 = 0 / 2 with registers capped for 5 CTAs per SM (2x2 FP32 blocks)
+    int sell_variant = 0;
 
     // right-hand side, solution and solver work vectors
     amie::DevArray<double> rhs, x, r, z, p, q, xc, rc, red;

@@ -343,8 +343,8 @@ struct ServerOps {
         AMIE_LAUNCHED();
         double bb = 0.0, rr = 0.0;
         AMIE_TRY(read_sum_on(st, s->parts.p, s->grid, &bb));
-        launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->grid, st);
-        AMIE_TRY(read_sum_on(st, s->parts.p + 3 * s->grid, s->grid, &rr));
+        launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->stride, st);
+        AMIE_TRY(read_sum_on(st, s->parts.p + 3 * s->stride, s->grid, &rr));
         r->bnorm = std::sqrt(bb);
         r->rnorm = std::sqrt(rr);
         return AMIE_OK;
@@ -487,8 +487,8 @@ struct ServerOps {
             r->refinements++;
         }
         double rr = 0.0;
-        launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->grid, st);
-        AMIE_TRY(read_sum_on(st, s->parts.p + 3 * s->grid, s->grid, &rr));
+        launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->stride, st);
+        AMIE_TRY(read_sum_on(st, s->parts.p + 3 * s->stride, s->grid, &rr));
         r->rnorm = std::sqrt(rr);
         const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
         if (!(rr == rr)) return retire(srv, r, AMIE_NAN);

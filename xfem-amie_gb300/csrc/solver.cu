@@ -3,10 +3,12 @@
 //
 //   AMIE_SOLVER_PCG_FP64   Jacobi-PCG in FP64, relative-residual stop, restarted
 //                          from the true residual b - A x if the recursive one drifted.
-//   AMIE_SOLVER_PCG_MIXED  FP64 iterative refinement: r = b - A x (FP64), inner
-//                          FP32 Jacobi-PCG on A d = r/|r| with FP32 SpMV, FP32
-//                          preconditioner and FP32 direction updates, then
-//                          x += |r| d accumulated in FP64.
+//   AMIE_SOLVER_PCG_MIXED  FP32 Jacobi-PCG (FP32 SpMV, preconditioner and vector
+//                          updates) with reliable updates: whenever the FP32
+//                          recursive residual has dropped by inner_rtol, the FP32
+//                          increment is added to x in FP64, r = b - A x is
+//                          recomputed in FP64 and the FP32 run continues from it
+//                          with its search direction kept (no Krylov restart).
 //   AMIE_SOLVER_AMIE_CG    ConjugateGradient::solve semantics (amie_cg.cu).
 #include "solver.cuh"
 
@@ -22,8 +24,11 @@ amie_status finalize_matrix_async(amie_topo *t, bool want32);
 amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *st);
 
 struct SolverState {
-    int grid = 0;
-    DevArray<double> parts;       // 4 * grid
+    int grid = 0;                 // block-CSR SpMV, AMIE_CG and server kernels
+    int grid_vec = 0;             // PCG vector kernels (full occupancy)
+    int grid_sell[2] = {0, 0};    // SELL SpMV, FP32 / FP64 (resident CTAs of that kernel)
+    int stride = 0;               // partials per kind in `parts` (the largest grid)
+    DevArray<double> parts;       // 4 * stride: pq, rz, rr, spare
     DevArray<PcgCtl> ctl;
     PcgCtl *h_ctl = nullptr;      // pinned
     cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
@@ -69,12 +74,63 @@ void dispatch_group(int group, F &&f)
     }
 }
 
-// Launch q = A p (+ partial p.q) for the topology's stride and lane group;
-// `done` (nullable) stops it, `fin` (nullable) receives pq and alpha.
+amie_status ensure_sell(amie_topo *t, bool want64, bool want32);
+
+// SELL copy of the current matrix in precision T (val == nullptr if not converted).
+template <typename T>
+SellView<T> sell_of(amie_topo *t);
+template <>
+SellView<double> sell_of<double>(amie_topo *t)
+{
+    return SellView<double>{t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p, t->sell_col.p,
+                            t->sell64_ok ? t->sell_val.p : nullptr};
+}
+template <>
+SellView<float> sell_of<float>(amie_topo *t)
+{
+    return SellView<float>{t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p, t->sell_col.p,
+                           t->sell32_ok ? t->sell_val32.p : nullptr};
+}
+
+template <typename T>
+using SellKernel = void (*)(SellView<T>, const T *, T *, double *, const int32_t *, PcgCtl *);
+
+// SELL SpMV kernel for block size s and loop variant (see amie_topo::sell_variant).
+template <typename T>
+SellKernel<T> sell_kernel(int s, int variant)
+{
+    if (s == 2) {
+        switch (variant) {
+        case 1: return k_sell_pq<2, 8, false, 1, T>;
+        case 2: return k_sell_pq<2, 2, true, 1, T>;
+        case 3: return k_sell_pq<2, 4, true, 1, T>;
+        case 4: return k_sell_pq<2, 4, false, 5, T>;
+        case 5: return k_sell_pq<2, 2, true, 5, T>;
+        default: return k_sell_pq<2, 4, false, 1, T>;
+        }
+    }
+    switch (variant) {
+    case 1: return k_sell_pq<3, 8, false, 1, T>;
+    case 2: case 5: return k_sell_pq<3, 2, true, 1, T>;
+    case 3: return k_sell_pq<3, 4, true, 1, T>;
+    default: return k_sell_pq<3, 4, false, 1, T>;
+    }
+}
+
+// Launch q = A p (+ partial p.q): on the SELL copy when it is current (see
+// ensure_sell), else on the block-CSR matrix with the topology's lane group;
+// `done` (nullable) stops it, `fin` (nullable) receives pq and alpha.  The
+// kernel writes `grid` partials.
 template <typename T>
 void launch_spmv_pq(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, const int32_t *done, PcgCtl *fin,
                     cudaStream_t st)
 {
+    const SellView<T> sv = sell_of<T>(t);
+    if (sv.val) {
+        sell_kernel<T>(t->s, t->sell_variant)<<<grid, kVecThreads, 0, st>>>(sv, v.p, v.q, part, done, fin);
+        AMIE_LAUNCHED();
+        return;
+    }
     auto go = [&](auto g) {
         constexpr int G = decltype(g)::value;
         if (t->s == 2) k_spmv_pq<2, G, T><<<grid, kVecThreads, 0, st>>>(v, part, done, fin);
@@ -120,7 +176,16 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         dispatch_group<2, double>(t->spmv_group, occ);
         per_sm = std::max(1, std::min(per_sm, 8));
         s->grid = t->ctx->num_sms * per_sm;
-        AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->grid));
+        auto resident = [&](const void *f) {
+            int k = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kVecThreads, 0);
+            return t->ctx->num_sms * std::max(1, std::min(k, 8));
+        };
+        s->grid_sell[0] = resident((const void *)sell_kernel<float>(t->s, t->sell_variant));
+        s->grid_sell[1] = resident((const void *)sell_kernel<double>(t->s, t->sell_variant));
+        s->grid_vec = resident((const void *)k_update<double>);
+        s->stride = std::max(std::max(s->grid, s->grid_vec), std::max(s->grid_sell[0], s->grid_sell[1]));
+        AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->stride));
         AMIE_TRY(s->ctl.alloc(t->ctx, 1));
         AMIE_CUDA(cudaMallocHost((void **)&s->h_ctl, sizeof(PcgCtl)));
         const uint64_t n = t->n;
@@ -145,9 +210,9 @@ PcgParts parts_of(SolverState *s)
 {
     PcgParts p;
     p.pq = s->parts.p;
-    p.rz = s->parts.p + s->grid;
-    p.rr = s->parts.p + 2 * s->grid;
-    p.spare = s->parts.p + 3 * s->grid;
+    p.rz = s->parts.p + s->stride;
+    p.rr = s->parts.p + 2 * s->stride;
+    p.spare = s->parts.p + 3 * s->stride;
     return p;
 }
 
@@ -175,10 +240,11 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     PcgParts parts = parts_of(s);
     cudaGraph_t graph;
     AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int gs = s->grid_sell[sizeof(T) == 8 ? 1 : 0];
     for (int it = 0; it < kGraphIters; it++) {
-        launch_spmv_pq<T>(t, s->grid, v, parts.pq, &s->ctl.p->done, s->ctl.p, st);
-        k_update<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts, s->ctl.p);
-        k_direction<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, s->ctl.p);
+        launch_spmv_pq<T>(t, gs, v, parts.pq, &s->ctl.p->done, s->ctl.p, st);
+        k_update<T><<<s->grid_vec, kVecThreads, 0, st>>>(v, t->n, parts, s->ctl.p);
+        k_direction<T><<<s->grid_vec, kVecThreads, 0, st>>>(v, t->n, s->ctl.p);
     }
     g_launches -= kGraphIters;   // captured, not launched: counted per graph launch
     AMIE_CUDA(cudaStreamEndCapture(st, &graph));
@@ -208,27 +274,13 @@ amie_status read_sum(amie_topo *t, const double *dev, int n, double *out)
     return AMIE_OK;
 }
 
-// One PCG run from the residual already in v.r; stops when r.r <= tol2 or after maxit iterations.
+// Launches the PCG graph until the control block reports done.
 template <typename T>
-amie_status run_pcg(amie_topo *t, SolverState *s, double tol2, int64_t maxit, int64_t *iters, double *rr_out)
+amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iters, double *rr_out)
 {
     cudaStream_t st = t->ctx->stream;
-    PcgVecs<T> v = vecs_of<T>(t);
-    PcgParts parts = parts_of(s);
     cudaGraphExec_t *g = sizeof(T) == 8 ? &s->graph64 : &s->graph32;
     AMIE_TRY(graph_for<T>(t, s, g));
-    PcgCtl init{};
-    init.done = 0;
-    init.ticket = 0;
-    init.iterations = 0;
-    init.maxit = maxit;
-    init.tol2 = tol2;
-    *s->h_ctl = init;
-    AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
-    k_pcg_start<T><<<s->grid, kVecThreads, 0, st>>>(v, t->n, parts, s->ctl.p);   // rz, rr into the control block
-    AMIE_LAUNCHED();
-    // The pinned copy is rewritten below only after this copy has completed.
-    AMIE_CUDA(cudaStreamSynchronize(st));
     // Host watchdog: the device sets `done` by maxit at the latest, so more
     // launches than maxit / kGraphIters + 2 mean the control block is not advancing.
     const int64_t max_launches = maxit / kGraphIters + 2;
@@ -248,6 +300,41 @@ amie_status run_pcg(amie_topo *t, SolverState *s, double tol2, int64_t maxit, in
     *iters = s->h_ctl->iterations;
     *rr_out = s->h_ctl->rr;
     return AMIE_OK;
+}
+
+// One PCG run from the residual already in v.r; stops when r.r <= tol2 or after maxit iterations.
+template <typename T>
+amie_status run_pcg(amie_topo *t, SolverState *s, double tol2, int64_t maxit, int64_t *iters, double *rr_out)
+{
+    cudaStream_t st = t->ctx->stream;
+    PcgCtl init{};
+    init.done = 0;
+    init.ticket = 0;
+    init.iterations = 0;
+    init.maxit = maxit;
+    init.tol2 = tol2;
+    *s->h_ctl = init;
+    AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
+    k_pcg_start<T><<<s->grid_vec, kVecThreads, 0, st>>>(vecs_of<T>(t), t->n, parts_of(s), s->ctl.p);   // rz, rr
+    AMIE_LAUNCHED();
+    // The pinned copy is rewritten by drive_pcg only after this copy has completed.
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    return drive_pcg<T>(t, s, maxit, iters, rr_out);
+}
+
+// Continues a stopped run whose residual v.r was replaced (rescaled by
+// `ratio`, see k_pcg_resume) with the previous search direction kept.
+template <typename T>
+amie_status resume_pcg(amie_topo *t, SolverState *s, double ratio, double tol2, int64_t maxit, int64_t *iters,
+                       double *rr_out)
+{
+    cudaStream_t st = t->ctx->stream;
+    const PcgVecs<T> v = vecs_of<T>(t);
+    k_pcg_resume<T><<<s->grid_vec, kVecThreads, 0, st>>>(v, t->n, parts_of(s), s->ctl.p, ratio, tol2, maxit);
+    k_direction<T><<<s->grid_vec, kVecThreads, 0, st>>>(v, t->n, s->ctl.p);
+    g_launches += 2;
+    AMIE_CUDA(cudaGetLastError());
+    return drive_pcg<T>(t, s, maxit, iters, rr_out);
 }
 
 __global__ void k_scale_to_f32(uint64_t n, const double *r, double inv, float *r32, float *d32)
@@ -277,9 +364,9 @@ __global__ void k_norm2_parts(uint64_t n, const double *v, double *part)
 // r = b - A x in FP64; returns r.r.
 amie_status true_residual(amie_topo *t, SolverState *s, double *rr)
 {
-    launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->grid, t->ctx->stream);
+    launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->stride, t->ctx->stream);
     AMIE_CUDA(cudaGetLastError());
-    return read_sum(t, s->parts.p + 3 * s->grid, s->grid, rr);
+    return read_sum(t, s->parts.p + 3 * s->stride, s->grid, rr);
 }
 
 amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *st_out, bool mixed)
@@ -287,10 +374,11 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
     SolverState *s = nullptr;
     AMIE_TRY(ensure_state(t, mixed, &s));
     if (mixed && !t->have32) AMIE_TRY(finalize_matrix_async(t, true));
+    AMIE_TRY(ensure_sell(t, !mixed, mixed));   // before any graph of this topology is captured
     cudaStream_t st = t->ctx->stream;
     const double rtol = o && o->rtol > 0 ? o->rtol : 1e-10;
     const int64_t maxit = o && o->maxit > 0 ? o->maxit : std::max<int64_t>(1000, (int64_t)t->n);
-    const double inner_rtol = o && o->inner_rtol > 0 ? o->inner_rtol : 1e-5;
+    const double inner_rtol = o && o->inner_rtol > 0 ? o->inner_rtol : 0.1;
     k_norm2_parts<<<s->grid, kVecThreads, 0, st>>>(t->n, t->rhs.p, s->parts.p);
     AMIE_LAUNCHED();
     double bb = 0.0;
@@ -308,6 +396,7 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
     double rr = 0.0;
     AMIE_TRY(true_residual(t, s, &rr));
     int64_t total = 0;
+    double prev_norm = 0.0;   // MIXED: scale of the FP32 run's vectors (0 = no run yet)
     const double target2 = (rtol * bnorm) * (rtol * bnorm);
     amie_status result = AMIE_NOT_CONVERGED;
     for (int outer = 0; outer < 200; outer++) {
@@ -320,13 +409,22 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
             // recursive residual target a little below the true one: the true residual is re-checked
             AMIE_TRY(run_pcg<double>(t, s, target2 * 0.25, maxit - total, &it, &rr_in));
         } else {
+            // FP32 PCG on the residual scaled to unit norm; at each return the FP32
+            // increment is added to x in FP64, r is replaced by the true FP64
+            // residual and the FP32 run resumes with its search direction kept.
             const double norm = std::sqrt(rr);
             k_scale_to_f32<<<s->grid, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / norm, t->r32.p, t->d32.p);
             AMIE_LAUNCHED();
             // reduce by inner_rtol, or by less when that is all the outer target still needs
             const double need = 0.3 * rtol * bnorm / norm;
             const double inner = std::min(0.5, std::max(inner_rtol, need));
-            AMIE_TRY(run_pcg<float>(t, s, inner * inner, maxit - total, &it, &rr_in));
+            // keep the search direction only while replacements show real progress; a
+            // true residual that fell by less than half means the FP32 recursion has
+            // drifted from it, and the run restarts from the new residual instead
+            if (prev_norm == 0.0 || norm > 0.5 * prev_norm)
+                AMIE_TRY(run_pcg<float>(t, s, inner * inner, maxit - total, &it, &rr_in));
+            else AMIE_TRY(resume_pcg<float>(t, s, norm / prev_norm, inner * inner, maxit - total, &it, &rr_in));
+            prev_norm = norm;
             k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, norm, t->x.p);
             AMIE_LAUNCHED();
             st_out->refinements++;
@@ -440,6 +538,7 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     SolverState *s = nullptr;
     AMIE_TRY(ensure_state(t, precision == 32, &s));
     if (precision == 32 && !t->have32) AMIE_TRY(finalize_matrix_async(t, true));
+    AMIE_TRY(ensure_sell(t, precision == 64, precision == 32));
     cudaStream_t st = t->ctx->stream;
     // p = 1 keeps the inputs defined; the kernel's cost does not depend on the values
     if (precision == 64) AMIE_CUDA(cudaMemsetAsync(t->p.p, 0, t->n * 8, st));
@@ -447,8 +546,8 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     PcgParts parts = parts_of(s);
     for (int i = 0; i <= reps; i++) {   // launch 0 is a warm-up
         if (i == 1) AMIE_CUDA(cudaEventRecord(t->ctx->ev0, st));
-        if (precision == 64) launch_spmv_pq<double>(t, s->grid, vecs_of<double>(t), parts.pq, nullptr, nullptr, st);
-        else launch_spmv_pq<float>(t, s->grid, vecs_of<float>(t), parts.pq, nullptr, nullptr, st);
+        if (precision == 64) launch_spmv_pq<double>(t, s->grid_sell[1], vecs_of<double>(t), parts.pq, nullptr, nullptr, st);
+        else launch_spmv_pq<float>(t, s->grid_sell[0], vecs_of<float>(t), parts.pq, nullptr, nullptr, st);
     }
     AMIE_CUDA(cudaEventRecord(t->ctx->ev1, st));
     AMIE_CUDA(cudaEventSynchronize(t->ctx->ev1));

@@ -35,6 +35,7 @@ struct PcgCtl {
     int64_t maxit;         // iteration cap of the current run
     double tol2;           // stop when r.r <= tol2
     double alpha, beta, rz, rr, pq;
+    double rz_prev;        // r.z of the iteration before the last one (kept for a resumed run)
 };
 
 // Per-CTA partial sums.
@@ -70,6 +71,26 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
     if (w == 0) {
         r = l < (kVecThreads >> 5) ? sh[l] : 0.0;
         r = warp_sum(r);
+    }
+    __syncthreads();
+    return r;
+}
+
+// CTA sum of one value per thread given in the vector precision T: the warp
+// levels add in T, the per-warp sums in FP64.  Result valid in thread 0.
+template <typename T>
+__device__ __forceinline__ double block_sum_v(T v, double *sh)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = (double)v;
+    __syncthreads();
+    double r = 0.0;
+    if (w == 0) {
+        r = l < (kVecThreads >> 5) ? sh[l] : 0.0;
+#pragma unroll
+        for (int o = (kVecThreads >> 6); o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
     }
     __syncthreads();
     return r;
@@ -192,6 +213,22 @@ __device__ __forceinline__ void row_spmv(const BsrView<T> &A, const T *__restric
     }
 }
 
+// Per-CTA partial of p.q; with `fin`, the last CTA stores pq and alpha = rz / pq.
+template <typename T>
+__device__ __forceinline__ void finish_pq(T dot_t, double *part_pq, PcgCtl *fin, double *sh, int *flag)
+{
+    const double dot = block_sum_v<T>(dot_t, sh);
+    if (threadIdx.x == 0) part_pq[blockIdx.x] = dot;
+    if (!fin) return;
+    if (!last_cta(&fin->ticket, flag)) return;
+    const double pq = ordered_sum(part_pq, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+        fin->pq = pq;
+        fin->alpha = pq != 0.0 ? fin->rz / pq : 0.0;
+        fin->ticket = 0;
+    }
+}
+
 // Kernel A: q = A p and per-CTA partial of p.q.  `done` (nullable) stops the
 // kernel; `fin` (nullable) receives pq and alpha = rz / pq from the last CTA.
 template <int S, int G, typename T>
@@ -203,7 +240,7 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv_pq(PcgVecs<T> v, double *p
     constexpr int RPB = kVecThreads / G;
     const int lane = threadIdx.x % G;
     const uint32_t n_rows = v.A.n_rows;
-    double dot = 0.0;
+    T dot = T(0);
     // the trip count depends on the CTA only, so every lane of a warp reaches the shuffles;
     // the next pass's row bounds are fetched while the current row is processed
     uint32_t row = blockIdx.x * RPB + threadIdx.x / G;
@@ -218,23 +255,114 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv_pq(PcgVecs<T> v, double *p
 #pragma unroll
             for (int r = 0; r < S; r++) {
                 v.q[(uint64_t)row * S + r] = acc[r];
-                dot += (double)acc[r] * (double)v.p[(uint64_t)row * S + r];
+                dot = fma(acc[r], v.p[(uint64_t)row * S + r], dot);
             }
         }
         row = nrow;
         b = nb;
         e = ne;
     }
-    dot = block_sum(dot, sh);
-    if (threadIdx.x == 0) part_pq[blockIdx.x] = dot;
-    if (!fin) return;
-    if (!last_cta(&fin->ticket, &flag)) return;
-    const double pq = ordered_sum(part_pq, gridDim.x, sh);
-    if (threadIdx.x == 0) {
-        fin->pq = pq;
-        fin->alpha = pq != 0.0 ? fin->rz / pq : 0.0;
-        fin->ticket = 0;
+    finish_pq<T>(dot, part_pq, fin, sh, &flag);
+}
+
+// One s x s block of the lane's row from a 32-slot SELL group (chunked layout).
+template <int S, typename T>
+__device__ __forceinline__ void load_sell_block(const T *__restrict__ group, uint32_t lane, T blk[S * S])
+{
+    constexpr int V = kSellVec<S, T>;
+    if constexpr (S == 2 && V == 4) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(group) + lane);
+        blk[0] = a.x; blk[1] = a.y; blk[2] = a.z; blk[3] = a.w;
+    } else if constexpr (S == 2 && V == 2) {
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(group) + lane);
+        const double2 b = __ldg(reinterpret_cast<const double2 *>(group + 64) + lane);
+        blk[0] = a.x; blk[1] = a.y; blk[2] = b.x; blk[3] = b.y;
+    } else {
+#pragma unroll
+        for (int c = 0; c < S * S; c++) blk[c] = __ldg(group + 32 * c + lane);
     }
+}
+
+// Columns and blocks of slots j0 .. j0+U-1 of the lane's row (those < len).
+template <int S, int U, typename T>
+__device__ __forceinline__ void load_sell_group(const SellView<T> &A, uint64_t g0, uint32_t j0, uint32_t len,
+                                                uint32_t lane, uint32_t (&c)[U], T (&blk)[U][S * S])
+{
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        if (j0 + u < len) {   // uniform over the warp
+            const uint64_t gs = g0 + (uint64_t)(j0 + u) * 32;
+            c[u] = __ldg(A.col + gs + lane);
+            load_sell_block<S, T>(A.val + gs * (S * S), lane, blk[u]);
+        }
+    }
+}
+
+// Kernel A on the SELL copy: one warp per slice, one lane per block row; every
+// load of blocks and columns is one contiguous run per warp.  U slots are
+// fetched per step; with PIPE the next step's columns and blocks are fetched
+// before the current step's x entries are gathered, so the matrix stream is
+// never idle while x is read.  Blocks of a row are visited in the order of the
+// block-CSR row with the same FMA sequence as row_spmv with one lane per row,
+// so q is bitwise that of k_spmv_pq<S,1,T>.
+// MINB (2x2 FP32 blocks only) asks the compiler for MINB resident CTAs per SM.
+template <int S, int U, bool PIPE, int MINB, typename T>
+__global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB : 1)
+    k_sell_pq(SellView<T> A, const T *__restrict__ x, T *__restrict__ y, double *part_pq, const int32_t *done,
+              PcgCtl *fin)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    if (done && *done) return;
+    constexpr uint32_t WPB = kVecThreads / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    T dot = T(0);   // the thread's few rows in the vector precision (FP64 issue slots are scarce on this part)
+    for (uint32_t sl = blockIdx.x * WPB + (threadIdx.x >> 5); sl < A.n_slices; sl += gridDim.x * WPB) {
+        const uint32_t row = __ldg(A.perm + (uint64_t)sl * 32 + lane);
+        const uint64_t g0 = __ldg(A.slice_ptr + sl);
+        const uint32_t len = (uint32_t)((__ldg(A.slice_ptr + sl + 1) - g0) >> 5);
+        T acc[S];
+#pragma unroll
+        for (int r = 0; r < S; r++) acc[r] = T(0);
+        uint32_t c[U];
+        T blk[U][S * S];
+        if constexpr (PIPE) load_sell_group<S, U, T>(A, g0, 0, len, lane, c, blk);
+        for (uint32_t j0 = 0; j0 < len; j0 += U) {
+            if constexpr (!PIPE) load_sell_group<S, U, T>(A, g0, j0, len, lane, c, blk);
+            T xv[U][S];
+#pragma unroll
+            for (int u = 0; u < U; u++)
+                if (j0 + u < len) load_x<S, T>(x, c[u], xv[u]);
+            uint32_t cn[U];
+            T bn[U][S * S];
+            if constexpr (PIPE) load_sell_group<S, U, T>(A, g0, j0 + U, len, lane, cn, bn);
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+#pragma unroll
+                    for (int r = 0; r < S; r++)
+#pragma unroll
+                        for (int cc = 0; cc < S; cc++) acc[r] = fma(blk[u][r * S + cc], xv[u][cc], acc[r]);
+                }
+            }
+            if constexpr (PIPE) {
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    c[u] = cn[u];
+#pragma unroll
+                    for (int q = 0; q < S * S; q++) blk[u][q] = bn[u][q];
+                }
+            }
+        }
+        if (row < A.n_rows) {
+#pragma unroll
+            for (int r = 0; r < S; r++) {
+                y[(uint64_t)row * S + r] = acc[r];
+                dot = fma(acc[r], x[(uint64_t)row * S + r], dot);
+            }
+        }
+    }
+    finish_pq<T>(dot, part_pq, fin, sh, &flag);
 }
 
 // Plain y = A x (+ optional y = b - A x with partial of y.y).
@@ -266,6 +394,62 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv(BsrView<T> A, const T *x, 
     }
 }
 
+// 16-byte packs of vector entries for the vector kernels.
+template <typename T> struct Pack;
+template <> struct Pack<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Pack<double> { using type = double2; static constexpr int n = 2; };
+
+__device__ __forceinline__ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+template <typename T>
+__device__ __forceinline__ void ld_pack(const T *p, uint64_t i, T (&o)[Pack<T>::n])
+{
+    if constexpr (sizeof(T) == 4) {
+        const float4 a = reinterpret_cast<const float4 *>(p)[i];
+        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    } else {
+        const double2 a = reinterpret_cast<const double2 *>(p)[i];
+        o[0] = a.x; o[1] = a.y;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void ldg_pack(const T *__restrict__ p, uint64_t i, T (&o)[Pack<T>::n])
+{
+    if constexpr (sizeof(T) == 4) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(p) + i);
+        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    } else {
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(p) + i);
+        o[0] = a.x; o[1] = a.y;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void st_pack(T *p, uint64_t i, const T (&o)[Pack<T>::n])
+{
+    if constexpr (sizeof(T) == 4) reinterpret_cast<float4 *>(p)[i] = make_float4(o[0], o[1], o[2], o[3]);
+    else reinterpret_cast<double2 *>(p)[i] = make_double2(o[0], o[1]);
+}
+
+// Runs f(i) for every entry i < n of this thread's share: packs of
+// Pack<T>::n entries (fpack(k) for pack k) when every vector is 16-byte
+// aligned, single entries otherwise and for the tail.
+template <typename T, typename FP, typename FS>
+__device__ __forceinline__ void for_entries(uint64_t n, bool aligned, FP &&fpack, FS &&fone)
+{
+    constexpr int W = Pack<T>::n;
+    const uint64_t tid = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * kVecThreads;
+    uint64_t first = 0;
+    if (aligned) {
+        const uint64_t npk = n / W;
+        for (uint64_t k = tid; k < npk; k += stride) fpack(k);
+        first = npk * W;
+    }
+    for (uint64_t i = first + tid; i < n; i += stride) fone(i);
+}
+
 // Kernel B: x += alpha p; r -= alpha q; z = D^-1 r; partials r.z, r.r.
 // Last CTA: totals, iteration count, stop test, beta = rz_new / rz.
 template <typename T>
@@ -274,22 +458,51 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     __shared__ double sh[33];
     __shared__ int flag;
     if (ctl->done) return;
+    constexpr int W = Pack<T>::n;
     const T a = (T)ctl->alpha;
-    double drz = 0.0, drr = 0.0;
-    for (uint64_t i = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kVecThreads) {
-        const T ri = v.r[i] - a * v.q[i];
-        v.x[i] += a * v.p[i];
-        v.r[i] = ri;
-        const T zi = ri * v.dinv[i];
-        v.z[i] = zi;
-        drz += (double)ri * (double)zi;
-        drr += (double)ri * (double)ri;
-    }
-    drz = block_sum(drz, sh);
-    drr = block_sum(drr, sh);
+    T *__restrict__ x = v.x;
+    T *__restrict__ r = v.r;
+    T *__restrict__ z = v.z;
+    const T *__restrict__ p = v.p;
+    const T *__restrict__ q = v.q;
+    const T *__restrict__ d = v.dinv;
+    T drz = T(0), drr = T(0);   // per-thread partials in the vector precision, CTA sums in FP64
+    const bool al = aligned16(x) && aligned16(r) && aligned16(z) && aligned16(p) && aligned16(q) && aligned16(d);
+    for_entries<T>(
+        n, al,
+        [&](uint64_t k) {
+            T rv[W], qv[W], xv[W], pv[W], dv[W], zv[W];
+            ld_pack<T>(r, k, rv);
+            ldg_pack<T>(q, k, qv);
+            ld_pack<T>(x, k, xv);
+            ldg_pack<T>(p, k, pv);
+            ldg_pack<T>(d, k, dv);
+#pragma unroll
+            for (int c = 0; c < W; c++) {
+                rv[c] = rv[c] - a * qv[c];
+                xv[c] += a * pv[c];
+                zv[c] = rv[c] * dv[c];
+                drz = fma(rv[c], zv[c], drz);
+                drr = fma(rv[c], rv[c], drr);
+            }
+            st_pack<T>(r, k, rv);
+            st_pack<T>(x, k, xv);
+            st_pack<T>(z, k, zv);
+        },
+        [&](uint64_t i) {
+            const T ri = r[i] - a * q[i];
+            x[i] += a * p[i];
+            r[i] = ri;
+            const T zi = ri * d[i];
+            z[i] = zi;
+            drz = fma(ri, zi, drz);
+            drr = fma(ri, ri, drr);
+        });
+    const double brz = block_sum_v<T>(drz, sh);
+    const double brr = block_sum_v<T>(drr, sh);
     if (threadIdx.x == 0) {
-        parts.rz[blockIdx.x] = drz;
-        parts.rr[blockIdx.x] = drr;
+        parts.rz[blockIdx.x] = brz;
+        parts.rr[blockIdx.x] = brr;
     }
     if (!last_cta(&ctl->ticket, &flag)) return;
     const double rz_new = ordered_sum(parts.rz, gridDim.x, sh);
@@ -298,6 +511,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
         const int64_t it = ctl->iterations + 1;
         ctl->iterations = it;
         ctl->rr = rr;
+        ctl->rz_prev = ctl->rz;
         const bool stop = rr <= ctl->tol2 || it >= ctl->maxit || !(rr == rr);
         if (stop) {
             ctl->done = 1;
@@ -314,9 +528,56 @@ template <typename T>
 __global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_t n, const PcgCtl *ctl)
 {
     if (ctl->done) return;
+    constexpr int W = Pack<T>::n;
     const T bt = (T)ctl->beta;
-    for (uint64_t i = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kVecThreads)
-        v.p[i] = v.z[i] + bt * v.p[i];
+    T *__restrict__ p = v.p;
+    const T *__restrict__ z = v.z;
+    for_entries<T>(
+        n, aligned16(p) && aligned16(z),
+        [&](uint64_t k) {
+            T pv[W], zv[W];
+            ld_pack<T>(p, k, pv);
+            ldg_pack<T>(z, k, zv);
+#pragma unroll
+            for (int c = 0; c < W; c++) pv[c] = zv[c] + bt * pv[c];
+            st_pack<T>(p, k, pv);
+        },
+        [&](uint64_t i) { p[i] = z[i] + bt * p[i]; });
+}
+
+// z = D^-1 r (and p = z when `set_p`); partials r.z, r.r.  Shared by the start
+// and the resume of a run.
+template <typename T, bool SET_P>
+__device__ __forceinline__ void precond_parts(const PcgVecs<T> &v, uint64_t n, T &drz, T &drr)
+{
+    constexpr int W = Pack<T>::n;
+    const T *__restrict__ r = v.r;
+    const T *__restrict__ d = v.dinv;
+    T *__restrict__ z = v.z;
+    T *__restrict__ p = v.p;
+    for_entries<T>(
+        n, aligned16(r) && aligned16(d) && aligned16(z) && aligned16(p),
+        [&](uint64_t k) {
+            T rv[W], dv[W], zv[W];
+            ldg_pack<T>(r, k, rv);
+            ldg_pack<T>(d, k, dv);
+#pragma unroll
+            for (int c = 0; c < W; c++) {
+                zv[c] = rv[c] * dv[c];
+                drz = fma(rv[c], zv[c], drz);
+                drr = fma(rv[c], rv[c], drr);
+            }
+            st_pack<T>(z, k, zv);
+            if (SET_P) st_pack<T>(p, k, zv);
+        },
+        [&](uint64_t i) {
+            const T ri = r[i];
+            const T zi = ri * d[i];
+            z[i] = zi;
+            if (SET_P) p[i] = zi;
+            drz = fma(ri, zi, drz);
+            drr = fma(ri, ri, drr);
+        });
 }
 
 // Start of a PCG run from the residual r (already holding b - A x):
@@ -326,20 +587,13 @@ __global__ void __launch_bounds__(kVecThreads) k_pcg_start(PcgVecs<T> v, uint64_
 {
     __shared__ double sh[33];
     __shared__ int flag;
-    double drz = 0.0, drr = 0.0;
-    for (uint64_t i = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kVecThreads) {
-        const T ri = v.r[i];
-        const T zi = ri * v.dinv[i];
-        v.z[i] = zi;
-        v.p[i] = zi;
-        drz += (double)ri * (double)zi;
-        drr += (double)ri * (double)ri;
-    }
-    drz = block_sum(drz, sh);
-    drr = block_sum(drr, sh);
+    T drz = T(0), drr = T(0);
+    precond_parts<T, true>(v, n, drz, drr);
+    const double brz = block_sum_v<T>(drz, sh);
+    const double brr = block_sum_v<T>(drr, sh);
     if (threadIdx.x == 0) {
-        parts.rz[blockIdx.x] = drz;
-        parts.rr[blockIdx.x] = drr;
+        parts.rz[blockIdx.x] = brz;
+        parts.rr[blockIdx.x] = brr;
     }
     if (!last_cta(&ctl->ticket, &flag)) return;
     const double rz = ordered_sum(parts.rz, gridDim.x, sh);
@@ -347,6 +601,40 @@ __global__ void __launch_bounds__(kVecThreads) k_pcg_start(PcgVecs<T> v, uint64_
     if (threadIdx.x == 0) {
         ctl->rz = rz;
         ctl->rr = rr;
+        ctl->ticket = 0;
+    }
+}
+
+// Resume of a stopped PCG run after its residual r was replaced by the true
+// residual, rescaled by `ratio` = old scale / new scale relative to the run's
+// vectors: z = D^-1 r, partials r.z, r.r; last CTA: beta = ratio * rz / rz_prev
+// so that the following k_direction keeps the previous search direction
+// (a reliable update), fresh tol2 / maxit, iterations and done cleared.
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_pcg_resume(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl,
+                                                            double ratio, double tol2, int64_t maxit)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    T drz = T(0), drr = T(0);
+    precond_parts<T, false>(v, n, drz, drr);
+    const double brz = block_sum_v<T>(drz, sh);
+    const double brr = block_sum_v<T>(drr, sh);
+    if (threadIdx.x == 0) {
+        parts.rz[blockIdx.x] = brz;
+        parts.rr[blockIdx.x] = brr;
+    }
+    if (!last_cta(&ctl->ticket, &flag)) return;
+    const double rz = ordered_sum(parts.rz, gridDim.x, sh);
+    const double rr = ordered_sum(parts.rr, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+        ctl->beta = ctl->rz_prev != 0.0 ? ratio * rz / ctl->rz_prev : 0.0;
+        ctl->rz = rz;
+        ctl->rr = rr;
+        ctl->tol2 = tol2;
+        ctl->maxit = maxit;
+        ctl->iterations = 0;
+        ctl->done = 0;
         ctl->ticket = 0;
     }
 }

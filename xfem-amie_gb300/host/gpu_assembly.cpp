@@ -190,7 +190,7 @@ bool Assembly::cgsolve(int maxit, bool verbose)
     o.eps = epsilon_;
     o.nssor = nssor_;
     o.maxit = maxit > 0 ? maxit : 0;
-    o.inner_rtol = 1e-5;
+    o.inner_rtol = 0.0;   // library default
     o.use_x0 = x.size() == n ? 1 : 0;
     x.resize(n, 0.0);
     amie_status s = amie_solve(topo_, &o, x.data(), &stats_);
