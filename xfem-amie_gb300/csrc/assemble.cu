@@ -685,14 +685,14 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
     const double avg = (double)t->nnzb / t->n_rows;
     t->spmv_group = avg <= 12 ? 1 : avg <= 24 ? 2 : 4;
     // tuning overrides for measurements: AMIE_SPMV_GROUP = 1, 2, 4, 8, 16 or 32 lanes per
-    // block row (block-CSR kernel); AMIE_SELL_VARIANT = 0..5 (SELL kernel loop, see amie_topo)
+    // block row (block-CSR kernel); AMIE_SELL_VARIANT = 0..7 (SELL kernel loop, see amie_topo)
     if (const char *g = std::getenv("AMIE_SPMV_GROUP")) {
         const int v = std::atoi(g);
         if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16 || v == 32) t->spmv_group = v;
     }
     if (const char *g = std::getenv("AMIE_SELL_VARIANT")) {
         const int v = std::atoi(g);
-        if (v >= 0 && v <= 5) t->sell_variant = v;
+        if (v >= 0 && v <= 7) t->sell_variant = v;
     }
 
     // SELL-32-sigma structure: rows sorted by length inside windows, slices of 32
@@ -703,8 +703,15 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
         t->n_slices = (t->n_rows + 31) / 32;
         std::vector<uint32_t> perm((size_t)t->n_slices * 32, t->n_rows);
         std::vector<uint64_t> sptr(t->n_slices + 1, 0);
-        for (uint32_t w0 = 0; w0 < t->n_rows; w0 += kSellSigma) {
-            const uint32_t w1 = std::min<uint32_t>(t->n_rows, w0 + kSellSigma);
+        // window of the length sort; tuning override for measurements: AMIE_SELL_SIGMA
+        // (a multiple of 32; 32 keeps every slice on 32 consecutive rows)
+        uint32_t sigma = kSellSigma;
+        if (const char *e = std::getenv("AMIE_SELL_SIGMA")) {
+            const long v = std::atol(e);
+            if (v >= 32 && v <= (1l << 24) && v % 32 == 0) sigma = (uint32_t)v;
+        }
+        for (uint32_t w0 = 0; w0 < t->n_rows; w0 += sigma) {
+            const uint32_t w1 = std::min<uint32_t>(t->n_rows, w0 + sigma);
             for (uint32_t r = w0; r < w1; r++) perm[r] = r;
             std::stable_sort(perm.begin() + w0, perm.begin() + w1, [&](uint32_t a, uint32_t b) {
                 return h_rp[a + 1] - h_rp[a] > h_rp[b + 1] - h_rp[b];
@@ -719,6 +726,7 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
             sptr[sl + 1] = sptr[sl] + 32ull * len;
         }
         t->n_slots = sptr[t->n_slices];
+        t->h_sell_ptr = sptr;
         if ((rc = upload(ctx, t->sell_perm, perm.data(), perm.size())) ||
             (rc = upload(ctx, t->sell_ptr, sptr.data(), sptr.size())) ||
             (rc = t->sell_blk.alloc(ctx, t->n_slots)) || (rc = t->sell_col.alloc(ctx, t->n_slots)))
@@ -875,6 +883,27 @@ amie_status ensure_sell(amie_topo *t, bool want64, bool want32)
         t->sell32_ok = true;
     }
     AMIE_CUDA(cudaGetLastError());
+    return AMIE_OK;
+}
+
+// Slice ranges of the CTAs of a SELL SpMV launch with `grid` CTAs: contiguous,
+// with about the same number of slots each (built once per grid, synchronously,
+// so before any graph capture that uses it).
+amie_status ensure_sell_partition(amie_topo *t, int grid)
+{
+    if (t->sell_cta_first.count(grid)) return AMIE_OK;
+    const std::vector<uint64_t> &sp = t->h_sell_ptr;
+    std::vector<uint32_t> first(grid + 1);
+    const uint64_t total = t->n_slots;
+    uint32_t sl = 0;
+    for (int b = 0; b <= grid; b++) {
+        const uint64_t target = total * (uint64_t)b / (uint64_t)grid;
+        while (sl < t->n_slices && sp[sl] < target) sl++;
+        first[b] = b == grid ? t->n_slices : sl;
+    }
+    DevArray<uint32_t> &d = t->sell_cta_first[grid];
+    AMIE_TRY(upload(t->ctx, d, first.data(), first.size()));
+    AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
     return AMIE_OK;
 }
 

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <map>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -121,7 +122,7 @@ struct BsrView {
 // of one j are stored in chunks of kSellVec<S,T> components: component c of
 // lane l at val[32*S*S*(group) + 32*V*(c / V) + V*l + c % V].  Padding slots
 // have zero values and the row's own column (no effect on the result).
-constexpr uint32_t kSellSigma = 1024;
+constexpr uint32_t kSellSigma = 128;
 constexpr uint32_t kSellNone = 0xffffffffu;
 template <int S, typename T>
 constexpr int kSellVec = S == 2 ? int(16 / sizeof(T)) : 1;
@@ -133,6 +134,7 @@ struct SellView {
     const uint64_t *slice_ptr;   // [n_slices + 1] first slot of each slice
     const uint32_t *col;         // [slots] block column
     const T *val;                // [slots * S * S] chunked as above
+    const uint32_t *cta_first;   // [grid + 1] first slice of each CTA of the launch (slot-balanced ranges)
 };
 
 }  // namespace amie
@@ -179,9 +181,12 @@ struct amie_topo {
     amie::DevArray<float> sell_val32;
     uint32_t n_slices = 0;
     uint64_t n_slots = 0;
+    std::vector<uint64_t> h_sell_ptr;                          // host copy of sell_ptr
+    std::map<int, amie::DevArray<uint32_t>> sell_cta_first;   // per launch grid: slice ranges of the CTAs
     bool sell64_ok = false, sell32_ok = false;
     // SELL SpMV loop: 0 = 4 slots per step, 1 = 8, 2 = 2 pipelined, 3 = 4 pipelined,
-    // 4 / 5 = 0 / 2 with registers capped for 5 CTAs per SM (2x2 FP32 blocks)
+    // 4 / 5 = 0 / 2 with registers capped for 5 CTAs per SM (2x2 FP32 blocks),
+    // 6 / 7 = matrix streamed through shared memory by cp.async (2 slots x 4 stages / 4 x 3)
     int sell_variant = 0;
 
     // right-hand side, solution and solver work vectors

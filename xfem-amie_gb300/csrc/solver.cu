@@ -13,6 +13,7 @@
 #include "solver.cuh"
 
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <mutex>
 #include <unordered_map>
@@ -28,6 +29,7 @@ struct SolverState {
     int grid_vec = 0;             // PCG vector kernels (full occupancy)
     int grid_sell[2] = {0, 0};    // SELL SpMV, FP32 / FP64 (resident CTAs of that kernel)
     int stride = 0;               // partials per kind in `parts` (the largest grid)
+    bool pdl = true;              // programmatic dependent launch inside the PCG graphs
     DevArray<double> parts;       // 4 * stride: pq, rz, rr, spare
     DevArray<PcgCtl> ctl;
     PcgCtl *h_ctl = nullptr;      // pinned
@@ -75,6 +77,7 @@ void dispatch_group(int group, F &&f)
 }
 
 amie_status ensure_sell(amie_topo *t, bool want64, bool want32);
+amie_status ensure_sell_partition(amie_topo *t, int grid);
 
 // SELL copy of the current matrix in precision T (val == nullptr if not converted).
 template <typename T>
@@ -83,22 +86,63 @@ template <>
 SellView<double> sell_of<double>(amie_topo *t)
 {
     return SellView<double>{t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p, t->sell_col.p,
-                            t->sell64_ok ? t->sell_val.p : nullptr};
+                            t->sell64_ok ? t->sell_val.p : nullptr, nullptr};
 }
 template <>
 SellView<float> sell_of<float>(amie_topo *t)
 {
     return SellView<float>{t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p, t->sell_col.p,
-                           t->sell32_ok ? t->sell_val32.p : nullptr};
+                           t->sell32_ok ? t->sell_val32.p : nullptr, nullptr};
+}
+
+// Launch with programmatic stream serialization (the kernel calls pdl_wait
+// before it reads anything its predecessor wrote) when `pdl`, else plainly.
+template <typename... KArgs, typename... Args>
+void launch_k(bool pdl, void (*kern)(KArgs...), int grid, size_t smem, cudaStream_t st, Args... args)
+{
+    if (!pdl) {
+        kern<<<grid, kVecThreads, smem, st>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kVecThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
 template <typename T>
 using SellKernel = void (*)(SellView<T>, const T *, T *, double *, const int32_t *, PcgCtl *);
 
-// SELL SpMV kernel for block size s and loop variant (see amie_topo::sell_variant).
+// SELL SpMV kernel for block size s and loop variant (see amie_topo::sell_variant)
+// and its dynamic shared memory.
 template <typename T>
-SellKernel<T> sell_kernel(int s, int variant)
+SellKernel<T> sell_kernel(int s, int variant, size_t *smem)
 {
+    *smem = 0;
+    constexpr size_t W = kVecThreads / 32;
+    if (variant == 6) {
+        if (s == 2) {
+            *smem = W * 4 * sell_stage_bytes<2, 2, T>();
+            return k_sell_pq_cp<2, 2, 4, T>;
+        }
+        *smem = W * 4 * sell_stage_bytes<3, 2, T>();
+        return k_sell_pq_cp<3, 2, 4, T>;
+    }
+    if (variant == 7) {
+        if (s == 2) {
+            *smem = W * 3 * sell_stage_bytes<2, 4, T>();
+            return k_sell_pq_cp<2, 4, 3, T>;
+        }
+        *smem = W * 3 * sell_stage_bytes<3, 2, T>();
+        return k_sell_pq_cp<3, 2, 3, T>;
+    }
     if (s == 2) {
         switch (variant) {
         case 1: return k_sell_pq<2, 8, false, 1, T>;
@@ -123,18 +167,22 @@ SellKernel<T> sell_kernel(int s, int variant)
 // kernel writes `grid` partials.
 template <typename T>
 void launch_spmv_pq(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, const int32_t *done, PcgCtl *fin,
-                    cudaStream_t st)
+                    cudaStream_t st, bool pdl = false)
 {
-    const SellView<T> sv = sell_of<T>(t);
-    if (sv.val) {
-        sell_kernel<T>(t->s, t->sell_variant)<<<grid, kVecThreads, 0, st>>>(sv, v.p, v.q, part, done, fin);
+    SellView<T> sv = sell_of<T>(t);
+    auto part_it = t->sell_cta_first.find(grid);   // made by ensure_state for every grid it hands out
+    if (sv.val && part_it != t->sell_cta_first.end()) {
+        sv.cta_first = part_it->second.p;
+        size_t smem = 0;
+        const SellKernel<T> k = sell_kernel<T>(t->s, t->sell_variant, &smem);
+        launch_k(pdl, k, grid, smem, st, sv, (const T *)v.p, v.q, part, done, fin);
         AMIE_LAUNCHED();
         return;
     }
     auto go = [&](auto g) {
         constexpr int G = decltype(g)::value;
-        if (t->s == 2) k_spmv_pq<2, G, T><<<grid, kVecThreads, 0, st>>>(v, part, done, fin);
-        else k_spmv_pq<3, G, T><<<grid, kVecThreads, 0, st>>>(v, part, done, fin);
+        if (t->s == 2) launch_k(pdl, k_spmv_pq<2, G, T>, grid, 0, st, v, part, done, fin);
+        else launch_k(pdl, k_spmv_pq<3, G, T>, grid, 0, st, v, part, done, fin);
     };
     dispatch_group<2, T>(t->spmv_group, go);
     AMIE_LAUNCHED();
@@ -176,15 +224,25 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         dispatch_group<2, double>(t->spmv_group, occ);
         per_sm = std::max(1, std::min(per_sm, 8));
         s->grid = t->ctx->num_sms * per_sm;
-        auto resident = [&](const void *f) {
+        auto resident = [&](const void *f, size_t smem) {
             int k = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kVecThreads, 0);
+            if (smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kVecThreads, smem);
             return t->ctx->num_sms * std::max(1, std::min(k, 8));
         };
-        s->grid_sell[0] = resident((const void *)sell_kernel<float>(t->s, t->sell_variant));
-        s->grid_sell[1] = resident((const void *)sell_kernel<double>(t->s, t->sell_variant));
-        s->grid_vec = resident((const void *)k_update<double>);
+        size_t sm32 = 0, sm64 = 0;
+        const void *k32 = (const void *)sell_kernel<float>(t->s, t->sell_variant, &sm32);
+        const void *k64 = (const void *)sell_kernel<double>(t->s, t->sell_variant, &sm64);
+        s->grid_sell[0] = resident(k32, sm32);
+        s->grid_sell[1] = resident(k64, sm64);
+        s->grid_vec = resident((const void *)k_update<double>, 0);
+        AMIE_CUDA(cudaGetLastError());
+        AMIE_TRY(ensure_sell_partition(t, s->grid));
+        AMIE_TRY(ensure_sell_partition(t, s->grid_sell[0]));
+        AMIE_TRY(ensure_sell_partition(t, s->grid_sell[1]));
         s->stride = std::max(std::max(s->grid, s->grid_vec), std::max(s->grid_sell[0], s->grid_sell[1]));
+        // tuning override for measurements: AMIE_PDL=0 launches the PCG graph kernels plainly
+        if (const char *e = std::getenv("AMIE_PDL")) s->pdl = std::atoi(e) != 0;
         AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->stride));
         AMIE_TRY(s->ctl.alloc(t->ctx, 1));
         AMIE_CUDA(cudaMallocHost((void **)&s->h_ctl, sizeof(PcgCtl)));
@@ -241,10 +299,13 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     cudaGraph_t graph;
     AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     const int gs = s->grid_sell[sizeof(T) == 8 ? 1 : 0];
+    const uint64_t n = t->n;
+    PcgCtl *ctl = s->ctl.p;
     for (int it = 0; it < kGraphIters; it++) {
-        launch_spmv_pq<T>(t, gs, v, parts.pq, &s->ctl.p->done, s->ctl.p, st);
-        k_update<T><<<s->grid_vec, kVecThreads, 0, st>>>(v, t->n, parts, s->ctl.p);
-        k_direction<T><<<s->grid_vec, kVecThreads, 0, st>>>(v, t->n, s->ctl.p);
+        // the first kernel follows the previous graph launch in plain stream order
+        launch_spmv_pq<T>(t, gs, v, parts.pq, &ctl->done, ctl, st, s->pdl && it > 0);
+        launch_k(s->pdl, k_update<T>, s->grid_vec, 0, st, v, n, parts, ctl);
+        launch_k(s->pdl, k_direction<T>, s->grid_vec, 0, st, v, n, (const PcgCtl *)ctl);
     }
     g_launches -= kGraphIters;   // captured, not launched: counted per graph launch
     AMIE_CUDA(cudaStreamEndCapture(st, &graph));

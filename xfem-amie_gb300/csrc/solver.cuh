@@ -26,6 +26,14 @@ namespace amie {
 
 constexpr int kVecThreads = 256;
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while its predecessor finishes; pdl_wait() blocks
+// (in hardware) until the predecessor grid has completed and its writes are
+// visible, pdl_release() lets the successor grid be scheduled.  Both are
+// no-ops for a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // Solver control block in device memory.  `done` is the first member: the
 // SpMV kernel's early exit also reads it from the AMIE_CG control block.
 struct PcgCtl {
@@ -236,6 +244,8 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv_pq(PcgVecs<T> v, double *p
 {
     __shared__ double sh[33];
     __shared__ int flag;
+    pdl_wait();
+    pdl_release();
     if (done && *done) return;
     constexpr int RPB = kVecThreads / G;
     const int lane = threadIdx.x % G;
@@ -299,7 +309,11 @@ __device__ __forceinline__ void load_sell_group(const SellView<T> &A, uint64_t g
 }
 
 // Kernel A on the SELL copy: one warp per slice, one lane per block row; every
-// load of blocks and columns is one contiguous run per warp.  U slots are
+// load of blocks and columns is one contiguous run per warp.  Each CTA works on
+// its own contiguous range of slices (A.cta_first, balanced by slots, so the x
+// entries its warps gather are close together) and its warps take the range's
+// slices one at a time from a shared counter (no warp idles while another still
+// has several slices to go).  U slots are
 // fetched per step; with PIPE the next step's columns and blocks are fetched
 // before the current step's x entries are gathered, so the matrix stream is
 // never idle while x is read.  Blocks of a row are visited in the order of the
@@ -313,11 +327,18 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
 {
     __shared__ double sh[33];
     __shared__ int flag;
+    __shared__ uint32_t next_sl;
+    pdl_wait();
+    pdl_release();
     if (done && *done) return;
     constexpr uint32_t WPB = kVecThreads / 32;
     const uint32_t lane = threadIdx.x & 31;
+    // the CTA's contiguous, slot-balanced range of slices; its warps take slices in turn
+    const uint32_t s_beg = __ldg(A.cta_first + blockIdx.x), s_end = __ldg(A.cta_first + blockIdx.x + 1);
+    if (threadIdx.x == 0) next_sl = s_beg + WPB;
+    __syncthreads();
     T dot = T(0);   // the thread's few rows in the vector precision (FP64 issue slots are scarce on this part)
-    for (uint32_t sl = blockIdx.x * WPB + (threadIdx.x >> 5); sl < A.n_slices; sl += gridDim.x * WPB) {
+    for (uint32_t sl = s_beg + (threadIdx.x >> 5); sl < s_end;) {
         const uint32_t row = __ldg(A.perm + (uint64_t)sl * 32 + lane);
         const uint64_t g0 = __ldg(A.slice_ptr + sl);
         const uint32_t len = (uint32_t)((__ldg(A.slice_ptr + sl + 1) - g0) >> 5);
@@ -361,7 +382,168 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
                 dot = fma(acc[r], x[(uint64_t)row * S + r], dot);
             }
         }
+        uint32_t nx = 0;
+        if (lane == 0) nx = atomicAdd(&next_sl, 1u);
+        sl = __shfl_sync(0xffffffffu, nx, 0);
     }
+    finish_pq<T>(dot, part_pq, fin, sh, &flag);
+}
+
+// Asynchronous 16-byte global -> shared copies (completion tracked per thread
+// in commit groups; cp.async.wait_group is a hardware wait on those copies).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// One s x s block of the lane's row from a 32-slot SELL group held in shared memory.
+template <int S, typename T>
+__device__ __forceinline__ void load_sell_block_sm(const T *group, uint32_t lane, T blk[S * S])
+{
+    constexpr int V = kSellVec<S, T>;
+    if constexpr (S == 2 && V == 4) {
+        const float4 a = reinterpret_cast<const float4 *>(group)[lane];
+        blk[0] = a.x; blk[1] = a.y; blk[2] = a.z; blk[3] = a.w;
+    } else if constexpr (S == 2 && V == 2) {
+        const double2 a = reinterpret_cast<const double2 *>(group)[lane];
+        const double2 b = reinterpret_cast<const double2 *>(group + 64)[lane];
+        blk[0] = a.x; blk[1] = a.y; blk[2] = b.x; blk[3] = b.y;
+    } else {
+#pragma unroll
+        for (int c = 0; c < S * S; c++) blk[c] = group[32 * c + lane];
+    }
+}
+
+// Bytes of one pipeline stage of k_sell_pq_cp: values and columns of U slot groups.
+template <int S, int U, typename T>
+__host__ __device__ constexpr uint32_t sell_stage_bytes()
+{
+    return (uint32_t)(U * 32 * S * S * sizeof(T) + U * 32 * 4);
+}
+
+// Kernel A on the SELL copy with the matrix streamed through shared memory:
+// each warp walks its slices in steps of U slot groups and keeps NST - 1 steps
+// of values and columns in flight as cp.async copies (no registers held), so
+// the matrix stream continues while the current step's x entries are gathered.
+// Same per-row FMA order as k_sell_pq, so q is bitwise the same.  Dynamic
+// shared memory: kVecThreads / 32 * NST * sell_stage_bytes<S, U, T>() bytes.
+template <int S, int U, int NST, typename T>
+__global__ void __launch_bounds__(kVecThreads) k_sell_pq_cp(SellView<T> A, const T *__restrict__ x,
+                                                            T *__restrict__ y, double *part_pq, const int32_t *done,
+                                                            PcgCtl *fin)
+{
+    extern __shared__ __align__(16) unsigned char sm_stage[];
+    __shared__ double sh[33];
+    __shared__ int flag;
+    pdl_wait();
+    pdl_release();
+    if (done && *done) return;
+    constexpr uint32_t WPB = kVecThreads / 32;
+    constexpr uint32_t VB = (uint32_t)(U * 32 * S * S * sizeof(T));
+    constexpr uint32_t SB = sell_stage_bytes<S, U, T>();
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char *wbase = sm_stage + (size_t)warp * NST * SB;
+    const uint32_t sl_step = gridDim.x * WPB;
+    const uint32_t n_slices = A.n_slices;
+
+    // issue side: next step whose copies have not been started
+    uint32_t i_sl = blockIdx.x * WPB + warp, i_j = 0, i_len = 0;
+    uint64_t i_g0 = 0;
+    auto i_enter = [&]() {
+        for (; i_sl < n_slices; i_sl += sl_step) {
+            i_g0 = __ldg(A.slice_ptr + i_sl);
+            i_len = (uint32_t)((__ldg(A.slice_ptr + i_sl + 1) - i_g0) >> 5);
+            if (i_len) break;
+        }
+    };
+    auto issue = [&](uint32_t stage) {
+        if (i_sl < n_slices) {
+            const uint32_t cnt = min((uint32_t)U, i_len - i_j);
+            const uint64_t gs = i_g0 + (uint64_t)i_j * 32;
+            unsigned char *dst = wbase + stage * SB;
+            const unsigned char *gv = reinterpret_cast<const unsigned char *>(A.val + gs * (S * S));
+            const uint32_t nv = cnt * (uint32_t)(32 * S * S * sizeof(T) / 16);
+            for (uint32_t k = lane; k < nv; k += 32) cp_async16(dst + 16 * k, gv + 16 * k);
+            const unsigned char *gc = reinterpret_cast<const unsigned char *>(A.col + gs);
+            for (uint32_t k = lane; k < cnt * 8; k += 32) cp_async16(dst + VB + 16 * k, gc + 16 * k);
+            i_j += U;
+            if (i_j >= i_len) {
+                i_j = 0;
+                i_sl += sl_step;
+                i_enter();
+            }
+        }
+        cp_async_commit();   // one group per step, empty past the end, so the counts line up
+    };
+    i_enter();
+#pragma unroll
+    for (int k = 0; k < NST - 1; k++) issue(k);
+
+    // consume side
+    uint32_t c_sl = blockIdx.x * WPB + warp, c_j = 0, c_len = 0, row = 0;
+    auto c_enter = [&]() {
+        for (; c_sl < n_slices; c_sl += sl_step) {
+            const uint64_t g0 = __ldg(A.slice_ptr + c_sl);
+            c_len = (uint32_t)((__ldg(A.slice_ptr + c_sl + 1) - g0) >> 5);
+            if (c_len) break;
+        }
+        if (c_sl < n_slices) row = __ldg(A.perm + (uint64_t)c_sl * 32 + lane);
+    };
+    c_enter();
+    T dot = T(0);
+    T acc[S];
+#pragma unroll
+    for (int r = 0; r < S; r++) acc[r] = T(0);
+    uint32_t stage = 0;
+    while (c_sl < n_slices) {   // uniform over the warp
+        issue(stage == 0 ? NST - 1 : stage - 1);
+        cp_async_wait<NST - 1>();
+        __syncwarp();
+        const unsigned char *src = wbase + stage * SB;
+        const T *vals = reinterpret_cast<const T *>(src);
+        const uint32_t *cols = reinterpret_cast<const uint32_t *>(src + VB);
+        const uint32_t cnt = min((uint32_t)U, c_len - c_j);
+        T xv[U][S];
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (u < cnt) load_x<S, T>(x, cols[u * 32 + lane], xv[u]);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (u < cnt) {
+                T blk[S * S];
+                load_sell_block_sm<S, T>(vals + u * 32 * S * S, lane, blk);
+#pragma unroll
+                for (int r = 0; r < S; r++)
+#pragma unroll
+                    for (int cc = 0; cc < S; cc++) acc[r] = fma(blk[r * S + cc], xv[u][cc], acc[r]);
+            }
+        }
+        __syncwarp();   // the stage may be refilled from here on
+        stage = stage + 1 == NST ? 0 : stage + 1;
+        c_j += U;
+        if (c_j >= c_len) {
+            if (row < A.n_rows) {
+#pragma unroll
+                for (int r = 0; r < S; r++) {
+                    y[(uint64_t)row * S + r] = acc[r];
+                    dot = fma(acc[r], x[(uint64_t)row * S + r], dot);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < S; r++) acc[r] = T(0);
+            c_j = 0;
+            c_sl += sl_step;
+            c_enter();
+        }
+    }
+    cp_async_wait<0>();
     finish_pq<T>(dot, part_pq, fin, sh, &flag);
 }
 
@@ -457,6 +639,8 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
 {
     __shared__ double sh[33];
     __shared__ int flag;
+    pdl_wait();
+    pdl_release();
     if (ctl->done) return;
     constexpr int W = Pack<T>::n;
     const T a = (T)ctl->alpha;
@@ -527,6 +711,8 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_t n, const PcgCtl *ctl)
 {
+    pdl_wait();
+    pdl_release();
     if (ctl->done) return;
     constexpr int W = Pack<T>::n;
     const T bt = (T)ctl->beta;
