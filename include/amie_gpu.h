@@ -289,6 +289,12 @@ AMIE_API amie_status amie_timer_stop(amie_ctx *ctx, double *ms);
  * kernel's achieved bandwidth against the HBM roofline. */
 AMIE_API amie_status amie_profile_spmv(amie_topo *topo, int32_t precision, int32_t reps, double *ms_per_launch);
 
+/* Average device duration of one plain streaming read of `bytes` bytes (16-byte
+ * loads, one launch, L2 evicted by reading a 512 MB buffer before each launch)
+ * over `reps` launches: the bandwidth a single launch of that size can reach,
+ * reported beside the SpMV's.  No reference counterpart. */
+AMIE_API amie_status amie_profile_stream(amie_ctx *ctx, uint64_t bytes, int32_t reps, double *ms_per_launch);
+
 /* Number of kernels this library has launched (process-wide counter). */
 AMIE_API uint64_t amie_kernel_launches(void);
 

@@ -231,6 +231,26 @@ def test_solve_is_deterministic(golden_topos):
     assert np.array_equal(x1, x2)
 
 
+@pytest.mark.parametrize("solver", ["fp64", "mixed"])
+def test_large_solve_is_deterministic(gpu_ctx, solver):
+    """Bitwise repeatable on a mesh with many more SELL slices than warps (dynamic slice scheduling)."""
+    import amie_gpu
+    import workloads as W
+    m, bcs, meta = W.cracked_square(300, L=0.1, order=2, n_inclusions=400, seed=3)
+    t = amie_gpu.Topology(gpu_ctx, m)
+    try:
+        assert t.n_rows // 32 > 152 * 8 * 8   # more slices than warps in any SpMV grid (8 CTAs/SM at most)
+        t.assemble()
+        t.apply_dirichlet(*bcs)
+        sv = amie_gpu.SOLVER_PCG_FP64 if solver == "fp64" else amie_gpu.SOLVER_PCG_MIXED
+        x1, s1 = t.solve(sv, rtol=1e-10)
+        x2, s2 = t.solve(sv, rtol=1e-10)
+        assert s1["iterations"] == s2["iterations"]
+        assert np.array_equal(x1, x2)
+    finally:
+        t.close()
+
+
 def test_warm_start_reduces_iterations(golden_topos):
     import amie_gpu
     d, m, t = golden_topos["incl_p1"]

@@ -34,7 +34,7 @@ EXPORTED = [
     "amie_solve_resident", "amie_solution_download", "amie_server_start", "amie_submit", "amie_poll",
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
     "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step", "amie_pcg_solve_noalloc",
-    "amie_topology_spmv_lanes",
+    "amie_topology_spmv_lanes", "amie_profile_stream",
 ]
 
 
@@ -149,6 +149,13 @@ class Context:
 
     def timer_start(self):
         check(lib().amie_timer_start(self.ptr), "amie_timer_start")
+
+    def profile_stream(self, nbytes: int, reps: int = 10) -> float:
+        """Milliseconds of one plain streaming read of `nbytes` (L2 evicted before each launch)."""
+        ms = C.c_double()
+        check(lib().amie_profile_stream(self.ptr, C.c_uint64(nbytes), C.c_int32(reps), C.byref(ms)),
+              "amie_profile_stream")
+        return ms.value
 
     def timer_stop(self) -> float:
         """Milliseconds of device time on the context's stream since timer_start."""

@@ -729,7 +729,8 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
         t->h_sell_ptr = sptr;
         if ((rc = upload(ctx, t->sell_perm, perm.data(), perm.size())) ||
             (rc = upload(ctx, t->sell_ptr, sptr.data(), sptr.size())) ||
-            (rc = t->sell_blk.alloc(ctx, t->n_slots)) || (rc = t->sell_col.alloc(ctx, t->n_slots)))
+            (rc = t->sell_blk.alloc(ctx, t->n_slots)) || (rc = t->sell_col.alloc(ctx, t->n_slots)) ||
+            (rc = t->sell_dot.alloc(ctx, t->n_slices)))
             return fail(rc);
         k_sell_fill<<<t->ctx->num_sms * 8, 256, 0, st>>>(t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p,
                                                          t->row_ptr.p, t->col.p, t->sell_blk.p, t->sell_col.p);

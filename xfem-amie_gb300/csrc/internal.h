@@ -135,6 +135,7 @@ struct SellView {
     const uint32_t *col;         // [slots] block column
     const T *val;                // [slots * S * S] chunked as above
     const uint32_t *cta_first;   // [grid + 1] first slice of each CTA of the launch (slot-balanced ranges)
+    T *slice_dot;                // [n_slices] per-slice partial of the fused dot product (scratch)
 };
 
 }  // namespace amie
@@ -182,6 +183,7 @@ struct amie_topo {
     uint32_t n_slices = 0;
     uint64_t n_slots = 0;
     std::vector<uint64_t> h_sell_ptr;                          // host copy of sell_ptr
+    amie::DevArray<double> sell_dot;                           // [n_slices] SpMV dot partials (FP32 or FP64)
     std::map<int, amie::DevArray<uint32_t>> sell_cta_first;   // per launch grid: slice ranges of the CTAs
     bool sell64_ok = false, sell32_ok = false;
     // SELL SpMV loop: 0 = 4 slots per step, 1 = 8, 2 = 2 pipelined, 3 = 4 pipelined,

@@ -26,7 +26,7 @@ amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_sta
 
 struct SolverState {
     int grid = 0;                 // block-CSR SpMV, AMIE_CG and server kernels
-    int grid_vec = 0;             // PCG vector kernels (full occupancy)
+    int grid_vec[2] = {0, 0};     // PCG vector kernels, FP32 / FP64 (resident CTAs of k_update)
     int grid_sell[2] = {0, 0};    // SELL SpMV, FP32 / FP64 (resident CTAs of that kernel)
     int stride = 0;               // partials per kind in `parts` (the largest grid)
     bool pdl = true;              // programmatic dependent launch inside the PCG graphs
@@ -86,13 +86,14 @@ template <>
 SellView<double> sell_of<double>(amie_topo *t)
 {
     return SellView<double>{t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p, t->sell_col.p,
-                            t->sell64_ok ? t->sell_val.p : nullptr, nullptr};
+                            t->sell64_ok ? t->sell_val.p : nullptr, nullptr, t->sell_dot.p};
 }
 template <>
 SellView<float> sell_of<float>(amie_topo *t)
 {
     return SellView<float>{t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p, t->sell_col.p,
-                           t->sell32_ok ? t->sell_val32.p : nullptr, nullptr};
+                           t->sell32_ok ? t->sell_val32.p : nullptr, nullptr,
+                           reinterpret_cast<float *>(t->sell_dot.p)};
 }
 
 // Launch with programmatic stream serialization (the kernel calls pdl_wait
@@ -235,12 +236,14 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         const void *k64 = (const void *)sell_kernel<double>(t->s, t->sell_variant, &sm64);
         s->grid_sell[0] = resident(k32, sm32);
         s->grid_sell[1] = resident(k64, sm64);
-        s->grid_vec = resident((const void *)k_update<double>, 0);
+        s->grid_vec[0] = resident((const void *)k_update<float>, 0);
+        s->grid_vec[1] = resident((const void *)k_update<double>, 0);
         AMIE_CUDA(cudaGetLastError());
         AMIE_TRY(ensure_sell_partition(t, s->grid));
         AMIE_TRY(ensure_sell_partition(t, s->grid_sell[0]));
         AMIE_TRY(ensure_sell_partition(t, s->grid_sell[1]));
-        s->stride = std::max(std::max(s->grid, s->grid_vec), std::max(s->grid_sell[0], s->grid_sell[1]));
+        s->stride = std::max(std::max(s->grid, std::max(s->grid_vec[0], s->grid_vec[1])),
+                             std::max(s->grid_sell[0], s->grid_sell[1]));
         // tuning override for measurements: AMIE_PDL=0 launches the PCG graph kernels plainly
         if (const char *e = std::getenv("AMIE_PDL")) s->pdl = std::atoi(e) != 0;
         AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->stride));
@@ -299,13 +302,14 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     cudaGraph_t graph;
     AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     const int gs = s->grid_sell[sizeof(T) == 8 ? 1 : 0];
+    const int gv = s->grid_vec[sizeof(T) == 8 ? 1 : 0];
     const uint64_t n = t->n;
     PcgCtl *ctl = s->ctl.p;
     for (int it = 0; it < kGraphIters; it++) {
         // the first kernel follows the previous graph launch in plain stream order
         launch_spmv_pq<T>(t, gs, v, parts.pq, &ctl->done, ctl, st, s->pdl && it > 0);
-        launch_k(s->pdl, k_update<T>, s->grid_vec, 0, st, v, n, parts, ctl);
-        launch_k(s->pdl, k_direction<T>, s->grid_vec, 0, st, v, n, (const PcgCtl *)ctl);
+        launch_k(s->pdl, k_update<T>, gv, 0, st, v, n, parts, ctl);
+        launch_k(s->pdl, k_direction<T>, gv, 0, st, v, n, (const PcgCtl *)ctl);
     }
     g_launches -= kGraphIters;   // captured, not launched: counted per graph launch
     AMIE_CUDA(cudaStreamEndCapture(st, &graph));
@@ -376,7 +380,8 @@ amie_status run_pcg(amie_topo *t, SolverState *s, double tol2, int64_t maxit, in
     init.tol2 = tol2;
     *s->h_ctl = init;
     AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
-    k_pcg_start<T><<<s->grid_vec, kVecThreads, 0, st>>>(vecs_of<T>(t), t->n, parts_of(s), s->ctl.p);   // rz, rr
+    k_pcg_start<T><<<s->grid_vec[sizeof(T) == 8 ? 1 : 0], kVecThreads, 0, st>>>(vecs_of<T>(t), t->n, parts_of(s),
+                                                                              s->ctl.p);   // rz, rr
     AMIE_LAUNCHED();
     // The pinned copy is rewritten by drive_pcg only after this copy has completed.
     AMIE_CUDA(cudaStreamSynchronize(st));
@@ -391,8 +396,9 @@ amie_status resume_pcg(amie_topo *t, SolverState *s, double ratio, double tol2, 
 {
     cudaStream_t st = t->ctx->stream;
     const PcgVecs<T> v = vecs_of<T>(t);
-    k_pcg_resume<T><<<s->grid_vec, kVecThreads, 0, st>>>(v, t->n, parts_of(s), s->ctl.p, ratio, tol2, maxit);
-    k_direction<T><<<s->grid_vec, kVecThreads, 0, st>>>(v, t->n, s->ctl.p);
+    const int gv = s->grid_vec[sizeof(T) == 8 ? 1 : 0];
+    k_pcg_resume<T><<<gv, kVecThreads, 0, st>>>(v, t->n, parts_of(s), s->ctl.p, ratio, tol2, maxit);
+    k_direction<T><<<gv, kVecThreads, 0, st>>>(v, t->n, s->ctl.p);
     g_launches += 2;
     AMIE_CUDA(cudaGetLastError());
     return drive_pcg<T>(t, s, maxit, iters, rr_out);
@@ -615,6 +621,60 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     float f = 0.0f;
     AMIE_CUDA(cudaEventElapsedTime(&f, t->ctx->ev0, t->ctx->ev1));
     *ms_per_launch = (double)f / reps;
+    return AMIE_OK;
+}
+
+namespace amie {
+
+// Streaming read of n4 16-byte words, four independent loads per thread in flight.
+__global__ void __launch_bounds__(kVecThreads) k_stream_read(const float4 *__restrict__ a, uint64_t n4, float *sink)
+{
+    float acc = 0.0f;
+    const uint64_t stride = (uint64_t)gridDim.x * kVecThreads;
+    uint64_t i = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = __ldg(a + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < 4; u++) acc += v[u].x + v[u].y + v[u].z + v[u].w;
+    }
+    for (; i < n4; i += stride) {
+        const float4 v = __ldg(a + i);
+        acc += v.x + v.y + v.z + v.w;
+    }
+    if (acc == 1234.5f) sink[blockIdx.x] = acc;   // keeps the loads; the buffers hold zeros
+}
+
+}  // namespace amie
+
+extern "C" amie_status amie_profile_stream(amie_ctx *ctx, uint64_t bytes, int32_t reps, double *ms_per_launch)
+{
+    if (!ctx || !ms_per_launch || reps <= 0 || bytes < 16) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const uint64_t flush_bytes = 512ull << 20;
+    DevArray<float4> buf, flush;
+    DevArray<float> sink;
+    const int grid = ctx->num_sms * 8;
+    AMIE_TRY(buf.alloc(ctx, bytes / 16));
+    AMIE_TRY(flush.alloc(ctx, flush_bytes / 16));
+    AMIE_TRY(sink.alloc(ctx, grid));
+    AMIE_CUDA(cudaMemsetAsync(buf.p, 0, (bytes / 16) * 16, st));
+    AMIE_CUDA(cudaMemsetAsync(flush.p, 0, flush_bytes, st));
+    double total = 0.0;
+    for (int i = 0; i <= reps; i++) {   // launch 0 is a warm-up
+        k_stream_read<<<grid, kVecThreads, 0, st>>>(flush.p, flush_bytes / 16, sink.p);   // clean lines only
+        AMIE_CUDA(cudaEventRecord(ctx->ev0, st));
+        k_stream_read<<<grid, kVecThreads, 0, st>>>(buf.p, bytes / 16, sink.p);
+        AMIE_CUDA(cudaEventRecord(ctx->ev1, st));
+        AMIE_CUDA(cudaEventSynchronize(ctx->ev1));
+        float f = 0.0f;
+        AMIE_CUDA(cudaEventElapsedTime(&f, ctx->ev0, ctx->ev1));
+        if (i > 0) total += f;
+    }
+    AMIE_CUDA(cudaGetLastError());
+    *ms_per_launch = total / reps;
     return AMIE_OK;
 }
 

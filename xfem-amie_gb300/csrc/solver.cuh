@@ -113,6 +113,50 @@ __device__ __forceinline__ double ordered_sum(const double *parts, int n, double
     return block_sum(v, sh);
 }
 
+// CTA sums of two values per thread (vector precision T, per-warp sums in
+// FP64) with one pair of barriers.  Results valid in thread 0.
+template <typename T>
+__device__ __forceinline__ void block_sum2_v(T a, T b, double *sh, double &ra, double &rb)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    constexpr int NW = kVecThreads >> 5;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        sh[w] = (double)a;
+        sh[NW + w] = (double)b;
+    }
+    __syncthreads();
+    double x = 0.0, y = 0.0;
+    if (w == 0) {
+        x = l < NW ? sh[l] : 0.0;
+        y = l < NW ? sh[NW + l] : 0.0;
+#pragma unroll
+        for (int o = NW >> 1; o > 0; o >>= 1) {
+            x += __shfl_xor_sync(0xffffffffu, x, o);
+            y += __shfl_xor_sync(0xffffffffu, y, o);
+        }
+    }
+    __syncthreads();
+    ra = x;
+    rb = y;
+}
+
+// ordered_sum of two partial arrays in one pass.  Valid in thread 0.
+__device__ __forceinline__ void ordered_sum2(const double *pa, const double *pb, int n, double *sh, double &ra,
+                                             double &rb)
+{
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += kVecThreads) {
+        a += __ldcg(pa + i);
+        b += __ldcg(pb + i);
+    }
+    block_sum2_v<double>(a, b, sh, ra, rb);
+}
+
 // Deterministic sum of `n` partials computed identically by every CTA that
 // needs it; broadcast to all threads of the CTA.
 __device__ __forceinline__ double sum_parts(const double *parts, int n, double *sh)
@@ -313,7 +357,9 @@ __device__ __forceinline__ void load_sell_group(const SellView<T> &A, uint64_t g
 // its own contiguous range of slices (A.cta_first, balanced by slots, so the x
 // entries its warps gather are close together) and its warps take the range's
 // slices one at a time from a shared counter (no warp idles while another still
-// has several slices to go).  U slots are
+// has several slices to go); the dot partial of each slice goes to its own slot
+// and the CTA adds its slots in index order, so the result does not depend on
+// which warp took which slice.  U slots are
 // fetched per step; with PIPE the next step's columns and blocks are fetched
 // before the current step's x entries are gathered, so the matrix stream is
 // never idle while x is read.  Blocks of a row are visited in the order of the
@@ -337,7 +383,6 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
     const uint32_t s_beg = __ldg(A.cta_first + blockIdx.x), s_end = __ldg(A.cta_first + blockIdx.x + 1);
     if (threadIdx.x == 0) next_sl = s_beg + WPB;
     __syncthreads();
-    T dot = T(0);   // the thread's few rows in the vector precision (FP64 issue slots are scarce on this part)
     for (uint32_t sl = s_beg + (threadIdx.x >> 5); sl < s_end;) {
         const uint32_t row = __ldg(A.perm + (uint64_t)sl * 32 + lane);
         const uint64_t g0 = __ldg(A.slice_ptr + sl);
@@ -375,6 +420,9 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
                 }
             }
         }
+        // the slice's share of p.q, summed in a fixed order whichever warp took the
+        // slice (in the vector precision: FP64 issue slots are scarce on this part)
+        T dot = T(0);
         if (row < A.n_rows) {
 #pragma unroll
             for (int r = 0; r < S; r++) {
@@ -382,10 +430,16 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
                 dot = fma(acc[r], x[(uint64_t)row * S + r], dot);
             }
         }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        if (lane == 0) A.slice_dot[sl] = dot;
         uint32_t nx = 0;
         if (lane == 0) nx = atomicAdd(&next_sl, 1u);
         sl = __shfl_sync(0xffffffffu, nx, 0);
     }
+    __syncthreads();   // the CTA's slice partials are visible to all its threads
+    T dot = T(0);
+    for (uint32_t i = s_beg + threadIdx.x; i < s_end; i += kVecThreads) dot += A.slice_dot[i];
     finish_pq<T>(dot, part_pq, fin, sh, &flag);
 }
 
@@ -633,11 +687,13 @@ __device__ __forceinline__ void for_entries(uint64_t n, bool aligned, FP &&fpack
 }
 
 // Kernel B: x += alpha p; r -= alpha q; z = D^-1 r; partials r.z, r.r.
-// Last CTA: totals, iteration count, stop test, beta = rz_new / rz.
+// Last CTA: totals, iteration count, stop test, beta = rz_new / rz.  Each
+// thread handles two 16-byte packs per step with all ten loads issued before
+// any arithmetic (one memory round trip per step).
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl)
 {
-    __shared__ double sh[33];
+    __shared__ double sh[2 * (kVecThreads >> 5)];
     __shared__ int flag;
     pdl_wait();
     pdl_release();
@@ -652,45 +708,61 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     const T *__restrict__ d = v.dinv;
     T drz = T(0), drr = T(0);   // per-thread partials in the vector precision, CTA sums in FP64
     const bool al = aligned16(x) && aligned16(r) && aligned16(z) && aligned16(p) && aligned16(q) && aligned16(d);
-    for_entries<T>(
-        n, al,
-        [&](uint64_t k) {
-            T rv[W], qv[W], xv[W], pv[W], dv[W], zv[W];
-            ld_pack<T>(r, k, rv);
-            ldg_pack<T>(q, k, qv);
-            ld_pack<T>(x, k, xv);
-            ldg_pack<T>(p, k, pv);
-            ldg_pack<T>(d, k, dv);
+    const uint64_t tid = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * kVecThreads;
+    const uint64_t npk = al ? n / W : 0;
+    for (uint64_t k = tid; k < npk; k += 2 * stride) {
+        const uint64_t k2 = k + stride;
+        const bool two = k2 < npk;   // the second pack of the step exists
+        T rv[2][W], qv[2][W], xv[2][W], pv[2][W], dv[2][W];
+        ld_pack<T>(r, k, rv[0]);
+        ldg_pack<T>(q, k, qv[0]);
+        ld_pack<T>(x, k, xv[0]);
+        ldg_pack<T>(p, k, pv[0]);
+        ldg_pack<T>(d, k, dv[0]);
+        if (two) {
+            ld_pack<T>(r, k2, rv[1]);
+            ldg_pack<T>(q, k2, qv[1]);
+            ld_pack<T>(x, k2, xv[1]);
+            ldg_pack<T>(p, k2, pv[1]);
+            ldg_pack<T>(d, k2, dv[1]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (h == 1 && !two) break;
+            T zv[W];
 #pragma unroll
             for (int c = 0; c < W; c++) {
-                rv[c] = rv[c] - a * qv[c];
-                xv[c] += a * pv[c];
-                zv[c] = rv[c] * dv[c];
-                drz = fma(rv[c], zv[c], drz);
-                drr = fma(rv[c], rv[c], drr);
+                rv[h][c] = rv[h][c] - a * qv[h][c];
+                xv[h][c] += a * pv[h][c];
+                zv[c] = rv[h][c] * dv[h][c];
+                drz = fma(rv[h][c], zv[c], drz);
+                drr = fma(rv[h][c], rv[h][c], drr);
             }
-            st_pack<T>(r, k, rv);
-            st_pack<T>(x, k, xv);
-            st_pack<T>(z, k, zv);
-        },
-        [&](uint64_t i) {
-            const T ri = r[i] - a * q[i];
-            x[i] += a * p[i];
-            r[i] = ri;
-            const T zi = ri * d[i];
-            z[i] = zi;
-            drz = fma(ri, zi, drz);
-            drr = fma(ri, ri, drr);
-        });
-    const double brz = block_sum_v<T>(drz, sh);
-    const double brr = block_sum_v<T>(drr, sh);
+            const uint64_t kk = h ? k2 : k;
+            st_pack<T>(r, kk, rv[h]);
+            st_pack<T>(x, kk, xv[h]);
+            st_pack<T>(z, kk, zv);
+        }
+    }
+    for (uint64_t i = npk * W + tid; i < n; i += stride) {   // tail, or everything when not aligned
+        const T ri = r[i] - a * q[i];
+        x[i] += a * p[i];
+        r[i] = ri;
+        const T zi = ri * d[i];
+        z[i] = zi;
+        drz = fma(ri, zi, drz);
+        drr = fma(ri, ri, drr);
+    }
+    double brz, brr;
+    block_sum2_v<T>(drz, drr, sh, brz, brr);
     if (threadIdx.x == 0) {
         parts.rz[blockIdx.x] = brz;
         parts.rr[blockIdx.x] = brr;
     }
     if (!last_cta(&ctl->ticket, &flag)) return;
-    const double rz_new = ordered_sum(parts.rz, gridDim.x, sh);
-    const double rr = ordered_sum(parts.rr, gridDim.x, sh);
+    double rz_new, rr;
+    ordered_sum2(parts.rz, parts.rr, gridDim.x, sh, rz_new, rr);
     if (threadIdx.x == 0) {
         const int64_t it = ctl->iterations + 1;
         ctl->iterations = it;
@@ -707,7 +779,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     }
 }
 
-// Kernel C: p = z + beta p.
+// Kernel C: p = z + beta p, two packs per thread per step.
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_t n, const PcgCtl *ctl)
 {
@@ -718,17 +790,29 @@ __global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_
     const T bt = (T)ctl->beta;
     T *__restrict__ p = v.p;
     const T *__restrict__ z = v.z;
-    for_entries<T>(
-        n, aligned16(p) && aligned16(z),
-        [&](uint64_t k) {
-            T pv[W], zv[W];
-            ld_pack<T>(p, k, pv);
-            ldg_pack<T>(z, k, zv);
+    const uint64_t tid = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * kVecThreads;
+    const uint64_t npk = aligned16(p) && aligned16(z) ? n / W : 0;
+    for (uint64_t k = tid; k < npk; k += 2 * stride) {
+        const uint64_t k2 = k + stride;
+        const bool two = k2 < npk;
+        T pv[2][W], zv[2][W];
+        ld_pack<T>(p, k, pv[0]);
+        ldg_pack<T>(z, k, zv[0]);
+        if (two) {
+            ld_pack<T>(p, k2, pv[1]);
+            ldg_pack<T>(z, k2, zv[1]);
+        }
 #pragma unroll
-            for (int c = 0; c < W; c++) pv[c] = zv[c] + bt * pv[c];
-            st_pack<T>(p, k, pv);
-        },
-        [&](uint64_t i) { p[i] = z[i] + bt * p[i]; });
+        for (int c = 0; c < W; c++) pv[0][c] = zv[0][c] + bt * pv[0][c];
+        st_pack<T>(p, k, pv[0]);
+        if (two) {
+#pragma unroll
+            for (int c = 0; c < W; c++) pv[1][c] = zv[1][c] + bt * pv[1][c];
+            st_pack<T>(p, k2, pv[1]);
+        }
+    }
+    for (uint64_t i = npk * W + tid; i < n; i += stride) p[i] = z[i] + bt * p[i];
 }
 
 // z = D^-1 r (and p = z when `set_p`); partials r.z, r.r.  Shared by the start
@@ -775,15 +859,15 @@ __global__ void __launch_bounds__(kVecThreads) k_pcg_start(PcgVecs<T> v, uint64_
     __shared__ int flag;
     T drz = T(0), drr = T(0);
     precond_parts<T, true>(v, n, drz, drr);
-    const double brz = block_sum_v<T>(drz, sh);
-    const double brr = block_sum_v<T>(drr, sh);
+    double brz, brr;
+    block_sum2_v<T>(drz, drr, sh, brz, brr);
     if (threadIdx.x == 0) {
         parts.rz[blockIdx.x] = brz;
         parts.rr[blockIdx.x] = brr;
     }
     if (!last_cta(&ctl->ticket, &flag)) return;
-    const double rz = ordered_sum(parts.rz, gridDim.x, sh);
-    const double rr = ordered_sum(parts.rr, gridDim.x, sh);
+    double rz, rr;
+    ordered_sum2(parts.rz, parts.rr, gridDim.x, sh, rz, rr);
     if (threadIdx.x == 0) {
         ctl->rz = rz;
         ctl->rr = rr;
@@ -804,15 +888,15 @@ __global__ void __launch_bounds__(kVecThreads) k_pcg_resume(PcgVecs<T> v, uint64
     __shared__ int flag;
     T drz = T(0), drr = T(0);
     precond_parts<T, false>(v, n, drz, drr);
-    const double brz = block_sum_v<T>(drz, sh);
-    const double brr = block_sum_v<T>(drr, sh);
+    double brz, brr;
+    block_sum2_v<T>(drz, drr, sh, brz, brr);
     if (threadIdx.x == 0) {
         parts.rz[blockIdx.x] = brz;
         parts.rr[blockIdx.x] = brr;
     }
     if (!last_cta(&ctl->ticket, &flag)) return;
-    const double rz = ordered_sum(parts.rz, gridDim.x, sh);
-    const double rr = ordered_sum(parts.rr, gridDim.x, sh);
+    double rz, rr;
+    ordered_sum2(parts.rz, parts.rr, gridDim.x, sh, rz, rr);
     if (threadIdx.x == 0) {
         ctl->beta = ctl->rz_prev != 0.0 ? ratio * rz / ctl->rz_prev : 0.0;
         ctl->rz = rz;
