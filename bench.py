@@ -106,9 +106,15 @@ def mesh_bytes(m: am.MeshData) -> int:
     return tot
 
 
-def spmv_bytes(nnzb: int, n_rows: int, s: int, w: int) -> int:
-    """Algorithmic bytes of one block SpMV: blocks + column indices + row pointers + x read + y write."""
-    return nnzb * (s * s * w + 4) + 4 * (n_rows + 1) + 2 * n_rows * s * w
+def fold_dir() -> bool:
+    """Whether the solver's SpMV also forms p = z + beta p (the library default; AMIE_FOLD_DIR=0 turns it off)."""
+    return os.environ.get("AMIE_FOLD_DIR", "1") != "0"
+
+
+def spmv_bytes(nnzb: int, n_rows: int, s: int, w: int, fold: bool = False) -> int:
+    """Algorithmic bytes of one block SpMV: blocks + column indices + row pointers + x read + y write;
+    with the direction update folded in, z and p_old are read and q and p_new written (4 vectors)."""
+    return nnzb * (s * s * w + 4) + 4 * (n_rows + 1) + (4 if fold else 2) * n_rows * s * w
 
 
 def load_peaks():
@@ -317,7 +323,8 @@ def run_ours(args, world, rank, local, dist):
         ms32 = topo.profile_spmv(32, args.reps)
         ms64 = topo.profile_spmv(64, args.reps)
         print(json.dumps({"profile": name, "n_dof": int(n), "nnzb": int(topo.nnzb), "reps": args.reps, "ms_spmv32": ms32,
-                          "ms_spmv64": ms64, "alg_bytes32": spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 4),
+                          "ms_spmv64": ms64, "fold_dir": fold_dir(),
+                          "alg_bytes32": spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 4, fold_dir()),
                           "alg_bytes64": spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 8)}))
         topo.close()
         ctx.close()
@@ -374,11 +381,11 @@ def run_ours(args, world, rank, local, dist):
     ms_spmv = topo.profile_spmv(prec, 50)
     ms_spmv64 = topo.profile_spmv(64, 50)
     peak, peak_kind = load_peaks()
-    alg = spmv_bytes(topo.nnzb, topo.n_rows, m.stride, w)
+    alg = spmv_bytes(topo.nnzb, topo.n_rows, m.stride, w, fold_dir() and w == 4)
     alg64 = spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 8)
     achieved = alg / (ms_spmv / 1e3) / 1e9
     achieved64 = alg64 / (ms_spmv64 / 1e3) / 1e9
-    traffic = load_traffic(f"{args.config}_spmv{prec}")
+    traffic = load_traffic(f"{args.config}_{'sell_dir' if fold_dir() and w == 4 else 'sell_pq'}{prec}")
     # what one plain streaming read of the same byte count reaches in one launch on this GPU
     ms_stream = ctx.profile_stream(alg, 10)
 
@@ -399,7 +406,8 @@ def run_ours(args, world, rank, local, dist):
         "mixed_vs_fp64_dof_it": value / world / fp64_value if solver == G.SOLVER_PCG_MIXED else 1.0,
         "mixed_vs_fp64_solve_time": ms64 / (t_local * 1e3 / args.steps) if solver == G.SOLVER_PCG_MIXED else 1.0,
         "assembly_ms": ms_asm,
-        "roofline": {"bound": "hbm", "kernel": f"k_sell_pq<{m.stride},4,{'float' if w == 4 else 'double'}>",
+        "roofline": {"bound": "hbm",
+                     "kernel": f"{'k_sell_dir' if fold_dir() and w == 4 else 'k_sell_pq'}<{m.stride},{'float' if w == 4 else 'double'}>",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "alg_bytes_per_launch": alg,
                      "ms_per_launch": ms_spmv,

@@ -283,10 +283,12 @@ AMIE_API amie_status amie_damage_step(amie_topo *topo, const amie_damage_params 
  * prints wall times only (solvers/assembly.cpp:1851-1853). */
 AMIE_API amie_status amie_timer_start(amie_ctx *ctx);
 AMIE_API amie_status amie_timer_stop(amie_ctx *ctx, double *ms);
-/* Average device duration of the block SpMV kernel with its fused dot product
- * (one PCG iteration's q = A p) over `reps` back-to-back launches on the current
- * matrix; precision 64 (FP64 values) or 32 (FP32 values).  Used to report the
- * kernel's achieved bandwidth against the HBM roofline. */
+/* Average device duration of the SpMV kernel of one PCG iteration as the solver
+ * graph runs it (q = A p with the fused p.q; for precision 32 also the direction
+ * update p = z + beta p, unless AMIE_FOLD_DIR=0) over `reps` back-to-back
+ * launches on the current matrix; precision 64 (FP64 values) or 32 (FP32
+ * values).  Used to report the kernel's achieved bandwidth against the HBM
+ * roofline.  Overwrites the solver's work vectors. */
 AMIE_API amie_status amie_profile_spmv(amie_topo *topo, int32_t precision, int32_t reps, double *ms_per_launch);
 
 /* Average device duration of one plain streaming read of `bytes` bytes (16-byte

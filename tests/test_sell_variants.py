@@ -48,3 +48,26 @@ def test_sell_variant_solves(gpu_ctx, monkeypatch, name, variant):
         assert np.abs(x32[s] - xo[s]).max() <= 1e-8 * scale
     finally:
         t.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_folded_direction_is_bitwise_identical(gpu_ctx, monkeypatch, name):
+    """FP32 graphs form p = z + beta p inside the SpMV (default) or in a separate
+    kernel (AMIE_FOLD_DIR=0, read when a topology's solver state is made); both
+    compute fma(beta, p, z), so the mixed solves must agree bit for bit."""
+    import amie_gpu
+    d = load_golden(name)
+    m = am.from_golden(d, "tabulated")
+    out = []
+    for fold in ("1", "0"):
+        monkeypatch.setenv("AMIE_FOLD_DIR", fold)
+        t = amie_gpu.Topology(gpu_ctx, m)
+        try:
+            t.assemble()
+            t.apply_dirichlet(*am.golden_bcs(d))
+            out.append(t.solve(amie_gpu.SOLVER_PCG_MIXED, rtol=1e-10))
+        finally:
+            t.close()
+    (x1, s1), (x0, s0) = out
+    assert s1["iterations"] == s0["iterations"]
+    assert np.array_equal(x1, x0)

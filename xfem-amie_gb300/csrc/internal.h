@@ -194,6 +194,8 @@ struct amie_topo {
     // right-hand side, solution and solver work vectors
     amie::DevArray<double> rhs, x, r, z, p, q, xc, rc, red;
     amie::DevArray<float> r32, z32, p32, q32, d32;
+    amie::DevArray<double> p_alt;     // second direction buffers of the PCG graphs
+    amie::DevArray<float> p32_alt;
     amie::DevArray<uint8_t> fixed;
     amie::DevArray<double> fixval;
     amie::DevArray<double> strain, damage, cscale_base;   // field recovery and damage loop

@@ -28,8 +28,15 @@ struct SolverState {
     int grid = 0;                 // block-CSR SpMV, AMIE_CG and server kernels
     int grid_vec[2] = {0, 0};     // PCG vector kernels, FP32 / FP64 (resident CTAs of k_update)
     int grid_sell[2] = {0, 0};    // SELL SpMV, FP32 / FP64 (resident CTAs of that kernel)
+    int grid_dir[2] = {0, 0};     // k_sell_dir, FP32 / FP64
     int stride = 0;               // partials per kind in `parts` (the largest grid)
     bool pdl = true;              // programmatic dependent launch inside the PCG graphs
+    // FP32 graphs form p = z + beta p inside the SpMV (two kernels per iteration);
+    // FP64 graphs keep the direction kernel: folding it costs one FP64 FMA per
+    // gathered entry instead of one per vector entry, and FP64 issue is the
+    // scarce resource of this GPU (the folded FP64 solve ran 1.4x slower)
+    bool fold_dir = true;
+    int graph_kernels[2] = {3, 3};   // kernels per iteration of the FP32 / FP64 graph
     DevArray<double> parts;       // 4 * stride: pq, rz, rr, spare
     DevArray<PcgCtl> ctl;
     PcgCtl *h_ctl = nullptr;      // pinned
@@ -42,6 +49,12 @@ struct SolverState {
         if (h_ctl) cudaFreeHost(h_ctl);
     }
 };
+
+template <typename T>
+bool fold(const SolverState *s)
+{
+    return sizeof(T) == 4 && s->fold_dir;
+}
 
 static std::mutex g_state_mu;
 static std::unordered_map<const amie_topo *, SolverState *> g_states;
@@ -238,14 +251,21 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         s->grid_sell[1] = resident(k64, sm64);
         s->grid_vec[0] = resident((const void *)k_update<float>, 0);
         s->grid_vec[1] = resident((const void *)k_update<double>, 0);
+        s->grid_dir[0] = resident(t->s == 2 ? (const void *)k_sell_dir<2, float> : (const void *)k_sell_dir<3, float>, 0);
+        s->grid_dir[1] = resident(t->s == 2 ? (const void *)k_sell_dir<2, double> : (const void *)k_sell_dir<3, double>, 0);
         AMIE_CUDA(cudaGetLastError());
         AMIE_TRY(ensure_sell_partition(t, s->grid));
         AMIE_TRY(ensure_sell_partition(t, s->grid_sell[0]));
         AMIE_TRY(ensure_sell_partition(t, s->grid_sell[1]));
-        s->stride = std::max(std::max(s->grid, std::max(s->grid_vec[0], s->grid_vec[1])),
-                             std::max(s->grid_sell[0], s->grid_sell[1]));
-        // tuning override for measurements: AMIE_PDL=0 launches the PCG graph kernels plainly
+        AMIE_TRY(ensure_sell_partition(t, s->grid_dir[0]));
+        AMIE_TRY(ensure_sell_partition(t, s->grid_dir[1]));
+        s->stride = std::max(std::max(std::max(s->grid, std::max(s->grid_vec[0], s->grid_vec[1])),
+                                      std::max(s->grid_sell[0], s->grid_sell[1])),
+                             std::max(s->grid_dir[0], s->grid_dir[1]));
+        // tuning overrides for measurements: AMIE_PDL=0 launches the PCG graph kernels plainly,
+        // AMIE_FOLD_DIR=0 keeps the separate direction kernel (three kernels per iteration)
         if (const char *e = std::getenv("AMIE_PDL")) s->pdl = std::atoi(e) != 0;
+        if (const char *e = std::getenv("AMIE_FOLD_DIR")) s->fold_dir = std::atoi(e) != 0;
         AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->stride));
         AMIE_TRY(s->ctl.alloc(t->ctx, 1));
         AMIE_CUDA(cudaMallocHost((void **)&s->h_ctl, sizeof(PcgCtl)));
@@ -254,6 +274,7 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         AMIE_TRY(t->z.alloc(t->ctx, n));
         AMIE_TRY(t->p.alloc(t->ctx, n));
         AMIE_TRY(t->q.alloc(t->ctx, n));
+        AMIE_TRY(t->p_alt.alloc(t->ctx, n));
     }
     if (want32 && !t->r32.p) {
         const uint64_t n = t->n;
@@ -262,6 +283,7 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         AMIE_TRY(t->p32.alloc(t->ctx, n));
         AMIE_TRY(t->q32.alloc(t->ctx, n));
         AMIE_TRY(t->d32.alloc(t->ctx, n));
+        AMIE_TRY(t->p32_alt.alloc(t->ctx, n));
     }
     *out = s;
     return AMIE_OK;
@@ -282,12 +304,28 @@ PcgVecs<T> vecs_of(amie_topo *t);
 template <>
 PcgVecs<double> vecs_of<double>(amie_topo *t)
 {
-    return PcgVecs<double>{bsr64(t), t->invdiag.p, t->x.p, t->r.p, t->z.p, t->p.p, t->q.p};
+    return PcgVecs<double>{bsr64(t), t->invdiag.p, t->x.p, t->r.p, t->z.p, t->p.p, t->q.p, t->p_alt.p};
 }
 template <>
 PcgVecs<float> vecs_of<float>(amie_topo *t)
 {
-    return PcgVecs<float>{bsr32(t), t->invdiag32.p, t->d32.p, t->r32.p, t->z32.p, t->p32.p, t->q32.p};
+    return PcgVecs<float>{bsr32(t), t->invdiag32.p, t->d32.p, t->r32.p, t->z32.p, t->p32.p, t->q32.p, t->p32_alt.p};
+}
+
+// q = A p with p = z + beta p formed inside the SpMV (two direction buffers, see
+// k_sell_dir); false when the SELL copy or the CTA table for `grid` is missing.
+template <typename T>
+bool launch_spmv_dir(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, PcgCtl *ctl, bool fin,
+                     cudaStream_t st, bool pdl)
+{
+    SellView<T> sv = sell_of<T>(t);
+    auto it = t->sell_cta_first.find(grid);
+    if (!sv.val || it == t->sell_cta_first.end() || !v.p2) return false;
+    sv.cta_first = it->second.p;
+    if (t->s == 2) launch_k(pdl, k_sell_dir<2, T>, grid, 0, st, sv, v, part, ctl, fin ? 1 : 0);
+    else launch_k(pdl, k_sell_dir<3, T>, grid, 0, st, sv, v, part, ctl, fin ? 1 : 0);
+    AMIE_LAUNCHED();
+    return true;
 }
 
 constexpr int kGraphIters = 16;   // PCG iterations per graph launch
@@ -301,17 +339,28 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     PcgParts parts = parts_of(s);
     cudaGraph_t graph;
     AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    const int gs = s->grid_sell[sizeof(T) == 8 ? 1 : 0];
-    const int gv = s->grid_vec[sizeof(T) == 8 ? 1 : 0];
+    const int pi = sizeof(T) == 8 ? 1 : 0;
+    const int gs = s->grid_sell[pi];
+    const int gd = s->grid_dir[pi];
+    const int gv = s->grid_vec[pi];
     const uint64_t n = t->n;
     PcgCtl *ctl = s->ctl.p;
+    const uint64_t before = g_launches.load();
     for (int it = 0; it < kGraphIters; it++) {
         // the first kernel follows the previous graph launch in plain stream order
-        launch_spmv_pq<T>(t, gs, v, parts.pq, &ctl->done, ctl, st, s->pdl && it > 0);
-        launch_k(s->pdl, k_update<T>, gv, 0, st, v, n, parts, ctl);
-        launch_k(s->pdl, k_direction<T>, gv, 0, st, v, n, (const PcgCtl *)ctl);
+        if (fold<T>(s)) {
+            launch_spmv_dir<T>(t, gd, v, parts.pq, ctl, true, st, s->pdl && it > 0);
+            launch_k(s->pdl, k_update<T>, gv, 0, st, v, n, parts, ctl);
+        } else {
+            PcgVecs<T> v1 = v;
+            v1.p2 = nullptr;   // one direction buffer: k_direction forms p
+            launch_spmv_pq<T>(t, gs, v1, parts.pq, &ctl->done, ctl, st, s->pdl && it > 0);
+            launch_k(s->pdl, k_update<T>, gv, 0, st, v1, n, parts, ctl);
+            launch_k(s->pdl, k_direction<T>, gv, 0, st, v1, n, (const PcgCtl *)ctl);
+        }
     }
-    g_launches -= kGraphIters;   // captured, not launched: counted per graph launch
+    s->graph_kernels[pi] = fold<T>(s) ? 2 : 3;
+    g_launches = before;   // captured, not launched: counted per graph launch
     AMIE_CUDA(cudaStreamEndCapture(st, &graph));
     cudaError_t e = cudaGraphInstantiate(g, graph, 0);
     cudaGraphDestroy(graph);
@@ -351,7 +400,7 @@ amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iter
     const int64_t max_launches = maxit / kGraphIters + 2;
     for (int64_t launch = 0;; launch++) {
         AMIE_CUDA(cudaGraphLaunch(*g, st));
-        g_launches += 3 * kGraphIters;
+        g_launches += s->graph_kernels[sizeof(T) == 8 ? 1 : 0] * kGraphIters;
         AMIE_CUDA(cudaMemcpyAsync(s->h_ctl, s->ctl.p, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
         AMIE_CUDA(cudaStreamSynchronize(st));
         if (s->h_ctl->done) break;
@@ -378,6 +427,8 @@ amie_status run_pcg(amie_topo *t, SolverState *s, double tol2, int64_t maxit, in
     init.iterations = 0;
     init.maxit = maxit;
     init.tol2 = tol2;
+    init.beta = 0.0;   // with the direction folded into the SpMV, the first p is z + 0 p
+    init.pcur = 0;     // k_pcg_start writes p into the first buffer
     *s->h_ctl = init;
     AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
     k_pcg_start<T><<<s->grid_vec[sizeof(T) == 8 ? 1 : 0], kVecThreads, 0, st>>>(vecs_of<T>(t), t->n, parts_of(s),
@@ -398,8 +449,13 @@ amie_status resume_pcg(amie_topo *t, SolverState *s, double ratio, double tol2, 
     const PcgVecs<T> v = vecs_of<T>(t);
     const int gv = s->grid_vec[sizeof(T) == 8 ? 1 : 0];
     k_pcg_resume<T><<<gv, kVecThreads, 0, st>>>(v, t->n, parts_of(s), s->ctl.p, ratio, tol2, maxit);
-    k_direction<T><<<gv, kVecThreads, 0, st>>>(v, t->n, s->ctl.p);
-    g_launches += 2;
+    g_launches += 1;
+    if (!fold<T>(s)) {   // else the graph's first SpMV forms p = z + beta p from the latest p
+        PcgVecs<T> v1 = v;
+        v1.p2 = nullptr;
+        k_direction<T><<<gv, kVecThreads, 0, st>>>(v1, t->n, s->ctl.p);
+        g_launches += 1;
+    }
     AMIE_CUDA(cudaGetLastError());
     return drive_pcg<T>(t, s, maxit, iters, rr_out);
 }
@@ -607,14 +663,29 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     if (precision == 32 && !t->have32) AMIE_TRY(finalize_matrix_async(t, true));
     AMIE_TRY(ensure_sell(t, precision == 64, precision == 32));
     cudaStream_t st = t->ctx->stream;
-    // p = 1 keeps the inputs defined; the kernel's cost does not depend on the values
-    if (precision == 64) AMIE_CUDA(cudaMemsetAsync(t->p.p, 0, t->n * 8, st));
-    else AMIE_CUDA(cudaMemsetAsync(t->p32.p, 0, t->n * 4, st));
+    // zeroed inputs keep every value defined; the kernel's cost does not depend on them
+    const size_t w = precision == 64 ? 8 : 4;
+    void *vz = precision == 64 ? (void *)t->z.p : (void *)t->z32.p;
+    void *vp = precision == 64 ? (void *)t->p.p : (void *)t->p32.p;
+    void *vp2 = precision == 64 ? (void *)t->p_alt.p : (void *)t->p32_alt.p;
+    AMIE_CUDA(cudaMemsetAsync(vz, 0, t->n * w, st));
+    AMIE_CUDA(cudaMemsetAsync(vp, 0, t->n * w, st));
+    AMIE_CUDA(cudaMemsetAsync(vp2, 0, t->n * w, st));
+    // the SpMV kernel of the solver graph: with the direction folded in, beta = 0.5, first buffer current
+    PcgCtl c{};
+    c.beta = 0.5;
+    *s->h_ctl = c;
+    AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
     PcgParts parts = parts_of(s);
+    const int pi = precision == 64 ? 1 : 0;
     for (int i = 0; i <= reps; i++) {   // launch 0 is a warm-up
         if (i == 1) AMIE_CUDA(cudaEventRecord(t->ctx->ev0, st));
-        if (precision == 64) launch_spmv_pq<double>(t, s->grid_sell[1], vecs_of<double>(t), parts.pq, nullptr, nullptr, st);
-        else launch_spmv_pq<float>(t, s->grid_sell[0], vecs_of<float>(t), parts.pq, nullptr, nullptr, st);
+        if (precision == 32 && fold<float>(s)) {
+            launch_spmv_dir<float>(t, s->grid_dir[pi], vecs_of<float>(t), parts.pq, s->ctl.p, false, st, false);
+        } else {
+            if (precision == 64) launch_spmv_pq<double>(t, s->grid_sell[pi], vecs_of<double>(t), parts.pq, nullptr, nullptr, st);
+            else launch_spmv_pq<float>(t, s->grid_sell[pi], vecs_of<float>(t), parts.pq, nullptr, nullptr, st);
+        }
     }
     AMIE_CUDA(cudaEventRecord(t->ctx->ev1, st));
     AMIE_CUDA(cudaEventSynchronize(t->ctx->ev1));

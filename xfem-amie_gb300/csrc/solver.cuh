@@ -44,6 +44,8 @@ struct PcgCtl {
     double tol2;           // stop when r.r <= tol2
     double alpha, beta, rz, rr, pq;
     double rz_prev;        // r.z of the iteration before the last one (kept for a resumed run)
+    int32_t pcur;          // with two direction buffers: the one holding the latest p (0 = p, 1 = p2)
+    int32_t pad_;
 };
 
 // Per-CTA partial sums.
@@ -59,6 +61,7 @@ struct PcgVecs {
     BsrView<T> A;
     const T *dinv;
     T *x, *r, *z, *p, *q;
+    T *p2 = nullptr;   // second direction buffer: p = z + beta p is then formed inside k_sell_dir
 };
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -443,6 +446,88 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
     finish_pq<T>(dot, part_pq, fin, sh, &flag);
 }
 
+// Kernel A with the direction update folded in (used with two direction
+// buffers): p_new = z + beta p_old is formed for every x entry the SpMV gathers
+// and stored for the warp's own rows, q = A p_new, partial p_new.q; last CTA:
+// pq and alpha.  p_old / p_new are chosen by ctl->pcur (flipped by k_update),
+// so a graph of iterations needs no copies.  Same scheduling, FMA order and
+// fixed-order dot as k_sell_pq; p_new equals k_direction's fma(beta, p, z).
+template <int S, typename T>
+__global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs<T> v, double *part_pq, PcgCtl *ctl,
+                                                          int fin)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    __shared__ uint32_t next_sl;
+    pdl_wait();
+    pdl_release();
+    if (ctl->done) return;
+    constexpr int U = kSpmvUnroll;
+    constexpr uint32_t WPB = kVecThreads / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    const T bt = (T)ctl->beta;
+    const bool second = ctl->pcur != 0;
+    const T *__restrict__ pold = second ? v.p2 : v.p;
+    T *__restrict__ pnew = second ? v.p : v.p2;
+    const T *__restrict__ z = v.z;
+    T *__restrict__ q = v.q;
+    const uint32_t s_beg = __ldg(A.cta_first + blockIdx.x), s_end = __ldg(A.cta_first + blockIdx.x + 1);
+    if (threadIdx.x == 0) next_sl = s_beg + WPB;
+    __syncthreads();
+    for (uint32_t sl = s_beg + (threadIdx.x >> 5); sl < s_end;) {
+        const uint32_t row = __ldg(A.perm + (uint64_t)sl * 32 + lane);
+        const uint64_t g0 = __ldg(A.slice_ptr + sl);
+        const uint32_t len = (uint32_t)((__ldg(A.slice_ptr + sl + 1) - g0) >> 5);
+        T acc[S];
+#pragma unroll
+        for (int r = 0; r < S; r++) acc[r] = T(0);
+        uint32_t c[U];
+        T blk[U][S * S];
+        for (uint32_t j0 = 0; j0 < len; j0 += U) {
+            load_sell_group<S, U, T>(A, g0, j0, len, lane, c, blk);
+            T zv[U][S], pv[U][S];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+                    load_x<S, T>(z, c[u], zv[u]);
+                    load_x<S, T>(pold, c[u], pv[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+#pragma unroll
+                    for (int r = 0; r < S; r++)
+#pragma unroll
+                        for (int cc = 0; cc < S; cc++)
+                            acc[r] = fma(blk[u][r * S + cc], fma(bt, pv[u][cc], zv[u][cc]), acc[r]);
+                }
+            }
+        }
+        T dot = T(0);
+        if (row < A.n_rows) {
+#pragma unroll
+            for (int r = 0; r < S; r++) {
+                const uint64_t i = (uint64_t)row * S + r;
+                const T pn = fma(bt, pold[i], z[i]);
+                pnew[i] = pn;
+                q[i] = acc[r];
+                dot = fma(acc[r], pn, dot);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        if (lane == 0) A.slice_dot[sl] = dot;
+        uint32_t nx = 0;
+        if (lane == 0) nx = atomicAdd(&next_sl, 1u);
+        sl = __shfl_sync(0xffffffffu, nx, 0);
+    }
+    __syncthreads();
+    T dot = T(0);
+    for (uint32_t i = s_beg + threadIdx.x; i < s_end; i += kVecThreads) dot += A.slice_dot[i];
+    finish_pq<T>(dot, part_pq, fin ? ctl : nullptr, sh, &flag);
+}
+
 // Asynchronous 16-byte global -> shared copies (completion tracked per thread
 // in commit groups; cp.async.wait_group is a hardware wait on those copies).
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -703,7 +788,8 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     T *__restrict__ x = v.x;
     T *__restrict__ r = v.r;
     T *__restrict__ z = v.z;
-    const T *__restrict__ p = v.p;
+    // with two direction buffers the SpMV just wrote this iteration's p into the other one
+    const T *__restrict__ p = v.p2 ? (ctl->pcur ? v.p : v.p2) : v.p;
     const T *__restrict__ q = v.q;
     const T *__restrict__ d = v.dinv;
     T drz = T(0), drr = T(0);   // per-thread partials in the vector precision, CTA sums in FP64
@@ -734,7 +820,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
 #pragma unroll
             for (int c = 0; c < W; c++) {
                 rv[h][c] = rv[h][c] - a * qv[h][c];
-                xv[h][c] += a * pv[h][c];
+                xv[h][c] = fma(a, pv[h][c], xv[h][c]);
                 zv[c] = rv[h][c] * dv[h][c];
                 drz = fma(rv[h][c], zv[c], drz);
                 drr = fma(rv[h][c], rv[h][c], drr);
@@ -747,7 +833,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     }
     for (uint64_t i = npk * W + tid; i < n; i += stride) {   // tail, or everything when not aligned
         const T ri = r[i] - a * q[i];
-        x[i] += a * p[i];
+        x[i] = fma(a, p[i], x[i]);
         r[i] = ri;
         const T zi = ri * d[i];
         z[i] = zi;
@@ -775,6 +861,7 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
             ctl->beta = ctl->rz != 0.0 ? rz_new / ctl->rz : 0.0;
         }
         ctl->rz = rz_new;
+        if (v.p2) ctl->pcur ^= 1;   // this iteration's p is now the latest
         ctl->ticket = 0;
     }
 }
@@ -804,15 +891,15 @@ __global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_
             ldg_pack<T>(z, k2, zv[1]);
         }
 #pragma unroll
-        for (int c = 0; c < W; c++) pv[0][c] = zv[0][c] + bt * pv[0][c];
+        for (int c = 0; c < W; c++) pv[0][c] = fma(bt, pv[0][c], zv[0][c]);
         st_pack<T>(p, k, pv[0]);
         if (two) {
 #pragma unroll
-            for (int c = 0; c < W; c++) pv[1][c] = zv[1][c] + bt * pv[1][c];
+            for (int c = 0; c < W; c++) pv[1][c] = fma(bt, pv[1][c], zv[1][c]);
             st_pack<T>(p, k2, pv[1]);
         }
     }
-    for (uint64_t i = npk * W + tid; i < n; i += stride) p[i] = z[i] + bt * p[i];
+    for (uint64_t i = npk * W + tid; i < n; i += stride) p[i] = fma(bt, p[i], z[i]);
 }
 
 // z = D^-1 r (and p = z when `set_p`); partials r.z, r.r.  Shared by the start
