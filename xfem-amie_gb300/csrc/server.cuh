@@ -25,189 +25,101 @@ namespace amie {
 
 constexpr int kBatchIters = 16;
 
-// Device view of one slot.
+// Device view of one slot: the slot's SELL copies (CTA table for its own CTA
+// count), vectors, control block and its range of the batch's partial sums.
 struct SlotDesc {
-    BsrView<float> A32;      // inner matrix (FP32 values) -- or FP64 below
-    BsrView<double> A64;
-    const float *dinv32;
-    const double *dinv64;
-    float *d32, *r32, *z32, *p32, *q32;   // inner vectors (mixed)
-    double *x64, *r64, *z64, *p64, *q64;  // FP64 vectors
+    SellView<float> A32;
+    SellView<double> A64;
+    PcgVecs<float> v32;      // inner vectors of the mixed solve (two direction buffers)
+    PcgVecs<double> v64;     // FP64 vectors (one direction buffer)
+    PcgParts parts;          // the batch partials of CTAs c0 .. c1-1
+    PcgCtl *ctl;             // the slot's control block
     uint64_t n;
     int32_t c0, c1;          // CTA range in the batch grid
     int32_t active;          // 1 = iterate
     int32_t mixed;
 };
 
-struct SlotCtl {
-    int32_t done;            // inner run finished (converged or capped)
-    int32_t pad;
-    int64_t iterations;      // inner iterations of the current run
-    int64_t maxit;
-    double tol2;
-    double rr;
-};
-
-__device__ __forceinline__ double slot_sum(const double *parts, int c0, int c1, double *sh)
-{
-    double v = 0.0;
-    for (int i = c0 + threadIdx.x; i < c1; i += kVecThreads) v += parts[i];
-    v = block_sum(v, sh);
-    if (threadIdx.x == 0) sh[32] = v;
-    __syncthreads();
-    const double r = sh[32];
-    __syncthreads();
-    return r;
-}
+template <typename T>
+__device__ __forceinline__ const SellView<T> &slot_A(const SlotDesc &d);
+template <>
+__device__ __forceinline__ const SellView<float> &slot_A<float>(const SlotDesc &d) { return d.A32; }
+template <>
+__device__ __forceinline__ const SellView<double> &slot_A<double>(const SlotDesc &d) { return d.A64; }
 
 template <typename T>
-__device__ __forceinline__ BsrView<T> slot_A(const SlotDesc &d);
+__device__ __forceinline__ const PcgVecs<T> &slot_v(const SlotDesc &d);
 template <>
-__device__ __forceinline__ BsrView<float> slot_A<float>(const SlotDesc &d) { return d.A32; }
+__device__ __forceinline__ const PcgVecs<float> &slot_v<float>(const SlotDesc &d) { return d.v32; }
 template <>
-__device__ __forceinline__ BsrView<double> slot_A<double>(const SlotDesc &d) { return d.A64; }
+__device__ __forceinline__ const PcgVecs<double> &slot_v<double>(const SlotDesc &d) { return d.v64; }
 
-template <typename T>
-struct SlotVecs {
-    const T *dinv;
-    T *x, *r, *z, *p, *q;
-};
-template <typename T>
-__device__ __forceinline__ SlotVecs<T> slot_vecs(const SlotDesc &d);
-template <>
-__device__ __forceinline__ SlotVecs<float> slot_vecs<float>(const SlotDesc &d)
+// The slot of this CTA and the CTA's place in the slot's group, or null when
+// the CTA has no slot, the slot is idle or its run has finished.
+__device__ __forceinline__ const SlotDesc *slot_of(const SlotDesc *slots, const int16_t *cta_slot, Cta *c)
 {
-    return SlotVecs<float>{d.dinv32, d.d32, d.r32, d.z32, d.p32, d.q32};
-}
-template <>
-__device__ __forceinline__ SlotVecs<double> slot_vecs<double>(const SlotDesc &d)
-{
-    return SlotVecs<double>{d.dinv64, d.x64, d.r64, d.z64, d.p64, d.q64};
-}
-
-// Batched kernel A: q = A p per slot, partial p.q per CTA.
-template <typename T, int G>
-__global__ void __launch_bounds__(kVecThreads) kb_spmv_pq(const SlotDesc *slots, const int16_t *cta_slot,
-                                                          const SlotCtl *ctl, double *part_pq)
-{
-    __shared__ double sh[33];
     const int s = cta_slot[blockIdx.x];
-    if (s < 0) return;
-    const SlotDesc d = slots[s];
-    if (!d.active || ctl[s].done) return;
-    constexpr int RPB = kVecThreads / G;
-    const int lane = threadIdx.x % G;
-    const BsrView<T> A = slot_A<T>(d);
-    const SlotVecs<T> v = slot_vecs<T>(d);
-    const int lc = blockIdx.x - d.c0, nc = d.c1 - d.c0;
-    double dot = 0.0;
-    for (uint32_t base = lc * RPB; base < A.n_rows; base += nc * RPB) {
-        const uint32_t row = base + threadIdx.x / G;
-        const bool valid = row < A.n_rows;
-        const uint32_t rb = valid ? __ldg(A.row_ptr + row) : 0u, re = valid ? __ldg(A.row_ptr + row + 1) : 0u;
-        T acc[2];
-        row_spmv<2, G, T>(A, v.p, rb, re, lane, acc);
-        if (valid && lane == 0) {
-            v.q[(uint64_t)row * 2] = acc[0];
-            v.q[(uint64_t)row * 2 + 1] = acc[1];
-            dot += (double)acc[0] * (double)v.p[(uint64_t)row * 2] + (double)acc[1] * (double)v.p[(uint64_t)row * 2 + 1];
-        }
-    }
-    dot = block_sum(dot, sh);
-    if (threadIdx.x == 0) part_pq[blockIdx.x] = dot;
+    if (s < 0) return nullptr;
+    const SlotDesc *d = slots + s;
+    if (!d->active || d->ctl->done) return nullptr;
+    *c = Cta{blockIdx.x - (uint32_t)d->c0, (uint32_t)(d->c1 - d->c0)};
+    return d;
 }
 
-// Batched kernel B: per-slot alpha, update, partials r.z and r.r.
+// Batched kernel A (mixed): per slot, p = z + beta p folded into q = A p, p.q,
+// alpha -- the single-solve k_sell_dir on the slot's own CTAs.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) kb_update(const SlotDesc *slots, const int16_t *cta_slot, SlotCtl *ctl,
-                                                         const double *part_pq, double *part_rz0, double *part_rz1,
-                                                         double *part_rr, int parity)
+__global__ void __launch_bounds__(kVecThreads) kb_sell_dir(const SlotDesc *slots, const int16_t *cta_slot)
 {
-    __shared__ double sh[33];
-    const int s = cta_slot[blockIdx.x];
-    if (s < 0) return;
-    const SlotDesc d = slots[s];
-    if (!d.active || ctl[s].done) return;
-    double *rz_new = parity ? part_rz1 : part_rz0;
-    const double *rz_old = parity ? part_rz0 : part_rz1;
-    const double pq = slot_sum(part_pq, d.c0, d.c1, sh);
-    const double rz = slot_sum(rz_old, d.c0, d.c1, sh);
-    const double alpha = pq != 0.0 ? rz / pq : 0.0;
-    const T a = (T)alpha;
-    const SlotVecs<T> v = slot_vecs<T>(d);
-    const int lc = blockIdx.x - d.c0, nc = d.c1 - d.c0;
-    double drz = 0.0, drr = 0.0;
-    for (uint64_t i = (uint64_t)lc * kVecThreads + threadIdx.x; i < d.n; i += (uint64_t)nc * kVecThreads) {
-        const T ri = v.r[i] - a * v.q[i];
-        v.x[i] += a * v.p[i];
-        v.r[i] = ri;
-        const T zi = ri * v.dinv[i];
-        v.z[i] = zi;
-        drz += (double)ri * (double)zi;
-        drr += (double)ri * (double)ri;
-    }
-    drz = block_sum(drz, sh);
-    drr = block_sum(drr, sh);
-    if (threadIdx.x == 0) {
-        rz_new[blockIdx.x] = drz;
-        part_rr[blockIdx.x] = drr;
-        if (blockIdx.x == d.c0) ctl[s].iterations += 1;
-    }
+    pdl_wait();
+    pdl_release();
+    Cta c;
+    const SlotDesc *d = slot_of(slots, cta_slot, &c);
+    if (!d) return;
+    sell_dir_body<2, T>(slot_A<T>(*d), slot_v<T>(*d), d->parts.pq, d->ctl, true, c);
 }
 
-// Batched kernel C: per-slot stop test, beta, p = z + beta p.
+// Batched kernel A (FP64): per slot q = A p, p.q, alpha.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) kb_direction(const SlotDesc *slots, const int16_t *cta_slot, SlotCtl *ctl,
-                                                            const double *part_rz0, const double *part_rz1,
-                                                            const double *part_rr, int parity)
+__global__ void __launch_bounds__(kVecThreads) kb_sell_pq(const SlotDesc *slots, const int16_t *cta_slot)
 {
     __shared__ double sh[33];
-    const int s = cta_slot[blockIdx.x];
-    if (s < 0) return;
-    const SlotDesc d = slots[s];
-    if (!d.active || ctl[s].done) return;
-    const double *rz_new = parity ? part_rz1 : part_rz0;
-    const double *rz_old = parity ? part_rz0 : part_rz1;
-    const double rzn = slot_sum(rz_new, d.c0, d.c1, sh);
-    const double rzo = slot_sum(rz_old, d.c0, d.c1, sh);
-    const double rr = slot_sum(part_rr, d.c0, d.c1, sh);
-    const bool stop = rr <= ctl[s].tol2 || ctl[s].iterations >= ctl[s].maxit || !(rr == rr);
-    if (stop) {
-        if (blockIdx.x == d.c0 && threadIdx.x == 0) {
-            ctl[s].done = 1;
-            ctl[s].rr = rr;
-        }
-        return;
-    }
-    const T bt = (T)(rzo != 0.0 ? rzn / rzo : 0.0);
-    const SlotVecs<T> v = slot_vecs<T>(d);
-    const int lc = blockIdx.x - d.c0, nc = d.c1 - d.c0;
-    for (uint64_t i = (uint64_t)lc * kVecThreads + threadIdx.x; i < d.n; i += (uint64_t)nc * kVecThreads)
-        v.p[i] = v.z[i] + bt * v.p[i];
+    __shared__ int flag;
+    __shared__ uint32_t next_sl;
+    pdl_wait();
+    pdl_release();
+    Cta c;
+    const SlotDesc *d = slot_of(slots, cta_slot, &c);
+    if (!d) return;
+    const PcgVecs<T> &v = slot_v<T>(*d);
+    sell_pq_body<2, kSpmvUnroll, false, T>(slot_A<T>(*d), v.p, v.q, d->parts.pq, d->ctl, sh, &flag, &next_sl, c);
 }
 
-// Start of an inner run of one slot: z = D^-1 r, p = z, partials r.z -> rz[1], r.r.
+// Batched kernel B: per slot x, r, z updates, r.z, r.r; last CTA of the slot:
+// stop test and beta.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) kb_start(SlotDesc d, double *part_rz1, double *part_rr)
+__global__ void __launch_bounds__(kVecThreads) kb_update(const SlotDesc *slots, const int16_t *cta_slot)
 {
-    __shared__ double sh[33];
-    const SlotVecs<T> v = slot_vecs<T>(d);
-    const int nc = d.c1 - d.c0;
-    double drz = 0.0, drr = 0.0;
-    for (uint64_t i = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x; i < d.n; i += (uint64_t)nc * kVecThreads) {
-        const T ri = v.r[i];
-        const T zi = ri * v.dinv[i];
-        v.z[i] = zi;
-        v.p[i] = zi;
-        drz += (double)ri * (double)zi;
-        drr += (double)ri * (double)ri;
-    }
-    drz = block_sum(drz, sh);
-    drr = block_sum(drr, sh);
-    if (threadIdx.x == 0) {
-        part_rz1[d.c0 + blockIdx.x] = drz;
-        part_rr[d.c0 + blockIdx.x] = drr;
-    }
+    __shared__ double sh[2 * (kVecThreads >> 5)];
+    __shared__ int flag;
+    pdl_wait();
+    pdl_release();
+    Cta c;
+    const SlotDesc *d = slot_of(slots, cta_slot, &c);
+    if (!d) return;
+    update_body<T>(slot_v<T>(*d), d->n, d->parts, d->ctl, sh, &flag, c);
+}
+
+// Batched kernel C (FP64): per slot p = z + beta p.
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) kb_direction(const SlotDesc *slots, const int16_t *cta_slot)
+{
+    pdl_wait();
+    pdl_release();
+    Cta c;
+    const SlotDesc *d = slot_of(slots, cta_slot, &c);
+    if (!d) return;
+    direction_body<T>(slot_v<T>(*d), d->n, d->ctl, c);
 }
 
 }  // namespace amie
@@ -235,7 +147,7 @@ struct amie_server {
         double t_submit = 0, t_admit = 0, t_done = 0;
         amie_topo *topo = nullptr;
         int slot = -1;
-        double bnorm = 0, rnorm = 0;
+        double bnorm = 0, rnorm = 0;   // rnorm: the true residual the current inner run was scaled by
         int64_t iterations = 0;
         int refinements = 0;
         amie_status status = AMIE_NOT_READY;
@@ -255,11 +167,11 @@ struct amie_server {
     // batch state
     std::vector<Req *> slot_req;                 // per slot
     amie::DevArray<amie::SlotDesc> d_slots;
-    amie::DevArray<amie::SlotCtl> d_ctl;
+    amie::DevArray<amie::PcgCtl> d_ctl;         // per slot
     amie::DevArray<int16_t> d_cta_slot;
-    amie::DevArray<double> d_parts;              // pq | rz0 | rz1 | rr, grid each
+    amie::DevArray<double> d_parts;              // pq | rz | rr | spare, grid each
     amie::SlotDesc *h_slots = nullptr;           // pinned
-    amie::SlotCtl *h_ctl = nullptr;              // pinned
+    amie::PcgCtl *h_ctl = nullptr;               // pinned
     int16_t *h_cta_slot = nullptr;               // pinned
     cudaGraphExec_t graph = nullptr;
     std::string error;
@@ -280,7 +192,7 @@ static void copy_vec(std::vector<T> &dst, const T *src, size_t n)
 }
 
 // Device bytes a request needs: staged element blocks, pattern keys and sort
-// scratch, matrix (FP64 + FP32), scatter map, vectors, element data.
+// scratch, matrix (FP64 + FP32), SELL copies, scatter map, vectors, element data.
 static uint64_t request_footprint(const amie_mesh &m)
 {
     uint64_t blocks = 0;
@@ -291,8 +203,8 @@ static uint64_t request_footprint(const amie_mesh &m)
     const uint64_t s2 = (uint64_t)m.stride * m.stride;
     const uint64_t rows = m.ndofmax ? m.ndofmax : 1;
     const uint64_t n = rows * m.stride;
-    return blocks * (s2 * 8 + 48) + blocks * (s2 * 12 + 8) + n * 8 * 16 + (uint64_t)m.n_elem * 64 +
-           (uint64_t)m.gp_ptr[m.n_elem] * 64 + (16u << 20);
+    return blocks * (s2 * 8 + 48) + blocks * (s2 * 12 + 8) + blocks * (s2 * 12 + 16) + n * 8 * 18 +
+           (uint64_t)m.n_elem * 64 + (uint64_t)m.gp_ptr[m.n_elem] * 64 + (16u << 20);
 }
 
 struct ServerOps {
@@ -334,6 +246,8 @@ struct ServerOps {
         SolverState *s = nullptr;
         AMIE_TRY(ensure_state(t, srv->mixed, &s));
         if (srv->mixed) AMIE_TRY(finalize_matrix_async(t, true));
+        AMIE_TRY(ensure_sell(t, !srv->mixed, srv->mixed));
+        AMIE_TRY(ensure_sell_partition(t, ctas_for(t->n_rows)));   // the slot's CTA count
         cudaStream_t st = srv->adm->stream;
         if (!r->x0.empty() && r->x0.size() == t->n)
             AMIE_CUDA(cudaMemcpyAsync(t->x.p, r->x0.data(), t->n * 8, cudaMemcpyHostToDevice, st));
@@ -370,12 +284,18 @@ struct ServerOps {
     static void fill_desc(amie_server *srv, int slot, amie_topo *t, int c0, int c1)
     {
         SlotDesc &d = srv->h_slots[slot];
-        d.A64 = bsr64(t);
-        d.A32 = t->val32.p ? bsr32(t) : BsrView<float>{t->n_rows, t->row_ptr.p, t->col.p, nullptr};
-        d.dinv32 = t->invdiag32.p;
-        d.dinv64 = t->invdiag.p;
-        d.d32 = t->d32.p; d.r32 = t->r32.p; d.z32 = t->z32.p; d.p32 = t->p32.p; d.q32 = t->q32.p;
-        d.x64 = t->x.p; d.r64 = t->r.p; d.z64 = t->z.p; d.p64 = t->p.p; d.q64 = t->q.p;
+        const uint32_t *first = t->sell_cta_first.at(c1 - c0).p;
+        d.A32 = sell_of<float>(t);
+        d.A32.cta_first = first;
+        d.A64 = sell_of<double>(t);
+        d.A64.cta_first = first;
+        d.v32 = vecs_of<float>(t);
+        d.v64 = vecs_of<double>(t);
+        d.v64.p2 = nullptr;   // FP64 batches keep the direction kernel
+        const int g = srv->grid;
+        double *pp = srv->d_parts.p;
+        d.parts = PcgParts{pp + c0, pp + g + c0, pp + 2 * g + c0, pp + 3 * g + c0};
+        d.ctl = srv->d_ctl.p + slot;
         d.n = t->n;
         d.c0 = c0;
         d.c1 = c1;
@@ -383,34 +303,58 @@ struct ServerOps {
         d.mixed = srv->mixed ? 1 : 0;
     }
 
-    // Start (or restart) the inner run of a slot from its FP64 residual r64 (norm rnorm).
+    // FP32 residual reduction between two FP64 residual replacements of a mixed slot.
+    static constexpr double kInnerReduction = 0.1;
+
+    // Start (or restart, with a fresh search direction) the inner run of a slot
+    // from its FP64 residual r64 (norm rnorm).
     static amie_status start_inner(amie_server *srv, int slot, amie_server::Req *r)
     {
         cudaStream_t st = srv->ctx->stream;
         amie_topo *t = r->topo;
         const SlotDesc &d = srv->h_slots[slot];
         const int nc = d.c1 - d.c0;
-        double *pq = srv->d_parts.p, *rz1 = srv->d_parts.p + 2 * srv->grid, *rr = srv->d_parts.p + 3 * srv->grid;
-        (void)pq;
-        SlotCtl c{};
-        c.done = 0;
-        c.iterations = 0;
+        PcgCtl c{};
         const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
         c.maxit = std::max<int64_t>(1, maxit - r->iterations);
         if (srv->mixed) {
-            k_scale_to_f32<<<nc, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / r->rnorm, t->r32.p, t->d32.p);
-            kb_start<float><<<nc, kVecThreads, 0, st>>>(d, rz1, rr);
-            const double inner = 1e-5;
+            const double need = 0.3 * srv->cfg.rtol * r->bnorm / r->rnorm;
+            const double inner = std::min(0.5, std::max(kInnerReduction, need));
             c.tol2 = inner * inner;
         } else {
-            kb_start<double><<<nc, kVecThreads, 0, st>>>(d, rz1, rr);
             const double target = srv->cfg.rtol * r->bnorm;
             c.tol2 = 0.25 * target * target;
         }
-        g_launches += 2;
         srv->h_ctl[slot] = c;
-        AMIE_CUDA(cudaMemcpyAsync(srv->d_ctl.p + slot, srv->h_ctl + slot, sizeof(SlotCtl), cudaMemcpyHostToDevice, st));
+        AMIE_CUDA(cudaMemcpyAsync(srv->d_ctl.p + slot, srv->h_ctl + slot, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
         AMIE_CUDA(cudaMemcpyAsync(srv->d_slots.p + slot, srv->h_slots + slot, sizeof(SlotDesc), cudaMemcpyHostToDevice, st));
+        if (srv->mixed) {
+            k_scale_to_f32<<<nc, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / r->rnorm, t->r32.p, t->d32.p);
+            k_pcg_start<float><<<nc, kVecThreads, 0, st>>>(d.v32, t->n, d.parts, d.ctl);
+        } else {
+            k_pcg_start<double><<<nc, kVecThreads, 0, st>>>(d.v64, t->n, d.parts, d.ctl);
+        }
+        g_launches += srv->mixed ? 2 : 1;
+        AMIE_CUDA(cudaStreamSynchronize(st));
+        return AMIE_OK;
+    }
+
+    // Continue a mixed slot's inner run from its replaced residual with the
+    // search direction kept (reliable update); `ratio` = new / old residual norm.
+    static amie_status resume_inner(amie_server *srv, int slot, amie_server::Req *r, double ratio)
+    {
+        cudaStream_t st = srv->ctx->stream;
+        amie_topo *t = r->topo;
+        const SlotDesc &d = srv->h_slots[slot];
+        const int nc = d.c1 - d.c0;
+        const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
+        const double need = 0.3 * srv->cfg.rtol * r->bnorm / r->rnorm;
+        const double inner = std::min(0.5, std::max(kInnerReduction, need));
+        k_scale_to_f32<<<nc, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / r->rnorm, t->r32.p, t->d32.p);
+        k_pcg_resume<float><<<nc, kVecThreads, 0, st>>>(d.v32, t->n, d.parts, d.ctl, ratio, inner * inner,
+                                                        std::max<int64_t>(1, maxit - r->iterations));
+        g_launches += 2;
+        srv->h_ctl[slot].done = 0;   // the device block now says so too; refreshed after the next batch
         AMIE_CUDA(cudaStreamSynchronize(st));
         return AMIE_OK;
     }
@@ -472,17 +416,18 @@ struct ServerOps {
         return AMIE_OK;
     }
 
-    // A slot's inner run is finished: FP64 refinement step / true residual, then retire or restart.
+    // A slot's inner run is finished: FP64 residual replacement, then retire, resume or restart.
     static amie_status advance(amie_server *srv, int slot)
     {
         amie_server::Req *r = srv->slot_req[slot];
         amie_topo *t = r->topo;
         cudaStream_t st = srv->ctx->stream;
         SolverState *s = state_of(t);
-        const SlotCtl &c = srv->h_ctl[slot];
+        const PcgCtl &c = srv->h_ctl[slot];
         r->iterations += c.iterations;
+        const double scale = r->rnorm;
         if (srv->mixed) {
-            k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, r->rnorm, t->x.p);
+            k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, scale, t->x.p);
             AMIE_LAUNCHED();
             r->refinements++;
         }
@@ -493,31 +438,34 @@ struct ServerOps {
         const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
         if (!(rr == rr)) return retire(srv, r, AMIE_NAN);
         if (r->rnorm <= srv->cfg.rtol * r->bnorm) return retire(srv, r, AMIE_OK);
-        if (r->iterations >= maxit || r->refinements > 100) return retire(srv, r, AMIE_NOT_CONVERGED);
+        if (r->iterations >= maxit || r->refinements > 200) return retire(srv, r, AMIE_NOT_CONVERGED);
+        // keep the direction while replacements show progress (see solve_pcg)
+        if (srv->mixed && r->rnorm <= 0.5 * scale) return resume_inner(srv, slot, r, r->rnorm / scale);
         return start_inner(srv, slot, r);
     }
 
     static amie_status capture(amie_server *srv)
     {
         cudaStream_t st = srv->ctx->stream;
-        double *pq = srv->d_parts.p, *rz0 = pq + srv->grid, *rz1 = pq + 2 * srv->grid, *rr = pq + 3 * srv->grid;
-        cudaGraph_t g;
+        const SlotDesc *sl = srv->d_slots.p;
+        const int16_t *cs = srv->d_cta_slot.p;
+        const int g = srv->grid;
+        cudaGraph_t graph;
         AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < kBatchIters; it++) {
-            const int parity = it & 1;
+            const bool pdl = it > 0;   // the first kernel follows the host's updates in plain stream order
             if (srv->mixed) {
-                kb_spmv_pq<float, 8><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, pq);
-                kb_update<float><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, pq, rz0, rz1, rr, parity);
-                kb_direction<float><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, rz0, rz1, rr, parity);
+                launch_k(pdl, kb_sell_dir<float>, g, 0, st, sl, cs);
+                launch_k(true, kb_update<float>, g, 0, st, sl, cs);
             } else {
-                kb_spmv_pq<double, 8><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, pq);
-                kb_update<double><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, pq, rz0, rz1, rr, parity);
-                kb_direction<double><<<srv->grid, kVecThreads, 0, st>>>(srv->d_slots.p, srv->d_cta_slot.p, srv->d_ctl.p, rz0, rz1, rr, parity);
+                launch_k(pdl, kb_sell_pq<double>, g, 0, st, sl, cs);
+                launch_k(true, kb_update<double>, g, 0, st, sl, cs);
+                launch_k(true, kb_direction<double>, g, 0, st, sl, cs);
             }
         }
-        AMIE_CUDA(cudaStreamEndCapture(st, &g));
-        cudaError_t e = cudaGraphInstantiate(&srv->graph, g, 0);
-        cudaGraphDestroy(g);
+        AMIE_CUDA(cudaStreamEndCapture(st, &graph));
+        cudaError_t e = cudaGraphInstantiate(&srv->graph, graph, 0);
+        cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
             set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
             return AMIE_CUDA_ERROR;
@@ -541,8 +489,8 @@ struct ServerOps {
             const bool active = any_active(srv);
             if (active) {
                 cudaGraphLaunch(srv->graph, srv->ctx->stream);
-                g_launches += 3 * kBatchIters;
-                cudaMemcpyAsync(srv->h_ctl, srv->d_ctl.p, srv->slot_req.size() * sizeof(SlotCtl), cudaMemcpyDeviceToHost,
+                g_launches += (srv->mixed ? 2 : 3) * kBatchIters;
+                cudaMemcpyAsync(srv->h_ctl, srv->d_ctl.p, srv->slot_req.size() * sizeof(PcgCtl), cudaMemcpyDeviceToHost,
                                 srv->ctx->stream);
                 cudaEventRecord(srv->ctx->ev1, srv->ctx->stream);
             }
@@ -667,15 +615,15 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
         (rc = srv->d_cta_slot.alloc(ctx, srv->grid)) || (rc = srv->d_parts.alloc(ctx, 4 * (size_t)srv->grid)))
         return fail(rc);
     if (cudaMallocHost((void **)&srv->h_slots, c.max_slots * sizeof(SlotDesc)) != cudaSuccess ||
-        cudaMallocHost((void **)&srv->h_ctl, c.max_slots * sizeof(SlotCtl)) != cudaSuccess ||
+        cudaMallocHost((void **)&srv->h_ctl, c.max_slots * sizeof(PcgCtl)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_cta_slot, srv->grid * sizeof(int16_t)) != cudaSuccess)
         return fail(AMIE_OOM);
     std::memset(srv->h_slots, 0, c.max_slots * sizeof(SlotDesc));
-    std::memset(srv->h_ctl, 0, c.max_slots * sizeof(SlotCtl));
+    std::memset(srv->h_ctl, 0, c.max_slots * sizeof(PcgCtl));
     for (int i = 0; i < srv->grid; i++) srv->h_cta_slot[i] = -1;
     cudaStream_t st = ctx->stream;
     cudaMemcpyAsync(srv->d_slots.p, srv->h_slots, c.max_slots * sizeof(SlotDesc), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(srv->d_ctl.p, srv->h_ctl, c.max_slots * sizeof(SlotCtl), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(srv->d_ctl.p, srv->h_ctl, c.max_slots * sizeof(PcgCtl), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(srv->d_cta_slot.p, srv->h_cta_slot, srv->grid * sizeof(int16_t), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(srv->d_parts.p, 0, 4 * (size_t)srv->grid * 8, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return fail(AMIE_CUDA_ERROR);

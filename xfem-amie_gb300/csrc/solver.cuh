@@ -174,14 +174,23 @@ __device__ __forceinline__ double sum_parts(const double *parts, int n, double *
     return r;
 }
 
-// Every CTA calls this after thread 0 stored the CTA's partials; returns true
-// in the last CTA to finish (all partials of the kernel are then visible).
-__device__ __forceinline__ bool last_cta(uint32_t *ticket, int *sh_flag)
+// Position of a CTA in the group of CTAs that share one reduction and one
+// control block: the whole grid for a single solve, one slot's CTA range in a
+// batched launch (the kernel bodies below take it explicitly).
+struct Cta {
+    uint32_t id, n;
+};
+__device__ __forceinline__ Cta grid_cta() { return Cta{blockIdx.x, gridDim.x}; }
+
+// Every CTA of a group of `n` calls this after thread 0 stored the CTA's
+// partials; returns true in the last CTA to finish (all partials of the group
+// are then visible).
+__device__ __forceinline__ bool last_cta(uint32_t *ticket, int *sh_flag, uint32_t n)
 {
     if (threadIdx.x == 0) {
         __threadfence();
         const uint32_t t = atomicAdd(ticket, 1u);
-        *sh_flag = (t == gridDim.x - 1) ? 1 : 0;
+        *sh_flag = (t == n - 1) ? 1 : 0;
     }
     __syncthreads();
     const bool last = *sh_flag != 0;
@@ -270,13 +279,13 @@ __device__ __forceinline__ void row_spmv(const BsrView<T> &A, const T *__restric
 
 // Per-CTA partial of p.q; with `fin`, the last CTA stores pq and alpha = rz / pq.
 template <typename T>
-__device__ __forceinline__ void finish_pq(T dot_t, double *part_pq, PcgCtl *fin, double *sh, int *flag)
+__device__ __forceinline__ void finish_pq(T dot_t, double *part_pq, PcgCtl *fin, double *sh, int *flag, Cta c)
 {
     const double dot = block_sum_v<T>(dot_t, sh);
-    if (threadIdx.x == 0) part_pq[blockIdx.x] = dot;
+    if (threadIdx.x == 0) part_pq[c.id] = dot;
     if (!fin) return;
-    if (!last_cta(&fin->ticket, flag)) return;
-    const double pq = ordered_sum(part_pq, gridDim.x, sh);
+    if (!last_cta(&fin->ticket, flag, c.n)) return;
+    const double pq = ordered_sum(part_pq, c.n, sh);
     if (threadIdx.x == 0) {
         fin->pq = pq;
         fin->alpha = pq != 0.0 ? fin->rz / pq : 0.0;
@@ -319,7 +328,7 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv_pq(PcgVecs<T> v, double *p
         b = nb;
         e = ne;
     }
-    finish_pq<T>(dot, part_pq, fin, sh, &flag);
+    finish_pq<T>(dot, part_pq, fin, sh, &flag, grid_cta());
 }
 
 // One s x s block of the lane's row from a 32-slot SELL group (chunked layout).
@@ -369,22 +378,16 @@ __device__ __forceinline__ void load_sell_group(const SellView<T> &A, uint64_t g
 // block-CSR row with the same FMA sequence as row_spmv with one lane per row,
 // so q is bitwise that of k_spmv_pq<S,1,T>.
 // MINB (2x2 FP32 blocks only) asks the compiler for MINB resident CTAs per SM.
-template <int S, int U, bool PIPE, int MINB, typename T>
-__global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB : 1)
-    k_sell_pq(SellView<T> A, const T *__restrict__ x, T *__restrict__ y, double *part_pq, const int32_t *done,
-              PcgCtl *fin)
+template <int S, int U, bool PIPE, typename T>
+__device__ __forceinline__ void sell_pq_body(const SellView<T> &A, const T *__restrict__ x, T *__restrict__ y,
+                                             double *part_pq, PcgCtl *fin, double *sh, int *flag, uint32_t *next_sl,
+                                             Cta cta)
 {
-    __shared__ double sh[33];
-    __shared__ int flag;
-    __shared__ uint32_t next_sl;
-    pdl_wait();
-    pdl_release();
-    if (done && *done) return;
     constexpr uint32_t WPB = kVecThreads / 32;
     const uint32_t lane = threadIdx.x & 31;
     // the CTA's contiguous, slot-balanced range of slices; its warps take slices in turn
-    const uint32_t s_beg = __ldg(A.cta_first + blockIdx.x), s_end = __ldg(A.cta_first + blockIdx.x + 1);
-    if (threadIdx.x == 0) next_sl = s_beg + WPB;
+    const uint32_t s_beg = __ldg(A.cta_first + cta.id), s_end = __ldg(A.cta_first + cta.id + 1);
+    if (threadIdx.x == 0) *next_sl = s_beg + WPB;
     __syncthreads();
     for (uint32_t sl = s_beg + (threadIdx.x >> 5); sl < s_end;) {
         const uint32_t row = __ldg(A.perm + (uint64_t)sl * 32 + lane);
@@ -437,13 +440,27 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
         for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
         if (lane == 0) A.slice_dot[sl] = dot;
         uint32_t nx = 0;
-        if (lane == 0) nx = atomicAdd(&next_sl, 1u);
+        if (lane == 0) nx = atomicAdd(next_sl, 1u);
         sl = __shfl_sync(0xffffffffu, nx, 0);
     }
     __syncthreads();   // the CTA's slice partials are visible to all its threads
     T dot = T(0);
     for (uint32_t i = s_beg + threadIdx.x; i < s_end; i += kVecThreads) dot += A.slice_dot[i];
-    finish_pq<T>(dot, part_pq, fin, sh, &flag);
+    finish_pq<T>(dot, part_pq, fin, sh, flag, cta);
+}
+
+template <int S, int U, bool PIPE, int MINB, typename T>
+__global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB : 1)
+    k_sell_pq(SellView<T> A, const T *__restrict__ x, T *__restrict__ y, double *part_pq, const int32_t *done,
+              PcgCtl *fin)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    __shared__ uint32_t next_sl;
+    pdl_wait();
+    pdl_release();
+    if (done && *done) return;
+    sell_pq_body<S, U, PIPE, T>(A, x, y, part_pq, fin, sh, &flag, &next_sl, grid_cta());
 }
 
 // Kernel A with the direction update folded in (used with two direction
@@ -525,8 +542,86 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
     __syncthreads();
     T dot = T(0);
     for (uint32_t i = s_beg + threadIdx.x; i < s_end; i += kVecThreads) dot += A.slice_dot[i];
-    finish_pq<T>(dot, part_pq, fin ? ctl : nullptr, sh, &flag);
+    finish_pq<T>(dot, part_pq, fin ? ctl : nullptr, sh, &flag, grid_cta());
 }
+
+// k_sell_dir for a group of CTAs given explicitly (one slot's CTAs in a batched
+// launch).  The single-solve kernel below is kept as its own copy: with the
+// group position and the views held as values the compiler keeps fewer loads in
+// flight at the kernel's 64-register budget (49 us instead of 33 us on cfg1).
+template <int S, typename T>
+__device__ __forceinline__ void sell_dir_body(const SellView<T> &A, const PcgVecs<T> &v, double *part_pq, PcgCtl *ctl,
+                                              bool fin, Cta cta)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    __shared__ uint32_t next_sl;
+    constexpr int U = kSpmvUnroll;
+    constexpr uint32_t WPB = kVecThreads / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    const T bt = (T)ctl->beta;
+    const bool second = ctl->pcur != 0;
+    const T *__restrict__ pold = second ? v.p2 : v.p;
+    T *__restrict__ pnew = second ? v.p : v.p2;
+    const T *__restrict__ z = v.z;
+    T *__restrict__ q = v.q;
+    const uint32_t s_beg = __ldg(A.cta_first + cta.id), s_end = __ldg(A.cta_first + cta.id + 1);
+    if (threadIdx.x == 0) next_sl = s_beg + WPB;
+    __syncthreads();
+    for (uint32_t sl = s_beg + (threadIdx.x >> 5); sl < s_end;) {
+        const uint32_t row = __ldg(A.perm + (uint64_t)sl * 32 + lane);
+        const uint64_t g0 = __ldg(A.slice_ptr + sl);
+        const uint32_t len = (uint32_t)((__ldg(A.slice_ptr + sl + 1) - g0) >> 5);
+        T acc[S];
+#pragma unroll
+        for (int r = 0; r < S; r++) acc[r] = T(0);
+        uint32_t c[U];
+        T blk[U][S * S];
+        for (uint32_t j0 = 0; j0 < len; j0 += U) {
+            load_sell_group<S, U, T>(A, g0, j0, len, lane, c, blk);
+            T zv[U][S], pv[U][S];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+                    load_x<S, T>(z, c[u], zv[u]);
+                    load_x<S, T>(pold, c[u], pv[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+#pragma unroll
+                    for (int r = 0; r < S; r++)
+#pragma unroll
+                        for (int cc = 0; cc < S; cc++)
+                            acc[r] = fma(blk[u][r * S + cc], fma(bt, pv[u][cc], zv[u][cc]), acc[r]);
+                }
+            }
+        }
+        T dot = T(0);
+        if (row < A.n_rows) {
+#pragma unroll
+            for (int r = 0; r < S; r++) {
+                const uint64_t i = (uint64_t)row * S + r;
+                const T pn = fma(bt, pold[i], z[i]);
+                pnew[i] = pn;
+                q[i] = acc[r];
+                dot = fma(acc[r], pn, dot);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        if (lane == 0) A.slice_dot[sl] = dot;
+        uint32_t nx = 0;
+        if (lane == 0) nx = atomicAdd(&next_sl, 1u);
+        sl = __shfl_sync(0xffffffffu, nx, 0);
+    }
+    __syncthreads();
+    T dot = T(0);
+    for (uint32_t i = s_beg + threadIdx.x; i < s_end; i += kVecThreads) dot += A.slice_dot[i];
+    finish_pq<T>(dot, part_pq, fin ? ctl : nullptr, sh, &flag, cta);
+}
+
 
 // Asynchronous 16-byte global -> shared copies (completion tracked per thread
 // in commit groups; cp.async.wait_group is a hardware wait on those copies).
@@ -683,7 +778,7 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_pq_cp(SellView<T> A, const
         }
     }
     cp_async_wait<0>();
-    finish_pq<T>(dot, part_pq, fin, sh, &flag);
+    finish_pq<T>(dot, part_pq, fin, sh, &flag, grid_cta());
 }
 
 // Plain y = A x (+ optional y = b - A x with partial of y.y).
@@ -757,11 +852,11 @@ __device__ __forceinline__ void st_pack(T *p, uint64_t i, const T (&o)[Pack<T>::
 // Pack<T>::n entries (fpack(k) for pack k) when every vector is 16-byte
 // aligned, single entries otherwise and for the tail.
 template <typename T, typename FP, typename FS>
-__device__ __forceinline__ void for_entries(uint64_t n, bool aligned, FP &&fpack, FS &&fone)
+__device__ __forceinline__ void for_entries(uint64_t n, bool aligned, Cta cta, FP &&fpack, FS &&fone)
 {
     constexpr int W = Pack<T>::n;
-    const uint64_t tid = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x;
-    const uint64_t stride = (uint64_t)gridDim.x * kVecThreads;
+    const uint64_t tid = (uint64_t)cta.id * kVecThreads + threadIdx.x;
+    const uint64_t stride = (uint64_t)cta.n * kVecThreads;
     uint64_t first = 0;
     if (aligned) {
         const uint64_t npk = n / W;
@@ -776,13 +871,9 @@ __device__ __forceinline__ void for_entries(uint64_t n, bool aligned, FP &&fpack
 // thread handles two 16-byte packs per step with all ten loads issued before
 // any arithmetic (one memory round trip per step).
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl)
+__device__ __forceinline__ void update_body(const PcgVecs<T> &v, uint64_t n, const PcgParts &parts, PcgCtl *ctl,
+                                            double *sh, int *flag, Cta cta)
 {
-    __shared__ double sh[2 * (kVecThreads >> 5)];
-    __shared__ int flag;
-    pdl_wait();
-    pdl_release();
-    if (ctl->done) return;
     constexpr int W = Pack<T>::n;
     const T a = (T)ctl->alpha;
     T *__restrict__ x = v.x;
@@ -794,8 +885,8 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     const T *__restrict__ d = v.dinv;
     T drz = T(0), drr = T(0);   // per-thread partials in the vector precision, CTA sums in FP64
     const bool al = aligned16(x) && aligned16(r) && aligned16(z) && aligned16(p) && aligned16(q) && aligned16(d);
-    const uint64_t tid = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x;
-    const uint64_t stride = (uint64_t)gridDim.x * kVecThreads;
+    const uint64_t tid = (uint64_t)cta.id * kVecThreads + threadIdx.x;
+    const uint64_t stride = (uint64_t)cta.n * kVecThreads;
     const uint64_t npk = al ? n / W : 0;
     for (uint64_t k = tid; k < npk; k += 2 * stride) {
         const uint64_t k2 = k + stride;
@@ -843,12 +934,12 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     double brz, brr;
     block_sum2_v<T>(drz, drr, sh, brz, brr);
     if (threadIdx.x == 0) {
-        parts.rz[blockIdx.x] = brz;
-        parts.rr[blockIdx.x] = brr;
+        parts.rz[cta.id] = brz;
+        parts.rr[cta.id] = brr;
     }
-    if (!last_cta(&ctl->ticket, &flag)) return;
+    if (!last_cta(&ctl->ticket, flag, cta.n)) return;
     double rz_new, rr;
-    ordered_sum2(parts.rz, parts.rr, gridDim.x, sh, rz_new, rr);
+    ordered_sum2(parts.rz, parts.rr, cta.n, sh, rz_new, rr);
     if (threadIdx.x == 0) {
         const int64_t it = ctl->iterations + 1;
         ctl->iterations = it;
@@ -866,19 +957,27 @@ __global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n
     }
 }
 
-// Kernel C: p = z + beta p, two packs per thread per step.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_t n, const PcgCtl *ctl)
+__global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl)
 {
+    __shared__ double sh[2 * (kVecThreads >> 5)];
+    __shared__ int flag;
     pdl_wait();
     pdl_release();
     if (ctl->done) return;
+    update_body<T>(v, n, parts, ctl, sh, &flag, grid_cta());
+}
+
+// Kernel C: p = z + beta p, two packs per thread per step.
+template <typename T>
+__device__ __forceinline__ void direction_body(const PcgVecs<T> &v, uint64_t n, const PcgCtl *ctl, Cta cta)
+{
     constexpr int W = Pack<T>::n;
     const T bt = (T)ctl->beta;
     T *__restrict__ p = v.p;
     const T *__restrict__ z = v.z;
-    const uint64_t tid = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x;
-    const uint64_t stride = (uint64_t)gridDim.x * kVecThreads;
+    const uint64_t tid = (uint64_t)cta.id * kVecThreads + threadIdx.x;
+    const uint64_t stride = (uint64_t)cta.n * kVecThreads;
     const uint64_t npk = aligned16(p) && aligned16(z) ? n / W : 0;
     for (uint64_t k = tid; k < npk; k += 2 * stride) {
         const uint64_t k2 = k + stride;
@@ -902,10 +1001,19 @@ __global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_
     for (uint64_t i = npk * W + tid; i < n; i += stride) p[i] = fma(bt, p[i], z[i]);
 }
 
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_direction(PcgVecs<T> v, uint64_t n, const PcgCtl *ctl)
+{
+    pdl_wait();
+    pdl_release();
+    if (ctl->done) return;
+    direction_body<T>(v, n, ctl, grid_cta());
+}
+
 // z = D^-1 r (and p = z when `set_p`); partials r.z, r.r.  Shared by the start
 // and the resume of a run.
 template <typename T, bool SET_P>
-__device__ __forceinline__ void precond_parts(const PcgVecs<T> &v, uint64_t n, T &drz, T &drr)
+__device__ __forceinline__ void precond_parts(const PcgVecs<T> &v, uint64_t n, Cta cta, T &drz, T &drr)
 {
     constexpr int W = Pack<T>::n;
     const T *__restrict__ r = v.r;
@@ -913,7 +1021,7 @@ __device__ __forceinline__ void precond_parts(const PcgVecs<T> &v, uint64_t n, T
     T *__restrict__ z = v.z;
     T *__restrict__ p = v.p;
     for_entries<T>(
-        n, aligned16(r) && aligned16(d) && aligned16(z) && aligned16(p),
+        n, aligned16(r) && aligned16(d) && aligned16(z) && aligned16(p), cta,
         [&](uint64_t k) {
             T rv[W], dv[W], zv[W];
             ldg_pack<T>(r, k, rv);
@@ -940,26 +1048,33 @@ __device__ __forceinline__ void precond_parts(const PcgVecs<T> &v, uint64_t n, T
 // Start of a PCG run from the residual r (already holding b - A x):
 // z = D^-1 r, p = z; last CTA: rz and rr into the control block.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_pcg_start(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl)
+__device__ __forceinline__ void start_body(const PcgVecs<T> &v, uint64_t n, const PcgParts &parts, PcgCtl *ctl,
+                                           double *sh, int *flag, Cta cta)
 {
-    __shared__ double sh[33];
-    __shared__ int flag;
     T drz = T(0), drr = T(0);
-    precond_parts<T, true>(v, n, drz, drr);
+    precond_parts<T, true>(v, n, cta, drz, drr);
     double brz, brr;
     block_sum2_v<T>(drz, drr, sh, brz, brr);
     if (threadIdx.x == 0) {
-        parts.rz[blockIdx.x] = brz;
-        parts.rr[blockIdx.x] = brr;
+        parts.rz[cta.id] = brz;
+        parts.rr[cta.id] = brr;
     }
-    if (!last_cta(&ctl->ticket, &flag)) return;
+    if (!last_cta(&ctl->ticket, flag, cta.n)) return;
     double rz, rr;
-    ordered_sum2(parts.rz, parts.rr, gridDim.x, sh, rz, rr);
+    ordered_sum2(parts.rz, parts.rr, cta.n, sh, rz, rr);
     if (threadIdx.x == 0) {
         ctl->rz = rz;
         ctl->rr = rr;
         ctl->ticket = 0;
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_pcg_start(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    start_body<T>(v, n, parts, ctl, sh, &flag, grid_cta());
 }
 
 // Resume of a stopped PCG run after its residual r was replaced by the true
@@ -968,22 +1083,20 @@ __global__ void __launch_bounds__(kVecThreads) k_pcg_start(PcgVecs<T> v, uint64_
 // so that the following k_direction keeps the previous search direction
 // (a reliable update), fresh tol2 / maxit, iterations and done cleared.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_pcg_resume(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl,
-                                                            double ratio, double tol2, int64_t maxit)
+__device__ __forceinline__ void resume_body(const PcgVecs<T> &v, uint64_t n, const PcgParts &parts, PcgCtl *ctl,
+                                            double ratio, double tol2, int64_t maxit, double *sh, int *flag, Cta cta)
 {
-    __shared__ double sh[33];
-    __shared__ int flag;
     T drz = T(0), drr = T(0);
-    precond_parts<T, false>(v, n, drz, drr);
+    precond_parts<T, false>(v, n, cta, drz, drr);
     double brz, brr;
     block_sum2_v<T>(drz, drr, sh, brz, brr);
     if (threadIdx.x == 0) {
-        parts.rz[blockIdx.x] = brz;
-        parts.rr[blockIdx.x] = brr;
+        parts.rz[cta.id] = brz;
+        parts.rr[cta.id] = brr;
     }
-    if (!last_cta(&ctl->ticket, &flag)) return;
+    if (!last_cta(&ctl->ticket, flag, cta.n)) return;
     double rz, rr;
-    ordered_sum2(parts.rz, parts.rr, gridDim.x, sh, rz, rr);
+    ordered_sum2(parts.rz, parts.rr, cta.n, sh, rz, rr);
     if (threadIdx.x == 0) {
         ctl->beta = ctl->rz_prev != 0.0 ? ratio * rz / ctl->rz_prev : 0.0;
         ctl->rz = rz;
@@ -994,6 +1107,15 @@ __global__ void __launch_bounds__(kVecThreads) k_pcg_resume(PcgVecs<T> v, uint64
         ctl->done = 0;
         ctl->ticket = 0;
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) k_pcg_resume(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl,
+                                                            double ratio, double tol2, int64_t maxit)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    resume_body<T>(v, n, parts, ctl, ratio, tol2, maxit, sh, &flag, grid_cta());
 }
 
 }  // namespace amie
