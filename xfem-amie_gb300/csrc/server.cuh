@@ -24,6 +24,7 @@
 namespace amie {
 
 constexpr int kBatchIters = 16;
+constexpr int kNormParts = 256;   // most CTAs of a slot's residual-norm launch
 
 // Device view of one slot: the slot's SELL copies (CTA table for its own CTA
 // count), vectors, control block and its range of the batch's partial sums.
@@ -172,6 +173,8 @@ struct amie_server {
     amie::DevArray<double> d_parts;              // pq | rz | rr | spare, grid each
     amie::SlotDesc *h_slots = nullptr;           // pinned
     amie::PcgCtl *h_ctl = nullptr;               // pinned
+    double *h_norm = nullptr;                    // pinned: residual partials of finishing slots
+    std::vector<int> h_norm_n;
     int16_t *h_cta_slot = nullptr;               // pinned
     cudaGraphExec_t graph = nullptr;
     std::string error;
@@ -335,7 +338,9 @@ struct ServerOps {
             k_pcg_start<double><<<nc, kVecThreads, 0, st>>>(d.v64, t->n, d.parts, d.ctl);
         }
         g_launches += srv->mixed ? 2 : 1;
-        AMIE_CUDA(cudaStreamSynchronize(st));
+        // no synchronisation: the pinned h_ctl / h_slots entries are next written by
+        // the D2H copy that follows the next batch on the same stream
+        AMIE_CUDA(cudaGetLastError());
         return AMIE_OK;
     }
 
@@ -355,7 +360,7 @@ struct ServerOps {
                                                         std::max<int64_t>(1, maxit - r->iterations));
         g_launches += 2;
         srv->h_ctl[slot].done = 0;   // the device block now says so too; refreshed after the next batch
-        AMIE_CUDA(cudaStreamSynchronize(st));
+        AMIE_CUDA(cudaGetLastError());
         return AMIE_OK;
     }
 
@@ -416,32 +421,49 @@ struct ServerOps {
         return AMIE_OK;
     }
 
-    // A slot's inner run is finished: FP64 residual replacement, then retire, resume or restart.
-    static amie_status advance(amie_server *srv, int slot)
+    // Slots whose inner runs finished in the last batch: FP64 residual
+    // replacement for all of them (launched back to back, one synchronisation),
+    // then retire, resume or restart each.
+    static amie_status advance_all(amie_server *srv, const std::vector<int> &slots)
     {
-        amie_server::Req *r = srv->slot_req[slot];
-        amie_topo *t = r->topo;
         cudaStream_t st = srv->ctx->stream;
-        SolverState *s = state_of(t);
-        const PcgCtl &c = srv->h_ctl[slot];
-        r->iterations += c.iterations;
-        const double scale = r->rnorm;
-        if (srv->mixed) {
-            k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, scale, t->x.p);
-            AMIE_LAUNCHED();
-            r->refinements++;
+        const int cap = kNormParts;
+        for (size_t k = 0; k < slots.size(); k++) {
+            const int slot = slots[k];
+            amie_server::Req *r = srv->slot_req[slot];
+            amie_topo *t = r->topo;
+            SolverState *s = state_of(t);
+            r->iterations += srv->h_ctl[slot].iterations;
+            if (srv->mixed) {
+                k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, r->rnorm, t->x.p);
+                AMIE_LAUNCHED();
+                r->refinements++;
+            }
+            // r = b - A x and its partial norms, on few CTAs (requests are small)
+            const int g = (int)std::min<uint64_t>((uint64_t)cap, std::max<uint64_t>(1, (t->n_rows + 255) / 256));
+            double *part = s->parts.p + 3 * s->stride;
+            launch_spmv<double>(t, g, bsr64(t), t->x.p, t->rhs.p, t->r.p, part, st);
+            AMIE_CUDA(cudaMemcpyAsync(srv->h_norm + (size_t)k * cap, part, g * sizeof(double), cudaMemcpyDeviceToHost, st));
+            srv->h_norm_n[k] = g;
         }
-        double rr = 0.0;
-        launch_spmv<double>(t, s->grid, bsr64(t), t->x.p, t->rhs.p, t->r.p, s->parts.p + 3 * s->stride, st);
-        AMIE_TRY(read_sum_on(st, s->parts.p + 3 * s->stride, s->grid, &rr));
-        r->rnorm = std::sqrt(rr);
-        const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
-        if (!(rr == rr)) return retire(srv, r, AMIE_NAN);
-        if (r->rnorm <= srv->cfg.rtol * r->bnorm) return retire(srv, r, AMIE_OK);
-        if (r->iterations >= maxit || r->refinements > 200) return retire(srv, r, AMIE_NOT_CONVERGED);
-        // keep the direction while replacements show progress (see solve_pcg)
-        if (srv->mixed && r->rnorm <= 0.5 * scale) return resume_inner(srv, slot, r, r->rnorm / scale);
-        return start_inner(srv, slot, r);
+        AMIE_CUDA(cudaStreamSynchronize(st));
+        for (size_t k = 0; k < slots.size(); k++) {
+            const int slot = slots[k];
+            amie_server::Req *r = srv->slot_req[slot];
+            amie_topo *t = r->topo;
+            double rr = 0.0;
+            for (int i = 0; i < srv->h_norm_n[k]; i++) rr += srv->h_norm[(size_t)k * cap + i];
+            const double scale = r->rnorm;
+            r->rnorm = std::sqrt(rr);
+            const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
+            if (!(rr == rr)) AMIE_TRY(retire(srv, r, AMIE_NAN));
+            else if (r->rnorm <= srv->cfg.rtol * r->bnorm) AMIE_TRY(retire(srv, r, AMIE_OK));
+            else if (r->iterations >= maxit || r->refinements > 200) AMIE_TRY(retire(srv, r, AMIE_NOT_CONVERGED));
+            // keep the direction while replacements show progress (see solve_pcg)
+            else if (srv->mixed && r->rnorm <= 0.5 * scale) AMIE_TRY(resume_inner(srv, slot, r, r->rnorm / scale));
+            else AMIE_TRY(start_inner(srv, slot, r));
+        }
+        return AMIE_OK;
     }
 
     static amie_status capture(amie_server *srv)
@@ -544,12 +566,14 @@ struct ServerOps {
             // 3. batch results
             if (active) {
                 cudaEventSynchronize(srv->ctx->ev1);
+                std::vector<int> finished;
                 for (size_t i = 0; i < srv->slot_req.size(); i++) {
                     amie_server::Req *r = srv->slot_req[i];
                     if (!r) continue;
                     if (r->cancelled) { retire(srv, r, AMIE_CANCELLED); continue; }
-                    if (srv->h_ctl[i].done) advance(srv, (int)i);
+                    if (srv->h_ctl[i].done) finished.push_back((int)i);
                 }
+                if (!finished.empty()) advance_all(srv, finished);
             }
             // 4. join admitted requests
             std::vector<amie_server::Req *> waiting;
@@ -611,11 +635,13 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
         return s;
     };
     srv->slot_req.assign(c.max_slots, nullptr);
+    srv->h_norm_n.assign(c.max_slots, 0);
     if ((rc = srv->d_slots.alloc(ctx, c.max_slots)) || (rc = srv->d_ctl.alloc(ctx, c.max_slots)) ||
         (rc = srv->d_cta_slot.alloc(ctx, srv->grid)) || (rc = srv->d_parts.alloc(ctx, 4 * (size_t)srv->grid)))
         return fail(rc);
     if (cudaMallocHost((void **)&srv->h_slots, c.max_slots * sizeof(SlotDesc)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_ctl, c.max_slots * sizeof(PcgCtl)) != cudaSuccess ||
+        cudaMallocHost((void **)&srv->h_norm, (size_t)c.max_slots * kNormParts * sizeof(double)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_cta_slot, srv->grid * sizeof(int16_t)) != cudaSuccess)
         return fail(AMIE_OOM);
     std::memset(srv->h_slots, 0, c.max_slots * sizeof(SlotDesc));
@@ -772,6 +798,7 @@ extern "C" amie_status amie_server_stop(amie_server *srv)
     if (srv->graph) cudaGraphExecDestroy(srv->graph);
     if (srv->h_slots) cudaFreeHost(srv->h_slots);
     if (srv->h_ctl) cudaFreeHost(srv->h_ctl);
+    if (srv->h_norm) cudaFreeHost(srv->h_norm);
     if (srv->h_cta_slot) cudaFreeHost(srv->h_cta_slot);
     srv->d_slots.release();
     srv->d_ctl.release();
