@@ -156,6 +156,17 @@ AMIE_API amie_status amie_topology_pattern(const amie_topo *topo, uint32_t *row_
  * into the device-resident block matrix.  Clears any previous Dirichlet
  * elimination and right-hand side. */
 AMIE_API amie_status amie_assemble(amie_topo *topo);
+/* Imposed strain per element (Voigt, [n_elem * nv]; NULL removes it).  Every
+ * assembly then adds its induced forces sum_g w_g B_f^T (C eps0) per element
+ * function to the right-hand side before the Dirichlet elimination
+ * (StiffnessWithImposedStrain::getBoundaryConditions,
+ * physics/stiffness_with_imposed_deformation.cpp:83-110, through
+ * DofDefinedBoundaryCondition SET_VOLUMIC_STRESS_*, features/boundarycondition.cpp:542-617,
+ * and Assembly::addForceOn, solvers/assembly.cpp:1477), and the recovered
+ * stress is C (eps - eps0) (REAL_STRESS_FIELD).  C is the undamaged material
+ * matrix in the forces, as in the reference.  Re-assembles an assembled topology. */
+AMIE_API amie_status amie_set_imposed_strain(amie_topo *topo, const double *eps0);
+
 /* Re-integrate with new per-element factors on C (damage step:
  * StiffnessAndFracture::apply, physics/stiffness_and_fracture.cpp:75-79). */
 AMIE_API amie_status amie_set_cscale(amie_topo *topo, const double *cscale);
@@ -260,6 +271,15 @@ AMIE_API amie_status amie_server_stop(amie_server *srv);
  * (FeatureTree::strainFromDisplacements / stressFromDisplacements,
  * features/features.cpp:4223, 3424).  strain, stress: [n_elem * nv] host arrays or NULL. */
 AMIE_API amie_status amie_element_fields(amie_topo *topo, double *strain, double *stress);
+
+/* Field averaged over the mesh: sum_e v_e f_e / sum_e v_e with f_e the element's
+ * Gauss-point average (as amie_element_fields) and v_e its area (2D: the
+ * triangle of its corners, from J^-1 at the centroid) or volume (3D), Kahan
+ * sums; FeatureTree::getAverageField (features/features.cpp:6711) through
+ * Mesh::getField (mesher/mesh.h:919-960) and ElementState::getAverageField
+ * (elements/integrable_entity.cpp:1992).  avg: [nv]; measure (nullable): sum v_e. */
+enum { AMIE_FIELD_STRAIN = 0, AMIE_FIELD_STRESS = 1 };
+AMIE_API amie_status amie_average_field(amie_topo *topo, int32_t field, double *avg, double *measure);
 
 /* One explicit scalar-damage update from the current solution
  * (StiffnessAndFracture::step, physics/stiffness_and_fracture.cpp:81-90): Mazars

@@ -306,6 +306,82 @@ extern "C" int oracle_element_fields(const oracle_mesh *m, const double *u, doub
     return 0;
 }
 
+// Induced forces of an imposed strain eps0 (per element, Voigt): for every
+// function f of every element, f_f += sum_g w_g B_f(g)^T (C eps0), added into
+// the global force vector in element order -- the SET_VOLUMIC_STRESS_* forces
+// StiffnessWithImposedStrain::getBoundaryConditions
+// (physics/stiffness_with_imposed_deformation.cpp:83-110) hands to
+// DofDefinedBoundaryCondition (features/boundarycondition.cpp:542-617), which
+// Assembly::addForceOn (solvers/assembly.cpp:1477-1530) accumulates per DOF.
+// C is the element's undamaged material matrix, as in the reference.
+extern "C" int oracle_induced_forces(const oracle_mesh *m, const double *imposed, double *force)
+{
+    const int dim = m->dim;
+    const int nv = dim == 2 ? 3 : 6;
+    for (int64_t e = 0; e < (int64_t)m->n_elem; e++) {
+        const double *C = m->cmat_table + (size_t)m->mat[e] * nv * nv;
+        double sig[6] = {0, 0, 0, 0, 0, 0};
+        for (int r = 0; r < nv; r++)
+            for (int c = 0; c < nv; c++) sig[r] += C[r * nv + c] * imposed[(size_t)e * nv + c];
+        const int kind = m->kind[e];
+        const int nshape = shape_count(kind);
+        const uint32_t e0 = m->enr_ptr ? m->enr_ptr[e] : 0, e1 = m->enr_ptr ? m->enr_ptr[e + 1] : 0;
+        const int nf = nshape + (int)(e1 - e0);
+        const double *Je = m->jinv + (size_t)e * dim * dim;
+        const uint32_t g0 = m->gp_ptr[e], g1 = m->gp_ptr[e + 1];
+        std::vector<double> pts, wts;
+        if (g1 > g0) {
+            for (uint32_t g = g0; g < g1; g++) {
+                for (int c = 0; c < dim; c++) pts.push_back(m->gp[(size_t)g * (dim + 1) + c]);
+                wts.push_back(m->gp[(size_t)g * (dim + 1) + dim]);
+            }
+        } else {
+            Rule r = default_rule(kind);
+            for (int g = 0; g < r.n; g++) {
+                for (int c = 0; c < dim; c++) pts.push_back(r.p[g][c]);
+                wts.push_back(r.w[g] / det(dim, Je));
+            }
+        }
+        const bool moved = m->moved && m->moved[e] && g1 > g0;
+        for (int f = 0; f < nf; f++) {
+            double acc[3] = {0, 0, 0};
+            for (size_t g = 0; g < wts.size(); g++) {
+                double sg[6][3];
+                shape_grad(kind, &pts[g * dim], sg);
+                const double *J = moved ? m->jinv_gp + (size_t)(g0 + g) * dim * dim : Je;
+                double lg[3] = {0, 0, 0};
+                if (f < nshape) {
+                    for (int c = 0; c < dim; c++) lg[c] = sg[f][c];
+                } else {
+                    const uint32_t fj = e0 + (f - nshape);
+                    const size_t off = (size_t)m->enr_data[fj] + g;
+                    if (m->enr_type[fj] == ORACLE_ENR_HEAVISIDE) {
+                        lg[0] = P1_GRAD[m->enr_vertex[fj]][0] * m->enr_jump[off];
+                        lg[1] = P1_GRAD[m->enr_vertex[fj]][1] * m->enr_jump[off];
+                    } else {
+                        for (int c = 0; c < dim; c++) lg[c] = m->enr_grad[off * dim + c];
+                    }
+                }
+                double d[3] = {0, 0, 0};
+                for (int r = 0; r < dim; r++)
+                    for (int c = 0; c < dim; c++) d[r] += lg[c] * J[r * dim + c];
+                const double w = wts[g];
+                if (dim == 2) {
+                    acc[0] += w * (d[0] * sig[0] + d[1] * sig[2]);
+                    acc[1] += w * (d[1] * sig[1] + d[0] * sig[2]);
+                } else {
+                    acc[0] += w * (d[0] * sig[0] + d[2] * sig[4] + d[1] * sig[5]);
+                    acc[1] += w * (d[1] * sig[1] + d[2] * sig[3] + d[0] * sig[5]);
+                    acc[2] += w * (d[2] * sig[2] + d[1] * sig[3] + d[0] * sig[4]);
+                }
+            }
+            const size_t id = m->dof_ids[m->dof_ptr[e] + f];
+            for (int c = 0; c < dim; c++) force[id * dim + c] += acc[c];
+        }
+    }
+    return 0;
+}
+
 extern "C" int oracle_pattern(const oracle_mesh *m, uint32_t *n_rows, uint64_t *nnzb, uint32_t *row_size,
                               uint32_t *column_index)
 {

@@ -57,6 +57,7 @@ int oracle_element_matrices(const oracle_mesh *m, const uint64_t *ke_off, double
 
 /* Sparsity pattern of Assembly::make_final (solvers/assembly.cpp:445-537).
  * Call once with row_size == NULL to get n_rows and nnzb, then with buffers. */
+int oracle_induced_forces(const oracle_mesh *m, const double *imposed, double *force);
 int oracle_pattern(const oracle_mesh *m, uint32_t *n_rows, uint64_t *nnzb, uint32_t *row_size,
                    uint32_t *column_index);
 

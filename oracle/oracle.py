@@ -127,6 +127,17 @@ def pcg(stride, rs, ci, arr, b, x0=None, rtol=1e-10, maxit=100000):
     return x, int(it.value), float(rr.value), int(rc)
 
 
+def induced_forces(m, imposed, n):
+    """Global force vector [n] of an imposed strain [n_elem, nv] (element order accumulation)."""
+    f = np.zeros(n, np.float64)
+    st = _mesh_struct(m)
+    imp = np.ascontiguousarray(imposed, np.float64)
+    rc = lib().oracle_induced_forces(C.byref(st), _p(imp), _p(f))
+    if rc != 0:
+        raise RuntimeError(f"oracle_induced_forces failed: {rc}")
+    return f
+
+
 def element_fields(m, u):
     """(strain, stress) per element, Voigt, from displacements u."""
     nv = m.nv

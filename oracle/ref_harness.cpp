@@ -36,6 +36,7 @@
 #include "features/inclusion.h"
 #include "features/crack.h"
 #include "physics/stiffness.h"
+#include "physics/stiffness_with_imposed_deformation.h"
 #include "utilities/placement.h"
 #include "solvers/assembly.h"
 #include "solvers/conjugategradient.h"
@@ -103,7 +104,7 @@ enum { KIND_TRI3 = 1, KIND_TRI6 = 2, KIND_TET4 = 3 };
 
 struct ElementExport {
     std::vector<uint32_t> kind, moved, dof_ptr{0}, dof_ids, gp_ptr{0}, enr_ptr{0}, enr_vertex, enr_gp_ptr{0};
-    std::vector<double> xy, gp, jinv, jinv_gp, cmat, scale, enr_val, enr_grad, ke;
+    std::vector<double> xy, gp, jinv, jinv_gp, cmat, scale, enr_val, enr_grad, ke, imposed;
     std::vector<uint32_t> ke_ptr{0};
 };
 
@@ -162,6 +163,9 @@ void export_element(IntegrableEntity *e, int dim, double scale, const std::vecto
     for (size_t r = 0; r < C.numRows(); r++)
         for (size_t c = 0; c < C.numCols(); c++) X.cmat.push_back(C[r][c]);
     X.scale.push_back(scale);
+    // imposed strain of the behaviour (physics/stiffness_with_imposed_deformation.h), zeros otherwise
+    const StiffnessWithImposedStrain *imp = dynamic_cast<const StiffnessWithImposedStrain *>(e->getBehaviour());
+    for (size_t k = 0; k < C.numRows(); k++) X.imposed.push_back(imp && k < imp->imposed.size() ? imp->imposed[k] : 0.0);
 
     for (size_t j = 0; j < nenr; j++) {
         const Function &f = e->getEnrichmentFunction(j);
@@ -212,6 +216,7 @@ void write_elements(Out &o, ElementExport &X)
     o.d("enr_grad", X.enr_grad);
     o.u("ke_ptr", X.ke_ptr);
     o.d("ke", X.ke);
+    o.d("elem_imposed", X.imposed);
 }
 
 // Dirichlet multipliers as stored by the Assembly (before make_final sorts them).
@@ -275,7 +280,13 @@ int run_2d(const std::string &which, Out &o, std::map<std::string, std::string> 
     const double disp = getd(kv, "disp", 1e-5);
 
     RectangularFeature box(nullptr, L, L, 0, 0);
-    box.setBehaviour(new Stiffness(E, nu, SPACE_TWO_DIMENSIONAL, PLANE_STRESS));
+    if (which == "imposed")
+        // the behaviour examples/test/test_stiffness_with_imposed_deformation.ini builds through
+        // utilities/object_translator.cpp:289-295 (the (E, nu, alpha) constructor)
+        box.setBehaviour(new StiffnessWithImposedStrain(E, nu, getd(kv, "imposed", 1e-3), SPACE_TWO_DIMENSIONAL,
+                                                        PLANE_STRESS, YOUNG_POISSON));
+    else
+        box.setBehaviour(new Stiffness(E, nu, SPACE_TWO_DIMENSIONAL, PLANE_STRESS));
     FeatureTree F(&box);
 
     std::vector<Feature *> placed;
@@ -300,6 +311,14 @@ int run_2d(const std::string &which, Out &o, std::map<std::string, std::string> 
         new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, BOTTOM),
         new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM),
         new BoundingBoxDefinedBoundaryCondition(SET_ALONG_ETA, TOP, disp)};
+    if (which == "imposed") {
+        // examples/main_check_behaviour.cpp with --free: the plate is held by rollers only
+        // and expands under its imposed strain; the reference's known answer is
+        // strain_yy * 1e3 = 1, stress_yy / 1e6 = 0
+        // (examples/test/check_behaviour_test_stiffness_with_imposed_deformation_base).
+        bcs = {new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM),
+               new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, BOTTOM_LEFT)};
+    }
     if (which == "plate") {
         // examples/main_check_behaviour.cpp with examples/test/test_stiffness.ini:
         // 10 x 10 mm plate, E = 10 GPa, nu = 0.2, 1 MPa imposed as a stress on TOP;
@@ -403,7 +422,7 @@ int main(int argc, char **argv)
     auto kv = parse_kv(argc, argv, 3);
     Out o(argv[2]);
     if (!o.f) return 3;
-    if (which == "incl" || which == "crack" || which == "plate") return run_2d(which, o, kv);
+    if (which == "incl" || which == "crack" || which == "plate" || which == "imposed") return run_2d(which, o, kv);
     if (which == "voxel") return run_voxel(o, kv);
     std::fprintf(stderr, "unknown case %s\n", which.c_str());
     return 2;

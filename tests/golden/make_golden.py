@@ -37,6 +37,10 @@ CASES = {
     # known-answer test of examples/test/test_stiffness.ini: 10 mm plate, 1 MPa imposed
     # stress on TOP (force multipliers), E = 10 GPa -> strain_yy = 1e-4 everywhere
     "plate": ("plate", ["size=0.01", "E=10e9", "nu=0.2", "sampling=4"]),
+    # known-answer test of examples/test/test_stiffness_with_imposed_deformation.ini: the
+    # same plate, free on rollers, imposed strain 1e-3 (induced force multipliers)
+    # -> strain_yy = 1e-3, real stress 0
+    "imposed": ("imposed", ["size=0.01", "E=10e9", "nu=0.2", "sampling=4", "imposed=1e-3"]),
     # config-2 style: voxel file -> 6 linear tets per voxel, 16 lognormal phases,
     # uniaxial imposed strain 1e-4
     "voxel_t4": ("voxel", ["n=6", "nphase=16", "seed=5", "strain=1e-4"]),

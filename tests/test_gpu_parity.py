@@ -186,6 +186,67 @@ def test_element_fields(golden_topos, name):
         assert np.allclose(eps[:, 1], 1e-4, rtol=1e-9) and np.allclose(sig[:, 1], 1e6, rtol=1e-9)
 
 
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_average_field(golden_topos, name):
+    """Mesh average of strain and stress (Mesh::getField): element Gauss averages weighted by
+    element area / volume, against the same sum over the oracle's element fields."""
+    import amie_gpu
+    d, m, t = golden_topos[name]
+    t.assemble()
+    t.apply_dirichlet(*am.golden_bcs(d))
+    x, st = t.solve(amie_gpu.SOLVER_PCG_FP64, rtol=1e-12)
+    eo, so = O.element_fields(m, x)
+    D = m.stride
+    J = m.jinv.reshape(-1, D, D)
+    v = (0.5 if D == 2 else 1.0 / 6.0) / np.abs(np.linalg.det(J))
+    for field, ref in ((amie_gpu.FIELD_STRAIN, eo), (amie_gpu.FIELD_STRESS, so)):
+        avg, w = t.average_field(field)
+        want = (v[:, None] * ref).sum(axis=0) / v.sum()
+        assert abs(w - v.sum()) <= 1e-12 * v.sum()
+        assert np.abs(avg - want).max() <= 1e-11 * max(np.abs(want).max(), 1e-300)
+    if name == "plate":   # the reference's known answer on the 10 x 10 mm plate
+        eps, w = t.average_field(amie_gpu.FIELD_STRAIN)
+        sig, _ = t.average_field(amie_gpu.FIELD_STRESS)
+        assert abs(eps[1] * 1e3 - 0.1) <= 1e-9 and abs(sig[1] / 1e6 - 1.0) <= 1e-9
+        assert abs(w - 1e-4) <= 1e-12 * 1e-4
+
+
+def test_imposed_strain_induced_forces(gpu_ctx):
+    """StiffnessWithImposedStrain on the device: with the reference's Dirichlet multipliers
+    only, the GPU's induced forces rebuild the reference's right-hand side (which holds
+    them as force multipliers), the solve matches, and the known answer of
+    check_behaviour_test_stiffness_with_imposed_deformation holds (strain_yy * 1e3 = 1,
+    real stress 0)."""
+    import amie_gpu
+    d = load_golden("imposed")
+    m = am.from_golden(d, "tabulated")
+    ids, vals, kinds = am.golden_bcs(d)
+    keep = kinds != am.BC_FORCE
+    eps0 = d["elem_imposed"].reshape(m.n_elem, -1)
+    t = amie_gpu.Topology(gpu_ctx, m)
+    try:
+        t.set_imposed_strain(eps0)
+        t.assemble()
+        t.apply_dirichlet(ids[keep], vals[keep], kinds[keep])
+        arr, rhs = t.matrix()
+        assert np.abs(rhs - d["rhs"]).max() <= 1e-12 * np.abs(d["rhs"]).max()
+        assert rel(arr, d["array"]) <= 1e-12
+        x, st = t.solve(amie_gpu.SOLVER_PCG_FP64, rtol=1e-12)
+        xo, _, _, _ = O.pcg(m.stride, d["row_size"], d["column_index"], d["array"], d["rhs"], rtol=1e-13)
+        assert rel(x, xo) <= 1e-9
+        eps, w = t.average_field(amie_gpu.FIELD_STRAIN)
+        assert abs(eps[1] * 1e3 - 1.0) <= 1e-9 and abs(eps[0] * 1e3 - 1.0) <= 1e-9
+        _, sig = t.element_fields()
+        assert np.abs(sig).max() / 1e6 <= 1e-6     # real stress C (eps - eps0)
+        # re-assembly keeps the forces; removing the imposed strain removes them
+        t.assemble()
+        assert np.abs(t.matrix()[1] - d["rhs"]).max() <= 1e-12 * np.abs(d["rhs"]).max()
+        t.set_imposed_strain(None)
+        assert np.abs(t.matrix()[1]).max() <= 1e-12 * np.abs(d["rhs"]).max()
+    finally:
+        t.close()
+
+
 def test_damage_step_and_reassembly(gpu_ctx):
     """Damage update on the device, then (1-d) C re-integration: matches the damage law
     applied to the oracle's strains and the oracle's K_e with cscale = 1 - d."""

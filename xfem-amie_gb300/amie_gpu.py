@@ -34,8 +34,9 @@ EXPORTED = [
     "amie_solve_resident", "amie_solution_download", "amie_server_start", "amie_submit", "amie_poll",
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
     "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step", "amie_pcg_solve_noalloc",
-    "amie_topology_spmv_lanes", "amie_profile_stream",
+    "amie_topology_spmv_lanes", "amie_profile_stream", "amie_average_field", "amie_set_imposed_strain",
 ]
+FIELD_STRAIN, FIELD_STRESS = 0, 1
 
 
 class DamageParams(C.Structure):
@@ -274,6 +275,23 @@ class Topology:
         sig = np.zeros(self.mesh.n_elem * nv, np.float64)
         check(lib().amie_element_fields(self.ptr, _p(eps), _p(sig)), "amie_element_fields")
         return eps.reshape(-1, nv), sig.reshape(-1, nv)
+
+    def set_imposed_strain(self, eps0):
+        """Imposed strain per element ([n_elem, nv] Voigt, None removes it): induced forces in the RHS."""
+        if eps0 is None:
+            check(lib().amie_set_imposed_strain(self.ptr, None), "amie_set_imposed_strain")
+            return
+        e = np.ascontiguousarray(eps0, np.float64).reshape(-1)
+        if e.size != self.mesh.n_elem * self.mesh.nv:
+            raise ValueError("eps0 must have n_elem * nv entries")
+        check(lib().amie_set_imposed_strain(self.ptr, _p(e)), "amie_set_imposed_strain")
+
+    def average_field(self, field=FIELD_STRAIN):
+        """(mesh average of the strain or stress, total area or volume) from the device solution."""
+        avg = np.zeros(self.mesh.nv, np.float64)
+        w = C.c_double()
+        check(lib().amie_average_field(self.ptr, C.c_int32(field), _p(avg), C.byref(w)), "amie_average_field")
+        return avg, w.value
 
     def damage_step(self, eps0=1e-4, softening=5000.0, d_max=0.9999, change_tol=1e-6, want_damage=True):
         """One damage update from the device solution; returns (elements changed, damage or None)."""

@@ -430,6 +430,107 @@ __global__ void k_to_sell(uint64_t n_slots, const uint32_t *sell_blk, const doub
     }
 }
 
+// Induced forces of the imposed strain, one thread per element: for every
+// function f, sum_g w_g B_f(g)^T (C eps0) into the staging slot of (element, f)
+// (StiffnessWithImposedStrain::getBoundaryConditions,
+// physics/stiffness_with_imposed_deformation.cpp:83-110, through the
+// SET_VOLUMIC_STRESS_* conditions of features/boundarycondition.cpp:542-617;
+// C undamaged, as there).
+template <int DIM>
+__global__ void k_elem_forces(MeshView m, double *fstage)
+{
+    constexpr int NV = DIM == 2 ? 3 : 6;
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m.n_elem) return;
+    const double *C = m.cmat_table + (size_t)m.mat[e] * NV * NV;
+    double sig[NV];
+#pragma unroll
+    for (int r = 0; r < NV; r++) {
+        double a = 0.0;
+#pragma unroll
+        for (int c = 0; c < NV; c++) a += C[r * NV + c] * m.imposed[(size_t)e * NV + c];
+        sig[r] = a;
+    }
+    const int kind = m.kind[e];
+    const int nshape = nshape_of(kind);
+    const uint32_t f0 = m.enr_ptr ? m.enr_ptr[e] : 0, f1 = m.enr_ptr ? m.enr_ptr[e + 1] : 0;
+    const int nf = nshape + (int)(f1 - f0);
+    const uint32_t d0 = m.dof_ptr[e];
+    double Je[DIM * DIM];
+#pragma unroll
+    for (int i = 0; i < DIM * DIM; i++) Je[i] = m.jinv[(size_t)e * DIM * DIM + i];
+    const uint32_t g0 = m.gp_ptr[e], g1 = m.gp_ptr[e + 1];
+    const bool explicit_gp = g1 > g0;
+    const bool moved = explicit_gp && m.moved && m.moved[e];
+    const int ngp = explicit_gp ? (int)(g1 - g0) : (kind == AMIE_TRI6 ? 4 : 1);
+    const double inv_det = 1.0 / det_small<DIM>(Je);
+    for (int f = 0; f < nf; f++) {
+        double acc[DIM];
+#pragma unroll
+        for (int c = 0; c < DIM; c++) acc[c] = 0.0;
+        for (int g = 0; g < ngp; g++) {
+            double p[3], w;
+            if (explicit_gp) {
+                const double *gp = m.gp + (size_t)(g0 + g) * (DIM + 1);
+                p[0] = gp[0]; p[1] = gp[1]; p[2] = DIM == 3 ? gp[2] : 0.0;
+                w = gp[DIM];
+            } else {
+                default_rule(kind, g, p, &w);
+                w *= inv_det;
+            }
+            const double *J = moved ? m.jinv_gp + (size_t)(g0 + g) * DIM * DIM : Je;
+            double lg[3] = {0.0, 0.0, 0.0};
+            if (f < nshape) {
+                shape_grad(kind, f, p[0], p[1], lg);
+            } else {
+                const uint32_t fj = f0 + (f - nshape);
+                const uint64_t off = (uint64_t)m.enr_data[fj] + g;
+                if (m.enr_type[fj] == AMIE_ENR_HEAVISIDE) {
+                    const int v = m.enr_vertex[fj];
+                    const double jump = (double)m.enr_jump[off];
+                    const double gx[3] = {0.0, -1.0, 1.0}, gy[3] = {1.0, -1.0, 0.0};
+                    lg[0] = gx[v] * jump;
+                    lg[1] = gy[v] * jump;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < DIM; c++) lg[c] = m.enr_grad[off * DIM + c];
+                }
+            }
+            double d[3];
+            phys_grad<DIM>(J, lg, d);
+            if (DIM == 2) {
+                acc[0] += w * (d[0] * sig[0] + d[1] * sig[2]);
+                acc[1] += w * (d[1] * sig[1] + d[0] * sig[2]);
+            } else {
+                acc[0] += w * (d[0] * sig[0] + d[2] * sig[4] + d[1] * sig[5]);
+                acc[1] += w * (d[1] * sig[1] + d[2] * sig[3] + d[0] * sig[5]);
+                acc[2] += w * (d[2] * sig[2] + d[1] * sig[3] + d[0] * sig[4]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < DIM; c++) fstage[(uint64_t)(d0 + f) * DIM + c] = acc[c];
+    }
+}
+
+// rhs += the staged forces of each block row, summed in element order.
+template <int S>
+__global__ void k_force_gather(uint32_t n_rows, const uint32_t *fmap_ptr, const uint32_t *fmap, const double *fstage,
+                               double *rhs)
+{
+    const uint32_t row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n_rows) return;
+    double acc[S];
+#pragma unroll
+    for (int c = 0; c < S; c++) acc[c] = 0.0;
+    for (uint32_t k = fmap_ptr[row]; k < fmap_ptr[row + 1]; k++) {
+        const uint64_t src = (uint64_t)fmap[k] * S;
+#pragma unroll
+        for (int c = 0; c < S; c++) acc[c] += fstage[src + c];
+    }
+#pragma unroll
+    for (int c = 0; c < S; c++) rhs[(uint64_t)row * S + c] += acc[c];
+}
+
 template <typename T>
 amie_status upload(amie_ctx *ctx, DevArray<T> &d, const T *h, size_t n)
 {
@@ -449,6 +550,7 @@ MeshView mesh_view(amie_topo *t)
     m.enr_ptr = t->enr_ptr.p; m.enr_type = t->enr_type.p; m.enr_vertex = t->enr_vertex.p;
     m.enr_data = t->enr_data.p; m.enr_jump = t->enr_jump.p; m.enr_grad = t->enr_grad.p;
     m.blk_off = t->blk_off.p; m.ke = t->ke.p;
+    m.imposed = t->has_imposed ? t->imposed.p : nullptr;
     return m;
 }
 
@@ -938,10 +1040,32 @@ amie_status dirichlet_async(amie_topo *t, uint32_t n_bc, const uint32_t *ids_dev
 namespace amie {
 
 // Elimination with the stored multipliers (after a fresh gather).
+// rhs += the forces induced by the imposed strain (before elimination: a
+// constrained row's right-hand side is then replaced by its value, as the
+// reference's force multipliers never reach a constrained DOF).
+amie_status add_induced_forces_async(amie_topo *t)
+{
+    if (!t->has_imposed) return AMIE_OK;
+    cudaStream_t st = t->ctx->stream;
+    const MeshView m = mesh_view(t);
+    if (t->dim == 2) k_elem_forces<2><<<blocks_for(t->n_elem, 128), 128, 0, st>>>(m, t->fstage.p);
+    else k_elem_forces<3><<<blocks_for(t->n_elem, 128), 128, 0, st>>>(m, t->fstage.p);
+    if (t->s == 2)
+        k_force_gather<2><<<blocks_for(t->n_rows, 256), 256, 0, st>>>(t->n_rows, t->fmap_ptr.p, t->fmap.p, t->fstage.p,
+                                                                      t->rhs.p);
+    else
+        k_force_gather<3><<<blocks_for(t->n_rows, 256), 256, 0, st>>>(t->n_rows, t->fmap_ptr.p, t->fmap.p, t->fstage.p,
+                                                                      t->rhs.p);
+    g_launches += 2;
+    AMIE_CUDA(cudaGetLastError());
+    return AMIE_OK;
+}
+
 amie_status reapply_dirichlet_async(amie_topo *t)
 {
     cudaStream_t st = t->ctx->stream;
     if (t->has_rhs0) AMIE_CUDA(cudaMemcpyAsync(t->rhs.p, t->rhs0.p, t->n * 8, cudaMemcpyDeviceToDevice, st));
+    AMIE_TRY(add_induced_forces_async(t));
     return dirichlet_async(t, t->n_bc, t->bc_ids.p, t->bc_vals.p, t->has_bc_kinds ? t->bc_kinds.p : nullptr);
 }
 
@@ -953,8 +1077,47 @@ extern "C" amie_status amie_assemble(amie_topo *t)
     AMIE_CUDA(cudaSetDevice(t->ctx->device));
     AMIE_TRY(assemble_async(t));
     if (t->bc_set) AMIE_TRY(reapply_dirichlet_async(t));
+    else AMIE_TRY(add_induced_forces_async(t));
     AMIE_TRY(finalize_matrix_async(t, false));
     AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_set_imposed_strain(amie_topo *t, const double *eps0)
+{
+    if (!t) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    cudaStream_t st = t->ctx->stream;
+    if (!eps0) {
+        t->has_imposed = false;
+    } else {
+        if (!t->fmap_ptr.p) {
+            // block row -> staging slots of its (element, function) pairs, in element order
+            const uint32_t nfun = t->h_dof_ptr[t->n_elem];
+            std::vector<uint32_t> ids(nfun);
+            AMIE_CUDA(cudaMemcpyAsync(ids.data(), t->dof_ids.p, (size_t)nfun * 4, cudaMemcpyDeviceToHost, st));
+            AMIE_CUDA(cudaStreamSynchronize(st));
+            std::vector<uint32_t> ptr(t->n_rows + 1, 0), map(nfun);
+            for (uint32_t c = 0; c < nfun; c++) {
+                if (ids[c] >= t->n_rows) {
+                    set_error("DOF id %u >= %u rows", ids[c], t->n_rows);
+                    return AMIE_BAD_INPUT;
+                }
+                ptr[ids[c] + 1]++;
+            }
+            for (uint32_t r = 0; r < t->n_rows; r++) ptr[r + 1] += ptr[r];
+            std::vector<uint32_t> fill(ptr.begin(), ptr.end() - 1);
+            for (uint32_t c = 0; c < nfun; c++) map[fill[ids[c]]++] = c;
+            AMIE_TRY(upload(t->ctx, t->fmap_ptr, ptr.data(), ptr.size()));
+            AMIE_TRY(upload(t->ctx, t->fmap, map.data(), map.size()));
+            AMIE_TRY(t->fstage.alloc(t->ctx, (size_t)nfun * t->s));
+        }
+        AMIE_TRY(upload(t->ctx, t->imposed, eps0, (size_t)t->n_elem * t->nv));
+        t->has_imposed = true;
+    }
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    // an assembled topology gets its right-hand side rebuilt from the original matrix
+    if (t->assembled) return amie_assemble(t);
     return AMIE_OK;
 }
 

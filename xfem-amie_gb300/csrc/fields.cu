@@ -10,6 +10,9 @@
 //            exponential softening d = 1 - (eps0/eq) exp(-B (eq - eps0)).
 #include "element.cuh"
 
+#include <algorithm>
+#include <vector>
+
 namespace amie {
 
 // Weighted average over the element's Gauss points of the strain
@@ -93,11 +96,15 @@ __global__ void k_element_fields(MeshView m, const double *x, double *strain, do
     const double *C = m.cmat_table + (size_t)m.mat[e] * NV * NV;
 #pragma unroll
     for (int k = 0; k < NV; k++) eps[k] *= inv;
+    // real stress C (eps - eps0) with an imposed strain (REAL_STRESS_FIELD)
+    double el[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) el[k] = m.imposed ? eps[k] - m.imposed[(size_t)e * NV + k] : eps[k];
 #pragma unroll
     for (int k = 0; k < NV; k++) {
         double s = 0.0;
 #pragma unroll
-        for (int l = 0; l < NV; l++) s += C[k * NV + l] * eps[l];
+        for (int l = 0; l < NV; l++) s += C[k * NV + l] * el[l];
         if (strain) strain[(size_t)e * NV + k] = eps[k];
         if (stress) stress[(size_t)e * NV + k] = cs * s;
     }
@@ -123,6 +130,46 @@ __global__ void k_damage(uint32_t n_elem, const double *strain, amie_damage_para
     damage[e] = d;
     cscale[e] = (cscale_base ? cscale_base[e] : 1.0) * (1.0 - d);
     if (d - dold > prm.change_tol) atomicAdd(n_changed, 1u);
+}
+
+// Per-CTA sums of v_e f_e (nv components) and v_e, v_e the element's area
+// (2D: 0.5 / |det J^-1|, the triangle of its corners) or volume (3D:
+// (1/6) / |det J^-1|), J^-1 at the centroid.  Each thread Kahan-sums its
+// elements in index order; the CTA adds its threads in a fixed tree.
+// parts: [gridDim.x][nv + 1].
+template <int DIM>
+__global__ void __launch_bounds__(256) k_average_parts(uint32_t n_elem, const double *jinv, const double *field,
+                                                       double *parts)
+{
+    constexpr int NV = DIM == 2 ? 3 : 6;
+    __shared__ double sh[256];
+    double acc[NV + 1], comp[NV + 1];
+#pragma unroll
+    for (int k = 0; k <= NV; k++) acc[k] = comp[k] = 0.0;
+    for (uint32_t e = blockIdx.x * 256 + threadIdx.x; e < n_elem; e += gridDim.x * 256) {
+        double J[DIM * DIM];
+#pragma unroll
+        for (int i = 0; i < DIM * DIM; i++) J[i] = jinv[(size_t)e * DIM * DIM + i];
+        const double v = (DIM == 2 ? 0.5 : 1.0 / 6.0) / fabs(det_small<DIM>(J));
+#pragma unroll
+        for (int k = 0; k <= NV; k++) {
+            const double term = (k < NV ? v * field[(size_t)e * NV + k] : v) - comp[k];
+            const double sum = acc[k] + term;
+            comp[k] = (sum - acc[k]) - term;
+            acc[k] = sum;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k <= NV; k++) {
+        sh[threadIdx.x] = acc[k];
+        __syncthreads();
+        for (int o = 128; o > 0; o >>= 1) {
+            if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) parts[(size_t)blockIdx.x * (NV + 1) + k] = sh[0];
+        __syncthreads();
+    }
 }
 
 MeshView mesh_view(amie_topo *t);
@@ -186,5 +233,46 @@ extern "C" amie_status amie_damage_step(amie_topo *t, const amie_damage_params *
     if (damage_out) AMIE_CUDA(cudaMemcpyAsync(damage_out, t->damage.p, (size_t)E * 8, cudaMemcpyDeviceToHost, st));
     AMIE_CUDA(cudaStreamSynchronize(st));
     if (n_changed) *n_changed = changed;
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_average_field(amie_topo *t, int32_t field, double *avg, double *measure)
+{
+    if (!t || !avg || (field != AMIE_FIELD_STRAIN && field != AMIE_FIELD_STRESS)) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    cudaStream_t st = t->ctx->stream;
+    const int nv = t->nv;
+    const uint32_t E = t->n_elem;
+    if (!t->strain.p) AMIE_TRY(t->strain.alloc(t->ctx, (size_t)E * nv));
+    DevArray<double> dstress, parts;
+    if (field == AMIE_FIELD_STRESS) AMIE_TRY(dstress.alloc(t->ctx, (size_t)E * nv));
+    const int grid = std::max(1, std::min<int>(t->ctx->num_sms * 4, (int)((E + 255) / 256)));
+    AMIE_TRY(parts.alloc(t->ctx, (size_t)grid * (nv + 1)));
+    const MeshView m = mesh_view(t);
+    const int blocks = (int)((E + 127) / 128);
+    const double *f = field == AMIE_FIELD_STRESS ? dstress.p : t->strain.p;
+    if (t->dim == 2) {
+        k_element_fields<2><<<blocks, 128, 0, st>>>(m, t->x.p, t->strain.p, dstress.p);
+        k_average_parts<2><<<grid, 256, 0, st>>>(E, t->jinv.p, f, parts.p);
+    } else {
+        k_element_fields<3><<<blocks, 128, 0, st>>>(m, t->x.p, t->strain.p, dstress.p);
+        k_average_parts<3><<<grid, 256, 0, st>>>(E, t->jinv.p, f, parts.p);
+    }
+    g_launches += 2;
+    std::vector<double> h((size_t)grid * (nv + 1));
+    AMIE_CUDA(cudaMemcpyAsync(h.data(), parts.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    // the CTA partials in index order (Kahan), then the reference's division
+    std::vector<double> acc(nv + 1, 0.0), comp(nv + 1, 0.0);
+    for (int b = 0; b < grid; b++)
+        for (int k = 0; k <= nv; k++) {
+            const double term = h[(size_t)b * (nv + 1) + k] - comp[k];
+            const double sum = acc[k] + term;
+            comp[k] = (sum - acc[k]) - term;
+            acc[k] = sum;
+        }
+    const double w = acc[nv];
+    for (int k = 0; k < nv; k++) avg[k] = w > 1e-24 ? acc[k] / w : acc[k];
+    if (measure) *measure = w;
     return AMIE_OK;
 }

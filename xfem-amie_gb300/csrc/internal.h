@@ -103,6 +103,7 @@ struct MeshView {
     const double *enr_grad;
     const uint64_t *blk_off;  // first staged block of each element (in s*s blocks)
     double *ke;               // staged element matrices: nf*nf blocks of s*s, row-major
+    const double *imposed;    // imposed strain per element (Voigt, nv), or null
 };
 
 // Block-sparse matrix on the device: CSR over block rows, s x s blocks row-major.
@@ -199,6 +200,11 @@ struct amie_topo {
     amie::DevArray<uint8_t> fixed;
     amie::DevArray<double> fixval;
     amie::DevArray<double> strain, damage, cscale_base;   // field recovery and damage loop
+    // imposed strain (per element) and its induced forces: staged per element
+    // function, gathered per block row through fmap (contributions in element order)
+    amie::DevArray<double> imposed, fstage;
+    amie::DevArray<uint32_t> fmap, fmap_ptr;
+    bool has_imposed = false;
     // Dirichlet / force multipliers and initial forces of the last
     // amie_apply_dirichlet; re-applied by every amie_assemble (make_final does
     // scatter + setBoundaryConditions in one call, solvers/assembly.cpp:803-816).
