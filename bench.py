@@ -483,6 +483,7 @@ def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, p
         tickets.append(srv.submit(m, *bcs))
     srv.drain(600.0)
     wall = time.perf_counter() - t0
+    loop_stats = srv.stats()
     lat, statuses, dofs, iters = [], [], [], []
     for k, tk in enumerate(tickets):
         r = srv.poll(tk, want_x=False)
@@ -500,7 +501,8 @@ def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, p
             "p99_latency_s": float(np.percentile(lat, 99)), "solves_per_s": ok / wall, "wall_s": wall,
             "mean_dof": float(np.mean(dofs)) if dofs else 0.0, "mean_iterations": float(np.mean(iters)) if iters else 0.0,
             "distinct_microstructures": pool,
-            "solver": "mixed" if solver == G.SOLVER_PCG_MIXED else "fp64"}
+            "solver": "mixed" if solver == G.SOLVER_PCG_MIXED else "fp64",
+            "host_loop_s": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in loop_stats.items()}}
 
 
 def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 6e-5):

@@ -264,6 +264,16 @@ AMIE_API amie_status amie_cancel(amie_server *srv, uint64_t ticket);
 AMIE_API amie_status amie_server_drain(amie_server *srv, double timeout_s);
 AMIE_API amie_status amie_server_stop(amie_server *srv);
 
+/* Where the server's host loop spent its time since start (seconds of wall
+ * clock): admitting requests (topology, assembly, elimination, SELL copy),
+ * waiting for batch graphs, residual replacements, joins; batches launched.
+ * No reference counterpart: a report of the serving loop. */
+typedef struct amie_server_stats {
+    double admit_s, wait_s, advance_s, join_s, loop_s;
+    uint64_t batches, admitted;
+} amie_server_stats;
+AMIE_API amie_status amie_server_query(amie_server *srv, amie_server_stats *stats);
+
 /* ------------------------------------------------------------------ fields and damage
  * Per-element strain (Voigt, engineering shear: xx yy xy in 2D, xx yy zz yz xz xy
  * in 3D) and stress (C_eff strain) from the device-resident solution, averaged

@@ -35,7 +35,13 @@ EXPORTED = [
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
     "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step", "amie_pcg_solve_noalloc",
     "amie_topology_spmv_lanes", "amie_profile_stream", "amie_average_field", "amie_set_imposed_strain",
+    "amie_server_query",
 ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("admit_s", C.c_double), ("wait_s", C.c_double), ("advance_s", C.c_double), ("join_s", C.c_double),
+                ("loop_s", C.c_double), ("batches", C.c_uint64), ("admitted", C.c_uint64)]
 FIELD_STRAIN, FIELD_STRESS = 0, 1
 
 
@@ -331,6 +337,12 @@ class Server:
         check(lib().amie_submit(self.ptr, C.byref(req), C.byref(t)), "amie_submit")
         self._n[t.value] = (int(max(m.ndofmax, int(m.dof_ids.max()) + 1)) * m.stride)
         return t.value
+
+    def stats(self) -> dict:
+        """Host-loop time split since start (admission, batch waits, residual replacements, joins)."""
+        st = ServerStats()
+        check(lib().amie_server_query(self.ptr, C.byref(st)), "amie_server_query")
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
 
     def poll(self, ticket: int, want_x: bool = True):
         """None while running; else (result dict, solution or None)."""

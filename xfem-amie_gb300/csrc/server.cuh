@@ -133,6 +133,7 @@ struct amie_server {
     amie_server_config cfg{};
     bool mixed = true;
     int grid = 0, group = 8;
+    int rows_per_cta = 512;   // block rows per CTA of a slot
     uint64_t budget = 0;
     std::atomic<uint64_t> in_use{0};
 
@@ -163,7 +164,10 @@ struct amie_server {
     std::map<uint64_t, Req *> all;
     uint64_t next_ticket = 1;
     bool running = false, stop_flag = false;
-    std::thread worker;
+    std::thread worker;     // the batch loop
+    std::thread admitter;   // admissions, on the admission context, overlapping the batch
+    std::deque<Req *> ready;                     // admitted, waiting to join (under mu)
+    int admitting = 0, n_active = 0, n_waiting = 0;   // (under mu) inside admit(), in slots, admitted but not joined
 
     // batch state
     std::vector<Req *> slot_req;                 // per slot
@@ -178,6 +182,7 @@ struct amie_server {
     int16_t *h_cta_slot = nullptr;               // pinned
     cudaGraphExec_t graph = nullptr;
     std::string error;
+    amie_server_stats stats{};   // written by the loop thread under `mu`
 };
 
 namespace amie {
@@ -250,7 +255,7 @@ struct ServerOps {
         AMIE_TRY(ensure_state(t, srv->mixed, &s));
         if (srv->mixed) AMIE_TRY(finalize_matrix_async(t, true));
         AMIE_TRY(ensure_sell(t, !srv->mixed, srv->mixed));
-        AMIE_TRY(ensure_sell_partition(t, ctas_for(t->n_rows)));   // the slot's CTA count
+        AMIE_TRY(ensure_sell_partition(t, ctas_for(srv, t->n_rows)));   // the slot's CTA count
         cudaStream_t st = srv->adm->stream;
         if (!r->x0.empty() && r->x0.size() == t->n)
             AMIE_CUDA(cudaMemcpyAsync(t->x.p, r->x0.data(), t->n * 8, cudaMemcpyHostToDevice, st));
@@ -278,9 +283,11 @@ struct ServerOps {
         return -1;
     }
 
-    static int ctas_for(uint64_t n_rows)
+    // CTAs of a slot: a function of its row count only (so a solve is the same
+    // alone and in any mix), srv->rows_per_cta block rows each, at most 128.
+    static int ctas_for(const amie_server *srv, uint64_t n_rows)
     {
-        const uint64_t per = (uint64_t)(kVecThreads / 8) * 8;   // 8 row passes of 32 rows
+        const uint64_t per = (uint64_t)srv->rows_per_cta;
         return (int)std::max<uint64_t>(1, std::min<uint64_t>(128, (n_rows + per - 1) / per));
     }
 
@@ -370,12 +377,16 @@ struct ServerOps {
         for (size_t i = 0; i < srv->slot_req.size(); i++)
             if (!srv->slot_req[i]) { slot = (int)i; break; }
         if (slot < 0) return AMIE_NOT_READY;
-        const int count = ctas_for(r->topo->n_rows);
+        const int count = ctas_for(srv, r->topo->n_rows);
         const int c0 = alloc_ctas(srv, count);
         if (c0 < 0) return AMIE_NOT_READY;
         for (int c = c0; c < c0 + count; c++) srv->h_cta_slot[c] = (int16_t)slot;
         srv->slot_req[slot] = r;
         r->slot = slot;
+        {
+            std::lock_guard<std::mutex> lk(srv->mu);
+            srv->n_active++;
+        }
         fill_desc(srv, slot, r->topo, c0, c0 + count);
         cudaStream_t st = srv->ctx->stream;
         AMIE_CUDA(cudaMemcpyAsync(srv->d_cta_slot.p, srv->h_cta_slot, srv->grid * sizeof(int16_t), cudaMemcpyHostToDevice, st));
@@ -407,6 +418,8 @@ struct ServerOps {
             AMIE_CUDA(cudaStreamSynchronize(st));
             srv->slot_req[slot] = nullptr;
             r->slot = -1;
+            std::lock_guard<std::mutex> lk(srv->mu);
+            srv->n_active--;
         }
         if (t) {
             amie_topology_destroy(t);
@@ -502,11 +515,74 @@ struct ServerOps {
         return false;
     }
 
+    // Admission thread: takes pending requests while slots allow and admits
+    // them (topology, assembly, elimination, SELL copy, first residual) on the
+    // admission context, overlapping the batch loop; hands them over in `ready`.
+    static void admit_loop(amie_server *srv)
+    {
+        cudaSetDevice(srv->ctx->device);
+        while (true) {
+            amie_server::Req *r = nullptr;
+            {
+                std::unique_lock<std::mutex> lk(srv->mu);
+                while (true) {
+                    if (srv->stop_flag && srv->pending.empty()) return;
+                    const int used = srv->n_active + srv->n_waiting + (int)srv->ready.size() + srv->admitting;
+                    if (!srv->pending.empty() && used < (int)srv->slot_req.size()) {
+                        amie_server::Req *c = srv->pending.front();
+                        if (c->cancelled) {
+                            srv->pending.pop_front();
+                            c->status = AMIE_CANCELLED;
+                            c->t_done = now_s();
+                            srv->cv.notify_all();
+                            continue;
+                        }
+                        if (c->footprint > srv->budget) {   // can never fit
+                            srv->pending.pop_front();
+                            c->status = AMIE_OOM;
+                            c->t_done = now_s();
+                            srv->cv.notify_all();
+                            continue;
+                        }
+                        if (srv->in_use + c->footprint <= srv->budget) {
+                            srv->pending.pop_front();
+                            srv->in_use += c->footprint;
+                            srv->admitting++;
+                            r = c;
+                            break;
+                        }
+                    }
+                    srv->cv.wait_for(lk, std::chrono::milliseconds(2));
+                }
+            }
+            const double ta = now_s();
+            r->t_admit = ta;
+            const amie_status st = admit(srv, r);
+            if (st != AMIE_OK && r->topo) {
+                amie_topology_destroy(r->topo);
+                r->topo = nullptr;
+            }
+            std::lock_guard<std::mutex> lk(srv->mu);
+            srv->admitting--;
+            srv->stats.admit_s += now_s() - ta;
+            srv->stats.admitted++;
+            if (st != AMIE_OK) {
+                srv->in_use -= r->footprint;
+                r->status = st;
+                r->t_done = now_s();
+            } else {
+                srv->ready.push_back(r);
+            }
+            srv->cv.notify_all();
+        }
+    }
+
     static void loop(amie_server *srv)
     {
         cudaSetDevice(srv->ctx->device);
-        std::vector<amie_server::Req *> admitted;
+        std::vector<amie_server::Req *> admitted;   // handed over, not yet joined
         while (true) {
+            const double t_round = now_s();
             // 1. batch iterations in flight on the solve stream
             const bool active = any_active(srv);
             if (active) {
@@ -516,56 +592,26 @@ struct ServerOps {
                                 srv->ctx->stream);
                 cudaEventRecord(srv->ctx->ev1, srv->ctx->stream);
             }
-            // 2. admission, overlapping the batch on the device
-            std::vector<amie_server::Req *> to_admit;
+            // 2. requests the admission thread has finished
             {
                 std::unique_lock<std::mutex> lk(srv->mu);
-                if (!active && srv->pending.empty() && admitted.empty()) {
-                    if (srv->stop_flag) break;
+                if (!active && srv->ready.empty() && admitted.empty()) {
+                    if (srv->stop_flag && srv->pending.empty() && srv->admitting == 0) break;
                     srv->cv.wait_for(lk, std::chrono::milliseconds(2));
                     continue;
                 }
-                size_t free_slots = 0;
-                for (auto *r : srv->slot_req)
-                    if (!r) free_slots++;
-                while (!srv->pending.empty() && to_admit.size() + admitted.size() < free_slots) {
-                    amie_server::Req *r = srv->pending.front();
-                    if (r->cancelled) {
-                        srv->pending.pop_front();
-                        r->status = AMIE_CANCELLED;
-                        r->t_done = now_s();
-                        continue;
-                    }
-                    if (r->footprint > srv->budget) {   // can never fit
-                        srv->pending.pop_front();
-                        r->status = AMIE_OOM;
-                        r->t_done = now_s();
-                        continue;
-                    }
-                    if (srv->in_use + r->footprint > srv->budget) break;   // wait for memory
-                    srv->pending.pop_front();
-                    srv->in_use += r->footprint;
-                    to_admit.push_back(r);
+                while (!srv->ready.empty()) {
+                    admitted.push_back(srv->ready.front());
+                    srv->ready.pop_front();
                 }
-                srv->cv.notify_all();
+                srv->n_waiting = (int)admitted.size();
             }
-            for (auto *r : to_admit) {
-                r->t_admit = now_s();
-                amie_status st = admit(srv, r);
-                if (st != AMIE_OK) {
-                    if (r->topo) {
-                        amie_topology_destroy(r->topo);
-                        r->topo = nullptr;
-                    }
-                    srv->in_use -= r->footprint;
-                    fail_req(srv, r, st);
-                } else {
-                    admitted.push_back(r);
-                }
-            }
+            const double tw = now_s();
             // 3. batch results
+            double t_waited = tw, tv = tw, t_adv = 0.0;
             if (active) {
                 cudaEventSynchronize(srv->ctx->ev1);
+                t_waited = now_s();
                 std::vector<int> finished;
                 for (size_t i = 0; i < srv->slot_req.size(); i++) {
                     amie_server::Req *r = srv->slot_req[i];
@@ -573,16 +619,34 @@ struct ServerOps {
                     if (r->cancelled) { retire(srv, r, AMIE_CANCELLED); continue; }
                     if (srv->h_ctl[i].done) finished.push_back((int)i);
                 }
+                tv = now_s();
                 if (!finished.empty()) advance_all(srv, finished);
+                t_adv = now_s() - tv;
             }
+            const double tj = now_s();
             // 4. join admitted requests
             std::vector<amie_server::Req *> waiting;
             for (auto *r : admitted) {
+                if (r->cancelled) {
+                    fail_req(srv, r, AMIE_CANCELLED);
+                    continue;
+                }
                 amie_status st = join(srv, r);
                 if (st == AMIE_NOT_READY) waiting.push_back(r);
                 else if (st != AMIE_OK) fail_req(srv, r, st);
             }
             admitted.swap(waiting);
+            {
+                const double te = now_s();
+                std::lock_guard<std::mutex> lk(srv->mu);
+                srv->n_waiting = (int)admitted.size();
+                srv->stats.wait_s += t_waited - tw;
+                srv->stats.advance_s += t_adv;
+                srv->stats.join_s += te - tj;
+                srv->stats.loop_s += te - t_round;
+                if (active) srv->stats.batches++;
+                srv->cv.notify_all();
+            }
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) {
                 srv->error = cudaGetErrorString(e);
@@ -622,7 +686,30 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     srv->budget = c.hbm_budget_bytes ? c.hbm_budget_bytes : (uint64_t)(0.9 * free_b);
-    srv->grid = std::max(ctx->num_sms * 8, c.max_slots);
+    // the batch grid: the CTAs of the batch kernels that fit on the GPU at once
+    // (a larger grid would run in waves), and at least one CTA per slot
+    {
+        int occ = 8;
+        auto lower = [&](const void *f) {
+            int k = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, kVecThreads, 0);
+            occ = std::min(occ, std::max(1, k));
+        };
+        if (srv->mixed) {
+            lower((const void *)kb_sell_dir<float>);
+            lower((const void *)kb_update<float>);
+        } else {
+            lower((const void *)kb_sell_pq<double>);
+            lower((const void *)kb_update<double>);
+            lower((const void *)kb_direction<double>);
+        }
+        srv->grid = std::max(ctx->num_sms * occ, c.max_slots);
+        // tuning override for measurements: AMIE_SERVER_ROWS_PER_CTA
+        if (const char *e = std::getenv("AMIE_SERVER_ROWS_PER_CTA")) {
+            const int v = std::atoi(e);
+            if (v >= 32 && v <= (1 << 20)) srv->rows_per_cta = v;
+        }
+    }
     amie_config ac{ctx->device, 0, 0};
     amie_status rc = amie_ctx_create(&ac, &srv->adm);
     if (rc != AMIE_OK) {
@@ -656,6 +743,7 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
     if ((rc = ServerOps::capture(srv)) != AMIE_OK) return fail(rc);
     srv->running = true;
     srv->worker = std::thread(ServerOps::loop, srv);
+    srv->admitter = std::thread(ServerOps::admit_loop, srv);
     *out = srv;
     return AMIE_OK;
 }
@@ -784,10 +872,12 @@ extern "C" amie_status amie_server_stop(amie_server *srv)
         std::lock_guard<std::mutex> lk(srv->mu);
         srv->stop_flag = true;
         for (auto *r : srv->pending) r->cancelled = true;
+        for (auto *r : srv->ready) r->cancelled = true;
         for (auto *r : srv->slot_req)
             if (r) r->cancelled = true;
         srv->cv.notify_all();
     }
+    if (srv->admitter.joinable()) srv->admitter.join();
     if (srv->worker.joinable()) srv->worker.join();
     cudaSetDevice(srv->ctx->device);
     cudaStreamSynchronize(srv->ctx->stream);
@@ -806,5 +896,13 @@ extern "C" amie_status amie_server_stop(amie_server *srv)
     srv->d_parts.release();
     amie_ctx_destroy(srv->adm);
     delete srv;
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_server_query(amie_server *srv, amie_server_stats *stats)
+{
+    if (!srv || !stats) return AMIE_BAD_INPUT;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    *stats = srv->stats;
     return AMIE_OK;
 }
