@@ -44,10 +44,15 @@ def _wait(srv, tickets, timeout=120):
     return res
 
 
-@pytest.mark.parametrize("solver", ["mixed", "fp64"])
-def test_alone_equals_mix(gpu_ctx, solver):
+@pytest.mark.parametrize("solver", ["mixed", "fp64", "mixed-persistent"])
+def test_alone_equals_mix(gpu_ctx, monkeypatch, solver):
+    """Each result is the same alone and in a mix (bitwise for the node displacements'
+    1e-12 check); "mixed-persistent" runs the batches as one cooperative launch
+    (AMIE_SERVER_PERSISTENT=1, read when a server starts)."""
     import amie_gpu as G
-    sv = G.SOLVER_PCG_MIXED if solver == "mixed" else G.SOLVER_PCG_FP64
+    if solver == "mixed-persistent":
+        monkeypatch.setenv("AMIE_SERVER_PERSISTENT", "1")
+    sv = G.SOLVER_PCG_FP64 if solver == "fp64" else G.SOLVER_PCG_MIXED
     reqs = _requests()
     alone = []
     for m, bcs, _ in reqs:

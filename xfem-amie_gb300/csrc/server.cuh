@@ -123,6 +123,65 @@ __global__ void __launch_bounds__(kVecThreads) kb_direction(const SlotDesc *slot
     direction_body<T>(slot_v<T>(*d), d->n, d->ctl, c);
 }
 
+// Persistent batch (mixed solver): one cooperative launch runs `iters` PCG
+// iterations of every active slot; the CTAs of a slot meet at a slot barrier
+// after each phase instead of at kernel boundaries.  Every wait is bounded:
+// a barrier that is not reached within kBarrierPolls polls sets *err, and a CTA
+// that sees *err set returns, so the launch always ends.
+constexpr uint32_t kBarrierPolls = 1u << 22;   // ~0.3 s at 64 ns per poll
+
+__device__ __forceinline__ bool slot_barrier(uint32_t *count, uint32_t target, int32_t *err, int *sh_ok)
+{
+    __syncthreads();   // the CTA's work of the phase is done
+    if (threadIdx.x == 0) {
+        __threadfence();   // ... and visible before the arrival
+        atomicAdd(count, 1u);
+        int ok = 1;
+        for (uint32_t polls = 0;; polls++) {
+            if (__ldcg(count) >= target) break;
+            if (__ldcg(err) != 0) {
+                ok = 0;
+                break;
+            }
+            if (polls >= kBarrierPolls) {
+                atomicExch(err, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        *sh_ok = ok;
+    }
+    __syncthreads();
+    return *sh_ok != 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kVecThreads) kb_persistent(const SlotDesc *slots, const int16_t *cta_slot, int iters,
+                                                             uint32_t *bar, int32_t *err)
+{
+    __shared__ double sh[2 * (kVecThreads >> 5)];
+    __shared__ int flag, ok;
+    const int s = cta_slot[blockIdx.x];
+    if (s < 0) return;
+    const SlotDesc *d = slots + s;
+    if (!d->active) return;
+    const Cta c{blockIdx.x - (uint32_t)d->c0, (uint32_t)(d->c1 - d->c0)};
+    PcgCtl *ctl = d->ctl;
+    uint32_t target = 0;
+    for (int it = 0; it < iters; it++) {
+        // the same for every CTA of the slot: written before the barrier they all passed
+        if (ctl_ld<true>(&ctl->done)) break;
+        sell_dir_body<2, T, true>(slot_A<T>(*d), slot_v<T>(*d), d->parts.pq, ctl, true, c);
+        target += c.n;
+        if (!slot_barrier(bar + s, target, err, &ok)) return;
+        update_body<T, true>(slot_v<T>(*d), d->n, d->parts, ctl, sh, &flag, c);
+        target += c.n;
+        if (!slot_barrier(bar + s, target, err, &ok)) return;
+    }
+}
+
 }  // namespace amie
 
 // ------------------------------------------------------------------ host side
@@ -134,6 +193,10 @@ struct amie_server {
     bool mixed = true;
     int grid = 0, group = 8;
     int rows_per_cta = 512;   // block rows per CTA of a slot
+    bool persistent = false;  // mixed batches as one cooperative launch (kb_persistent)
+    amie::DevArray<uint32_t> d_bar;   // per slot barrier counters of kb_persistent
+    amie::DevArray<int32_t> d_err;    // barrier timeout flag
+    int32_t *h_err = nullptr;         // pinned copy
     uint64_t budget = 0;
     std::atomic<uint64_t> in_use{0};
 
@@ -586,11 +649,38 @@ struct ServerOps {
             // 1. batch iterations in flight on the solve stream
             const bool active = any_active(srv);
             if (active) {
-                cudaGraphLaunch(srv->graph, srv->ctx->stream);
-                g_launches += (srv->mixed ? 2 : 3) * kBatchIters;
+                cudaStream_t st = srv->ctx->stream;
+                if (srv->persistent) {
+                    cudaMemsetAsync(srv->d_bar.p, 0, srv->slot_req.size() * sizeof(uint32_t), st);
+                    const SlotDesc *sl = srv->d_slots.p;
+                    const int16_t *cs = srv->d_cta_slot.p;
+                    int iters = kBatchIters;
+                    uint32_t *bar = srv->d_bar.p;
+                    int32_t *err = srv->d_err.p;
+                    void *args[] = {(void *)&sl, (void *)&cs, (void *)&iters, (void *)&bar, (void *)&err};
+                    const cudaError_t le = cudaLaunchCooperativeKernel((const void *)kb_persistent<float>,
+                                                                       dim3(srv->grid), dim3(kVecThreads), args, 0, st);
+                    if (le != cudaSuccess) {   // nothing ran: report and stop rather than wait on stale blocks
+                        srv->error = std::string("cooperative launch: ") + cudaGetErrorString(le);
+                        std::lock_guard<std::mutex> lk(srv->mu);
+                        for (auto &kv : srv->all)
+                            if (kv.second->status == AMIE_NOT_READY) {
+                                kv.second->status = AMIE_CUDA_ERROR;
+                                kv.second->t_done = now_s();
+                            }
+                        srv->stop_flag = true;
+                        srv->cv.notify_all();
+                        break;
+                    }
+                    g_launches += 1;
+                    cudaMemcpyAsync(srv->h_err, srv->d_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+                } else {
+                    cudaGraphLaunch(srv->graph, st);
+                    g_launches += (srv->mixed ? 2 : 3) * kBatchIters;
+                }
                 cudaMemcpyAsync(srv->h_ctl, srv->d_ctl.p, srv->slot_req.size() * sizeof(PcgCtl), cudaMemcpyDeviceToHost,
-                                srv->ctx->stream);
-                cudaEventRecord(srv->ctx->ev1, srv->ctx->stream);
+                                st);
+                cudaEventRecord(srv->ctx->ev1, st);
             }
             // 2. requests the admission thread has finished
             {
@@ -612,6 +702,18 @@ struct ServerOps {
             if (active) {
                 cudaEventSynchronize(srv->ctx->ev1);
                 t_waited = now_s();
+                if (srv->persistent && *srv->h_err) {   // a slot barrier timed out: stop serving
+                    srv->error = "persistent batch: slot barrier timed out";
+                    std::lock_guard<std::mutex> lk(srv->mu);
+                    for (auto &kv : srv->all)
+                        if (kv.second->status == AMIE_NOT_READY) {
+                            kv.second->status = AMIE_TIMEOUT;
+                            kv.second->t_done = now_s();
+                        }
+                    srv->stop_flag = true;
+                    srv->cv.notify_all();
+                    break;
+                }
                 std::vector<int> finished;
                 for (size_t i = 0; i < srv->slot_req.size(); i++) {
                     amie_server::Req *r = srv->slot_req[i];
@@ -703,7 +805,22 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
             lower((const void *)kb_update<double>);
             lower((const void *)kb_direction<double>);
         }
-        srv->grid = std::max(ctx->num_sms * occ, c.max_slots);
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+        // opt-in (AMIE_SERVER_PERSISTENT=1): one cooperative launch per batch.  Measured
+        // slower than the graph of batched kernels (145 vs 174 solves/s saturated, same
+        // 16 ms for a lone request): small slots are bound by dependent memory latency,
+        // not by launches, and the kernel's 128 registers leave 2 CTAs per SM.
+        srv->persistent = false;
+        if (const char *e = std::getenv("AMIE_SERVER_PERSISTENT"))
+            srv->persistent = srv->mixed && coop != 0 && std::atoi(e) != 0;
+        if (srv->persistent) {
+            int k = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, (const void *)kb_persistent<float>, kVecThreads, 0);
+            occ = std::max(1, std::min(occ, k));
+        }
+        // a cooperative launch needs every CTA resident: the grid cannot exceed occ per SM
+        srv->grid = srv->persistent ? ctx->num_sms * occ : std::max(ctx->num_sms * occ, c.max_slots);
         // tuning override for measurements: AMIE_SERVER_ROWS_PER_CTA
         if (const char *e = std::getenv("AMIE_SERVER_ROWS_PER_CTA")) {
             const int v = std::atoi(e);
@@ -724,15 +841,19 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
     srv->slot_req.assign(c.max_slots, nullptr);
     srv->h_norm_n.assign(c.max_slots, 0);
     if ((rc = srv->d_slots.alloc(ctx, c.max_slots)) || (rc = srv->d_ctl.alloc(ctx, c.max_slots)) ||
+        (rc = srv->d_bar.alloc(ctx, c.max_slots)) || (rc = srv->d_err.alloc(ctx, 1)) ||
         (rc = srv->d_cta_slot.alloc(ctx, srv->grid)) || (rc = srv->d_parts.alloc(ctx, 4 * (size_t)srv->grid)))
         return fail(rc);
     if (cudaMallocHost((void **)&srv->h_slots, c.max_slots * sizeof(SlotDesc)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_ctl, c.max_slots * sizeof(PcgCtl)) != cudaSuccess ||
+        cudaMallocHost((void **)&srv->h_err, sizeof(int32_t)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_norm, (size_t)c.max_slots * kNormParts * sizeof(double)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_cta_slot, srv->grid * sizeof(int16_t)) != cudaSuccess)
         return fail(AMIE_OOM);
     std::memset(srv->h_slots, 0, c.max_slots * sizeof(SlotDesc));
     std::memset(srv->h_ctl, 0, c.max_slots * sizeof(PcgCtl));
+    *srv->h_err = 0;
+    cudaMemsetAsync(srv->d_err.p, 0, sizeof(int32_t), ctx->stream);
     for (int i = 0; i < srv->grid; i++) srv->h_cta_slot[i] = -1;
     cudaStream_t st = ctx->stream;
     cudaMemcpyAsync(srv->d_slots.p, srv->h_slots, c.max_slots * sizeof(SlotDesc), cudaMemcpyHostToDevice, st);
@@ -888,10 +1009,13 @@ extern "C" amie_status amie_server_stop(amie_server *srv)
     if (srv->graph) cudaGraphExecDestroy(srv->graph);
     if (srv->h_slots) cudaFreeHost(srv->h_slots);
     if (srv->h_ctl) cudaFreeHost(srv->h_ctl);
+    if (srv->h_err) cudaFreeHost(srv->h_err);
     if (srv->h_norm) cudaFreeHost(srv->h_norm);
     if (srv->h_cta_slot) cudaFreeHost(srv->h_cta_slot);
     srv->d_slots.release();
     srv->d_ctl.release();
+    srv->d_bar.release();
+    srv->d_err.release();
     srv->d_cta_slot.release();
     srv->d_parts.release();
     amie_ctx_destroy(srv->adm);

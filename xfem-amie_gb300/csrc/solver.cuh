@@ -232,6 +232,32 @@ __device__ __forceinline__ void load_x(const T *__restrict__ x, uint32_t c, T xv
     }
 }
 
+// load_x through L2 only (ld.global.cg): for vectors other CTAs of a running
+// persistent kernel rewrite between its phases (an SM's L1 is not coherent
+// with the others' stores).
+template <int S, typename T>
+__device__ __forceinline__ void load_x_cg(const T *x, uint32_t c, T xv[S])
+{
+    if constexpr (S == 2) {
+        using V = typename Vec2<T>::type;
+        const V a = __ldcg(reinterpret_cast<const V *>(x + (uint64_t)c * 2));
+        xv[0] = a.x; xv[1] = a.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < S; q++) xv[q] = __ldcg(x + (uint64_t)c * S + q);
+    }
+}
+
+// A control-block field: inside a persistent kernel (CG) written by other CTAs
+// during the launch, so read through L2; otherwise a plain load (the writer
+// was an earlier kernel).
+template <bool CG, typename F>
+__device__ __forceinline__ F ctl_ld(const F *p)
+{
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+}
+
 constexpr int kSpmvUnroll = 4;
 
 // y = A x over a group of G lanes per block row; acc in the precision of T.
@@ -278,7 +304,7 @@ __device__ __forceinline__ void row_spmv(const BsrView<T> &A, const T *__restric
 }
 
 // Per-CTA partial of p.q; with `fin`, the last CTA stores pq and alpha = rz / pq.
-template <typename T>
+template <typename T, bool CG = false>
 __device__ __forceinline__ void finish_pq(T dot_t, double *part_pq, PcgCtl *fin, double *sh, int *flag, Cta c)
 {
     const double dot = block_sum_v<T>(dot_t, sh);
@@ -288,7 +314,7 @@ __device__ __forceinline__ void finish_pq(T dot_t, double *part_pq, PcgCtl *fin,
     const double pq = ordered_sum(part_pq, c.n, sh);
     if (threadIdx.x == 0) {
         fin->pq = pq;
-        fin->alpha = pq != 0.0 ? fin->rz / pq : 0.0;
+        fin->alpha = pq != 0.0 ? ctl_ld<CG>(&fin->rz) / pq : 0.0;
         fin->ticket = 0;
     }
 }
@@ -549,7 +575,7 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
 // launch).  The single-solve kernel below is kept as its own copy: with the
 // group position and the views held as values the compiler keeps fewer loads in
 // flight at the kernel's 64-register budget (49 us instead of 33 us on cfg1).
-template <int S, typename T>
+template <int S, typename T, bool CG = false>
 __device__ __forceinline__ void sell_dir_body(const SellView<T> &A, const PcgVecs<T> &v, double *part_pq, PcgCtl *ctl,
                                               bool fin, Cta cta)
 {
@@ -559,8 +585,8 @@ __device__ __forceinline__ void sell_dir_body(const SellView<T> &A, const PcgVec
     constexpr int U = kSpmvUnroll;
     constexpr uint32_t WPB = kVecThreads / 32;
     const uint32_t lane = threadIdx.x & 31;
-    const T bt = (T)ctl->beta;
-    const bool second = ctl->pcur != 0;
+    const T bt = (T)ctl_ld<CG>(&ctl->beta);
+    const bool second = ctl_ld<CG>(&ctl->pcur) != 0;
     const T *__restrict__ pold = second ? v.p2 : v.p;
     T *__restrict__ pnew = second ? v.p : v.p2;
     const T *__restrict__ z = v.z;
@@ -583,8 +609,13 @@ __device__ __forceinline__ void sell_dir_body(const SellView<T> &A, const PcgVec
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 if (j0 + u < len) {
-                    load_x<S, T>(z, c[u], zv[u]);
-                    load_x<S, T>(pold, c[u], pv[u]);
+                    if constexpr (CG) {
+                        load_x_cg<S, T>(z, c[u], zv[u]);
+                        load_x_cg<S, T>(pold, c[u], pv[u]);
+                    } else {
+                        load_x<S, T>(z, c[u], zv[u]);
+                        load_x<S, T>(pold, c[u], pv[u]);
+                    }
                 }
             }
 #pragma unroll
@@ -603,7 +634,7 @@ __device__ __forceinline__ void sell_dir_body(const SellView<T> &A, const PcgVec
 #pragma unroll
             for (int r = 0; r < S; r++) {
                 const uint64_t i = (uint64_t)row * S + r;
-                const T pn = fma(bt, pold[i], z[i]);
+                const T pn = CG ? fma(bt, __ldcg(pold + i), __ldcg(z + i)) : fma(bt, pold[i], z[i]);
                 pnew[i] = pn;
                 q[i] = acc[r];
                 dot = fma(acc[r], pn, dot);
@@ -619,7 +650,7 @@ __device__ __forceinline__ void sell_dir_body(const SellView<T> &A, const PcgVec
     __syncthreads();
     T dot = T(0);
     for (uint32_t i = s_beg + threadIdx.x; i < s_end; i += kVecThreads) dot += A.slice_dot[i];
-    finish_pq<T>(dot, part_pq, fin ? ctl : nullptr, sh, &flag, cta);
+    finish_pq<T, CG>(dot, part_pq, fin ? ctl : nullptr, sh, &flag, cta);
 }
 
 
@@ -841,6 +872,22 @@ __device__ __forceinline__ void ldg_pack(const T *__restrict__ p, uint64_t i, T 
     }
 }
 
+// A pack another CTA may have written during a running persistent kernel
+// (CG: through L2 only), else through the read-only path.
+template <typename T, bool CG>
+__device__ __forceinline__ void ldq_pack(const T *p, uint64_t i, T (&o)[Pack<T>::n])
+{
+    if constexpr (!CG) {
+        ldg_pack<T>(p, i, o);
+    } else if constexpr (sizeof(T) == 4) {
+        const float4 a = __ldcg(reinterpret_cast<const float4 *>(p) + i);
+        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    } else {
+        const double2 a = __ldcg(reinterpret_cast<const double2 *>(p) + i);
+        o[0] = a.x; o[1] = a.y;
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void st_pack(T *p, uint64_t i, const T (&o)[Pack<T>::n])
 {
@@ -870,17 +917,17 @@ __device__ __forceinline__ void for_entries(uint64_t n, bool aligned, Cta cta, F
 // Last CTA: totals, iteration count, stop test, beta = rz_new / rz.  Each
 // thread handles two 16-byte packs per step with all ten loads issued before
 // any arithmetic (one memory round trip per step).
-template <typename T>
+template <typename T, bool CG = false>
 __device__ __forceinline__ void update_body(const PcgVecs<T> &v, uint64_t n, const PcgParts &parts, PcgCtl *ctl,
                                             double *sh, int *flag, Cta cta)
 {
     constexpr int W = Pack<T>::n;
-    const T a = (T)ctl->alpha;
+    const T a = (T)ctl_ld<CG>(&ctl->alpha);
     T *__restrict__ x = v.x;
     T *__restrict__ r = v.r;
     T *__restrict__ z = v.z;
     // with two direction buffers the SpMV just wrote this iteration's p into the other one
-    const T *__restrict__ p = v.p2 ? (ctl->pcur ? v.p : v.p2) : v.p;
+    const T *__restrict__ p = v.p2 ? (ctl_ld<CG>(&ctl->pcur) ? v.p : v.p2) : v.p;
     const T *__restrict__ q = v.q;
     const T *__restrict__ d = v.dinv;
     T drz = T(0), drr = T(0);   // per-thread partials in the vector precision, CTA sums in FP64
@@ -893,15 +940,15 @@ __device__ __forceinline__ void update_body(const PcgVecs<T> &v, uint64_t n, con
         const bool two = k2 < npk;   // the second pack of the step exists
         T rv[2][W], qv[2][W], xv[2][W], pv[2][W], dv[2][W];
         ld_pack<T>(r, k, rv[0]);
-        ldg_pack<T>(q, k, qv[0]);
+        ldq_pack<T, CG>(q, k, qv[0]);
         ld_pack<T>(x, k, xv[0]);
-        ldg_pack<T>(p, k, pv[0]);
+        ldq_pack<T, CG>(p, k, pv[0]);
         ldg_pack<T>(d, k, dv[0]);
         if (two) {
             ld_pack<T>(r, k2, rv[1]);
-            ldg_pack<T>(q, k2, qv[1]);
+            ldq_pack<T, CG>(q, k2, qv[1]);
             ld_pack<T>(x, k2, xv[1]);
-            ldg_pack<T>(p, k2, pv[1]);
+            ldq_pack<T, CG>(p, k2, pv[1]);
             ldg_pack<T>(d, k2, dv[1]);
         }
 #pragma unroll
@@ -923,8 +970,10 @@ __device__ __forceinline__ void update_body(const PcgVecs<T> &v, uint64_t n, con
         }
     }
     for (uint64_t i = npk * W + tid; i < n; i += stride) {   // tail, or everything when not aligned
-        const T ri = r[i] - a * q[i];
-        x[i] = fma(a, p[i], x[i]);
+        const T qi = CG ? __ldcg(q + i) : q[i];
+        const T pi = CG ? __ldcg(p + i) : p[i];
+        const T ri = r[i] - a * qi;
+        x[i] = fma(a, pi, x[i]);
         r[i] = ri;
         const T zi = ri * d[i];
         z[i] = zi;
@@ -941,18 +990,19 @@ __device__ __forceinline__ void update_body(const PcgVecs<T> &v, uint64_t n, con
     double rz_new, rr;
     ordered_sum2(parts.rz, parts.rr, cta.n, sh, rz_new, rr);
     if (threadIdx.x == 0) {
-        const int64_t it = ctl->iterations + 1;
+        const int64_t it = ctl_ld<CG>(&ctl->iterations) + 1;
+        const double rz_old = ctl_ld<CG>(&ctl->rz);
         ctl->iterations = it;
         ctl->rr = rr;
-        ctl->rz_prev = ctl->rz;
-        const bool stop = rr <= ctl->tol2 || it >= ctl->maxit || !(rr == rr);
+        ctl->rz_prev = rz_old;
+        const bool stop = rr <= ctl_ld<CG>(&ctl->tol2) || it >= ctl_ld<CG>(&ctl->maxit) || !(rr == rr);
         if (stop) {
             ctl->done = 1;
         } else {
-            ctl->beta = ctl->rz != 0.0 ? rz_new / ctl->rz : 0.0;
+            ctl->beta = rz_old != 0.0 ? rz_new / rz_old : 0.0;
         }
         ctl->rz = rz_new;
-        if (v.p2) ctl->pcur ^= 1;   // this iteration's p is now the latest
+        if (v.p2) ctl->pcur = ctl_ld<CG>(&ctl->pcur) ^ 1;   // this iteration's p is now the latest
         ctl->ticket = 0;
     }
 }
