@@ -144,3 +144,31 @@ def test_imposed_strain_known_answer():
     C = m.cmat_table.reshape(-1, 3, 3)[m.mat]
     real = sig - np.einsum("eij,ej->ei", C, eps0)
     assert np.abs(real).max() / 1e6 <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["crack_p1", "crack_p2"])
+def test_cut_rules_reproduce_reference_element_matrices(name):
+    """The restated sub-triangulation rules of the crack's Heaviside elements:
+    where the reference integrated with its sub-triangles, the same number of
+    points and K_e to 1e-9 (its Heaviside gradients are finite differences);
+    where it fell back to 512 random points, a Monte-Carlo or order-dependent
+    status."""
+    import crack_cases as CC
+    import cut_rules as CR
+    d = load_golden(name)
+    m = am.from_golden(d, "auto")
+    elems = CC.heaviside_elements(m)
+    count, status, rule, hp, hv = CR.cut_rules(CC.corners(d, m, elems), CC.crack_line(d))
+    ngp = np.diff(m.gp_ptr.astype(np.int64))[elems]
+    mc = ngp == 512
+    assert np.all(np.isin(status[mc], (CR.MONTE_CARLO, CR.ORDER_DEPENDENT)))
+    assert np.all(status[~mc] == CR.OK) and np.array_equal(count[~mc], ngp[~mc])
+    ok = np.nonzero(status == CR.OK)[0]
+    assert len(ok) == {"crack_p1": 17, "crack_p2": 9}[name]
+    sub = CC.submesh(m, elems[ok], count[ok], rule[ok], hp[ok], hv[ok])
+    off, ke = O.element_matrices(sub)
+    for i, e in enumerate(elems[ok]):
+        assert rel(ke[off[i]:off[i + 1]], CC.golden_ke(d, e)) <= 1e-9, e
+    # weights add up to the element's area
+    area = np.array([sub.gp[3 * sub.gp_ptr[i] + 2:3 * sub.gp_ptr[i + 1]:3].sum() for i in range(len(ok))])
+    assert rel(area, np.array([m.gp[3 * m.gp_ptr[e] + 2:3 * m.gp_ptr[e + 1]:3].sum() for e in elems[ok]])) <= 1e-12

@@ -35,7 +35,7 @@ EXPORTED = [
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
     "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step", "amie_pcg_solve_noalloc",
     "amie_topology_spmv_lanes", "amie_profile_stream", "amie_average_field", "amie_set_imposed_strain",
-    "amie_server_query",
+    "amie_server_query", "amie_cut_rules",
 ]
 
 
@@ -43,6 +43,9 @@ class ServerStats(C.Structure):
     _fields_ = [("admit_s", C.c_double), ("wait_s", C.c_double), ("advance_s", C.c_double), ("join_s", C.c_double),
                 ("loop_s", C.c_double), ("batches", C.c_uint64), ("admitted", C.c_uint64)]
 FIELD_STRAIN, FIELD_STRESS = 0, 1
+# amie_cut_rules: points per element at most, and the per-element status codes
+CUT_MAX_POINTS = 52
+CUT_OK, CUT_NOT_CUT, CUT_MONTE_CARLO, CUT_ORDER_DEPENDENT, CUT_TOO_MANY_HINTS = 0, 1, 2, 3, 4
 
 
 class DamageParams(C.Structure):
@@ -156,6 +159,22 @@ class Context:
 
     def timer_start(self):
         check(lib().amie_timer_start(self.ptr), "amie_timer_start")
+
+    def cut_rules(self, corners, line):
+        """Rules of triangles crossed by the crack polyline `line` [(x, y), ...]:
+        (count [n], status [n], rule [n, CUT_MAX_POINTS, 3], h_point [n, CUT_MAX_POINTS], h_vertex [n, 3])."""
+        c = np.ascontiguousarray(corners, np.float64).reshape(-1, 6)
+        ln = np.ascontiguousarray(line, np.float64).reshape(-1, 2)
+        n = c.shape[0]
+        cnt = np.zeros(n, np.uint32)
+        status = np.zeros(n, np.int8)
+        rule = np.zeros((n, CUT_MAX_POINTS, 3), np.float64)
+        hp = np.zeros((n, CUT_MAX_POINTS), np.int8)
+        hv = np.zeros((n, 3), np.int8)
+        check(lib().amie_cut_rules(self.ptr, C.c_uint32(n), _p(c), C.c_uint32(ln.shape[0]), _p(ln), _p(cnt),
+                                   _p(status), _p(rule), _p(hp), _p(hv)), "amie_cut_rules")
+        return cnt, status, rule, hp, hv
+        return cnt, rule, side
 
     def profile_stream(self, nbytes: int, reps: int = 10) -> float:
         """Milliseconds of one plain streaming read of `nbytes` (L2 evicted before each launch)."""

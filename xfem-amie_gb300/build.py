@@ -17,7 +17,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libamie_gpu.so")
-SOURCES = ["common.cu", "assemble.cu", "solver.cu", "fields.cu", "noalloc.cu"]
+SOURCES = ["common.cu", "assemble.cu", "solver.cu", "fields.cu", "noalloc.cu", "cut_rules.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I", os.path.join(REPO, "include"), "-I", CSRC]
