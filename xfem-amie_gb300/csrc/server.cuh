@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kVecThreads) kb_sell_pq(const SlotDesc *slots,
     const SlotDesc *d = slot_of(slots, cta_slot, &c);
     if (!d) return;
     const PcgVecs<T> &v = slot_v<T>(*d);
-    sell_pq_body<2, kSpmvUnroll, false, T>(slot_A<T>(*d), v.p, v.q, d->parts.pq, d->ctl, sh, &flag, &next_sl, c);
+    sell_pq_body<2, kSpmvUnroll, false, T, 0>(slot_A<T>(*d), v.p, v.q, d->parts.pq, d->ctl, sh, &flag, &next_sl, c);
 }
 
 // Batched kernel B: per slot x, r, z updates, r.z, r.r; last CTA of the slot:

@@ -24,6 +24,20 @@ amie_status assemble_async(amie_topo *t);
 amie_status finalize_matrix_async(amie_topo *t, bool want32);
 amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *st);
 
+// k_sell_dir instance for the stride and the matrix-stream hint
+template <typename T>
+const void *sell_dir_kernel(int s, int hint)
+{
+    if (s == 2) {
+        if (hint == 1) return (const void *)k_sell_dir<2, T, 1>;
+        if (hint == 2) return (const void *)k_sell_dir<2, T, 2>;
+        return (const void *)k_sell_dir<2, T, 0>;
+    }
+    if (hint == 1) return (const void *)k_sell_dir<3, T, 1>;
+    if (hint == 2) return (const void *)k_sell_dir<3, T, 2>;
+    return (const void *)k_sell_dir<3, T, 0>;
+}
+
 struct SolverState {
     int grid = 0;                 // block-CSR SpMV, AMIE_CG and server kernels
     int grid_vec[2] = {0, 0};     // PCG vector kernels, FP32 / FP64 (resident CTAs of k_update)
@@ -36,6 +50,9 @@ struct SolverState {
     // gathered entry instead of one per vector entry, and FP64 issue is the
     // scarce resource of this GPU (the folded FP64 solve ran 1.4x slower)
     bool fold_dir = true;
+    // L2 eviction hint of the matrix stream in k_sell_dir (see ld_stream);
+    // AMIE_MATRIX_HINT overrides it for measurements
+    int matrix_hint = kMatrixHint;
     int graph_kernels[2] = {3, 3};   // kernels per iteration of the FP32 / FP64 graph
     DevArray<double> parts;       // 4 * stride: pq, rz, rr, spare
     DevArray<PcgCtl> ctl;
@@ -251,8 +268,9 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         s->grid_sell[1] = resident(k64, sm64);
         s->grid_vec[0] = resident((const void *)k_update<float>, 0);
         s->grid_vec[1] = resident((const void *)k_update<double>, 0);
-        s->grid_dir[0] = resident(t->s == 2 ? (const void *)k_sell_dir<2, float> : (const void *)k_sell_dir<3, float>, 0);
-        s->grid_dir[1] = resident(t->s == 2 ? (const void *)k_sell_dir<2, double> : (const void *)k_sell_dir<3, double>, 0);
+        if (const char *e = std::getenv("AMIE_MATRIX_HINT")) s->matrix_hint = std::min(2, std::max(0, std::atoi(e)));
+        s->grid_dir[0] = resident(sell_dir_kernel<float>(t->s, s->matrix_hint), 0);
+        s->grid_dir[1] = resident(sell_dir_kernel<double>(t->s, s->matrix_hint), 0);
         AMIE_CUDA(cudaGetLastError());
         AMIE_TRY(ensure_sell_partition(t, s->grid));
         AMIE_TRY(ensure_sell_partition(t, s->grid_sell[0]));
@@ -316,14 +334,14 @@ PcgVecs<float> vecs_of<float>(amie_topo *t)
 // k_sell_dir); false when the SELL copy or the CTA table for `grid` is missing.
 template <typename T>
 bool launch_spmv_dir(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, PcgCtl *ctl, bool fin,
-                     cudaStream_t st, bool pdl)
+                     cudaStream_t st, bool pdl, int hint)
 {
     SellView<T> sv = sell_of<T>(t);
     auto it = t->sell_cta_first.find(grid);
     if (!sv.val || it == t->sell_cta_first.end() || !v.p2) return false;
     sv.cta_first = it->second.p;
-    if (t->s == 2) launch_k(pdl, k_sell_dir<2, T>, grid, 0, st, sv, v, part, ctl, fin ? 1 : 0);
-    else launch_k(pdl, k_sell_dir<3, T>, grid, 0, st, sv, v, part, ctl, fin ? 1 : 0);
+    auto kern = (void (*)(SellView<T>, PcgVecs<T>, double *, PcgCtl *, int))sell_dir_kernel<T>(t->s, hint);
+    launch_k(pdl, kern, grid, 0, st, sv, v, part, ctl, fin ? 1 : 0);
     AMIE_LAUNCHED();
     return true;
 }
@@ -337,7 +355,7 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     cudaStream_t st = t->ctx->stream;
     PcgVecs<T> v = vecs_of<T>(t);
     PcgParts parts = parts_of(s);
-    cudaGraph_t graph;
+    cudaGraph_t graph = nullptr;
     AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     const int pi = sizeof(T) == 8 ? 1 : 0;
     const int gs = s->grid_sell[pi];
@@ -349,7 +367,7 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     for (int it = 0; it < kGraphIters; it++) {
         // the first kernel follows the previous graph launch in plain stream order
         if (fold<T>(s)) {
-            launch_spmv_dir<T>(t, gd, v, parts.pq, ctl, true, st, s->pdl && it > 0);
+            launch_spmv_dir<T>(t, gd, v, parts.pq, ctl, true, st, s->pdl && it > 0, s->matrix_hint);
             launch_k(s->pdl, k_update<T>, gv, 0, st, v, n, parts, ctl);
         } else {
             PcgVecs<T> v1 = v;
@@ -681,7 +699,8 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     for (int i = 0; i <= reps; i++) {   // launch 0 is a warm-up
         if (i == 1) AMIE_CUDA(cudaEventRecord(t->ctx->ev0, st));
         if (precision == 32 && fold<float>(s)) {
-            launch_spmv_dir<float>(t, s->grid_dir[pi], vecs_of<float>(t), parts.pq, s->ctl.p, false, st, false);
+            launch_spmv_dir<float>(t, s->grid_dir[pi], vecs_of<float>(t), parts.pq, s->ctl.p, false, st, false,
+                                   s->matrix_hint);
         } else {
             if (precision == 64) launch_spmv_pq<double>(t, s->grid_sell[pi], vecs_of<double>(t), parts.pq, nullptr, nullptr, st);
             else launch_spmv_pq<float>(t, s->grid_sell[pi], vecs_of<float>(t), parts.pq, nullptr, nullptr, st);

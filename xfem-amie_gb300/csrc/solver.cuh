@@ -22,6 +22,8 @@
 
 #include "internal.h"
 
+#include <type_traits>
+
 namespace amie {
 
 constexpr int kVecThreads = 256;
@@ -357,35 +359,79 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv_pq(PcgVecs<T> v, double *p
     finish_pq<T>(dot, part_pq, fin, sh, &flag, grid_cta());
 }
 
+// Matrix-stream loads with an L2 eviction hint.  HINT 0: plain read-only
+// loads; 1: ld.global.cs (lines allocated evict-first in L1 and L2); 2: an L2
+// evict-first access policy (createpolicy).  The matrix is read once per
+// iteration and is larger than L2, so without a hint it pushes the iteration's
+// vectors out of L2.  Measured on the 1.2 M-DOF P2 problem (FP32 matrix 150 MB,
+// vectors 29 MB): the SpMV+direction kernel takes 32.1 us with 0, 26.7 us
+// with 1 (the vector gathers and the next kernel's reads stay in L2) and
+// 45 us with 2; 1 is the default everywhere.
+constexpr int kMatrixHint = 1;
+template <int HINT>
+__device__ __forceinline__ uint64_t stream_policy()
+{
+    uint64_t pol = 0;
+    if constexpr (HINT == 2) asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+template <int HINT, typename V>
+__device__ __forceinline__ V ld_stream(const V *p, uint64_t pol)
+{
+    if constexpr (HINT == 1) {
+        return __ldcs(p);
+    } else if constexpr (HINT == 2) {
+        V v;
+        if constexpr (sizeof(V) == 16 && std::is_same_v<V, float4>)
+            asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                         : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p), "l"(pol));
+        else if constexpr (std::is_same_v<V, double2>)
+            asm volatile("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+                         : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(pol));
+        else if constexpr (std::is_same_v<V, float>)
+            asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+        else if constexpr (std::is_same_v<V, double>)
+            asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
+        else
+            asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+        return v;
+    } else {
+        return __ldg(p);
+    }
+}
+
 // One s x s block of the lane's row from a 32-slot SELL group (chunked layout).
-template <int S, typename T>
-__device__ __forceinline__ void load_sell_block(const T *__restrict__ group, uint32_t lane, T blk[S * S])
+template <int S, typename T, int HINT = kMatrixHint>
+__device__ __forceinline__ void load_sell_block(const T *__restrict__ group, uint32_t lane, T blk[S * S],
+                                                uint64_t pol = 0)
 {
     constexpr int V = kSellVec<S, T>;
     if constexpr (S == 2 && V == 4) {
-        const float4 a = __ldg(reinterpret_cast<const float4 *>(group) + lane);
+        const float4 a = ld_stream<HINT>(reinterpret_cast<const float4 *>(group) + lane, pol);
         blk[0] = a.x; blk[1] = a.y; blk[2] = a.z; blk[3] = a.w;
     } else if constexpr (S == 2 && V == 2) {
-        const double2 a = __ldg(reinterpret_cast<const double2 *>(group) + lane);
-        const double2 b = __ldg(reinterpret_cast<const double2 *>(group + 64) + lane);
+        const double2 a = ld_stream<HINT>(reinterpret_cast<const double2 *>(group) + lane, pol);
+        const double2 b = ld_stream<HINT>(reinterpret_cast<const double2 *>(group + 64) + lane, pol);
         blk[0] = a.x; blk[1] = a.y; blk[2] = b.x; blk[3] = b.y;
     } else {
 #pragma unroll
-        for (int c = 0; c < S * S; c++) blk[c] = __ldg(group + 32 * c + lane);
+        for (int c = 0; c < S * S; c++) blk[c] = ld_stream<HINT>(group + 32 * c + lane, pol);
     }
 }
 
 // Columns and blocks of slots j0 .. j0+U-1 of the lane's row (those < len).
-template <int S, int U, typename T>
+template <int S, int U, typename T, int HINT = kMatrixHint>
 __device__ __forceinline__ void load_sell_group(const SellView<T> &A, uint64_t g0, uint32_t j0, uint32_t len,
-                                                uint32_t lane, uint32_t (&c)[U], T (&blk)[U][S * S])
+                                                uint32_t lane, uint32_t (&c)[U], T (&blk)[U][S * S],
+                                                uint64_t pol = 0)
 {
 #pragma unroll
     for (int u = 0; u < U; u++) {
         if (j0 + u < len) {   // uniform over the warp
             const uint64_t gs = g0 + (uint64_t)(j0 + u) * 32;
-            c[u] = __ldg(A.col + gs + lane);
-            load_sell_block<S, T>(A.val + gs * (S * S), lane, blk[u]);
+            c[u] = ld_stream<HINT>(A.col + gs + lane, pol);
+            load_sell_block<S, T, HINT>(A.val + gs * (S * S), lane, blk[u], pol);
         }
     }
 }
@@ -404,7 +450,7 @@ __device__ __forceinline__ void load_sell_group(const SellView<T> &A, uint64_t g
 // block-CSR row with the same FMA sequence as row_spmv with one lane per row,
 // so q is bitwise that of k_spmv_pq<S,1,T>.
 // MINB (2x2 FP32 blocks only) asks the compiler for MINB resident CTAs per SM.
-template <int S, int U, bool PIPE, typename T>
+template <int S, int U, bool PIPE, typename T, int HINT = kMatrixHint>
 __device__ __forceinline__ void sell_pq_body(const SellView<T> &A, const T *__restrict__ x, T *__restrict__ y,
                                              double *part_pq, PcgCtl *fin, double *sh, int *flag, uint32_t *next_sl,
                                              Cta cta)
@@ -424,16 +470,16 @@ __device__ __forceinline__ void sell_pq_body(const SellView<T> &A, const T *__re
         for (int r = 0; r < S; r++) acc[r] = T(0);
         uint32_t c[U];
         T blk[U][S * S];
-        if constexpr (PIPE) load_sell_group<S, U, T>(A, g0, 0, len, lane, c, blk);
+        if constexpr (PIPE) load_sell_group<S, U, T, HINT>(A, g0, 0, len, lane, c, blk);
         for (uint32_t j0 = 0; j0 < len; j0 += U) {
-            if constexpr (!PIPE) load_sell_group<S, U, T>(A, g0, j0, len, lane, c, blk);
+            if constexpr (!PIPE) load_sell_group<S, U, T, HINT>(A, g0, j0, len, lane, c, blk);
             T xv[U][S];
 #pragma unroll
             for (int u = 0; u < U; u++)
                 if (j0 + u < len) load_x<S, T>(x, c[u], xv[u]);
             uint32_t cn[U];
             T bn[U][S * S];
-            if constexpr (PIPE) load_sell_group<S, U, T>(A, g0, j0 + U, len, lane, cn, bn);
+            if constexpr (PIPE) load_sell_group<S, U, T, HINT>(A, g0, j0 + U, len, lane, cn, bn);
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 if (j0 + u < len) {
@@ -495,7 +541,7 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
 // pq and alpha.  p_old / p_new are chosen by ctl->pcur (flipped by k_update),
 // so a graph of iterations needs no copies.  Same scheduling, FMA order and
 // fixed-order dot as k_sell_pq; p_new equals k_direction's fma(beta, p, z).
-template <int S, typename T>
+template <int S, typename T, int HINT = kMatrixHint>
 __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs<T> v, double *part_pq, PcgCtl *ctl,
                                                           int fin)
 {
@@ -515,6 +561,7 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
     const T *__restrict__ z = v.z;
     T *__restrict__ q = v.q;
     const uint32_t s_beg = __ldg(A.cta_first + blockIdx.x), s_end = __ldg(A.cta_first + blockIdx.x + 1);
+    const uint64_t pol = stream_policy<HINT>();
     if (threadIdx.x == 0) next_sl = s_beg + WPB;
     __syncthreads();
     for (uint32_t sl = s_beg + (threadIdx.x >> 5); sl < s_end;) {
@@ -527,7 +574,7 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
         uint32_t c[U];
         T blk[U][S * S];
         for (uint32_t j0 = 0; j0 < len; j0 += U) {
-            load_sell_group<S, U, T>(A, g0, j0, len, lane, c, blk);
+            load_sell_group<S, U, T, HINT>(A, g0, j0, len, lane, c, blk, pol);
             T zv[U][S], pv[U][S];
 #pragma unroll
             for (int u = 0; u < U; u++) {
@@ -572,7 +619,9 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
 }
 
 // k_sell_dir for a group of CTAs given explicitly (one slot's CTAs in a batched
-// launch).  The single-solve kernel below is kept as its own copy: with the
+// launch; plain matrix loads: a batch's small matrices are re-read every
+// iteration from L2, and evict-first lines there raised the serving p99 from
+// 0.28 s to 0.45 s).  The single-solve kernel below is kept as its own copy: with the
 // group position and the views held as values the compiler keeps fewer loads in
 // flight at the kernel's 64-register budget (49 us instead of 33 us on cfg1).
 template <int S, typename T, bool CG = false>
@@ -604,7 +653,7 @@ __device__ __forceinline__ void sell_dir_body(const SellView<T> &A, const PcgVec
         uint32_t c[U];
         T blk[U][S * S];
         for (uint32_t j0 = 0; j0 < len; j0 += U) {
-            load_sell_group<S, U, T>(A, g0, j0, len, lane, c, blk);
+            load_sell_group<S, U, T, 0>(A, g0, j0, len, lane, c, blk);
             T zv[U][S], pv[U][S];
 #pragma unroll
             for (int u = 0; u < U; u++) {
@@ -1007,15 +1056,135 @@ __device__ __forceinline__ void update_body(const PcgVecs<T> &v, uint64_t n, con
     }
 }
 
+// Kernel B of a single solve: update_body's work with its fixed latencies cut.
+// The loads of the thread's first step that the SpMV does not produce (x and r,
+// last written by the previous update, which finished before the SpMV could
+// start; D^-1) are issued before the wait on the SpMV; done, alpha and the
+// direction buffer are read in one round; the last CTA fetches the control
+// fields together with the partials.  FP32 asks for four resident CTAs per SM
+// (FP64 three), so that on the grid of resident CTAs one FP32 step covers
+// 1.2 M entries.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) k_update(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl)
+__global__ void __launch_bounds__(kVecThreads, sizeof(T) == 4 ? 4 : 3)
+    k_update(PcgVecs<T> v, uint64_t n, PcgParts parts, PcgCtl *ctl)
 {
     __shared__ double sh[2 * (kVecThreads >> 5)];
     __shared__ int flag;
+    constexpr int W = Pack<T>::n;
+    T *__restrict__ x = v.x;
+    T *__restrict__ r = v.r;
+    T *__restrict__ z = v.z;
+    const T *__restrict__ q = v.q;
+    const T *__restrict__ d = v.dinv;
+    const bool al = aligned16(x) && aligned16(r) && aligned16(z) && aligned16(v.p) && aligned16(q) &&
+                    aligned16(d) && (!v.p2 || aligned16(v.p2));
+    const uint64_t tid = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x;
+    const uint64_t stride = (uint64_t)gridDim.x * kVecThreads;
+    const uint64_t npk = al ? n / W : 0;
+    T rv[2][W], xv[2][W], dv[2][W];
+    if (tid < npk) {
+        ld_pack<T>(r, tid, rv[0]);
+        ld_pack<T>(x, tid, xv[0]);
+        ldg_pack<T>(d, tid, dv[0]);
+        if (tid + stride < npk) {
+            ld_pack<T>(r, tid + stride, rv[1]);
+            ld_pack<T>(x, tid + stride, xv[1]);
+            ldg_pack<T>(d, tid + stride, dv[1]);
+        }
+    }
     pdl_wait();
     pdl_release();
-    if (ctl->done) return;
-    update_body<T>(v, n, parts, ctl, sh, &flag, grid_cta());
+    const int32_t done = ctl->done;
+    const T a = (T)ctl->alpha;
+    const int32_t pcur = ctl->pcur;
+    if (done) return;
+    // with two direction buffers the SpMV just wrote this iteration's p into the other one
+    const T *__restrict__ p = v.p2 ? (pcur ? v.p : v.p2) : v.p;
+    T drz = T(0), drr = T(0);   // per-thread partials in the vector precision, CTA sums in FP64
+    for (uint64_t k = tid; k < npk; k += 2 * stride) {
+        const uint64_t k2 = k + stride;
+        const bool two = k2 < npk;   // the second pack of the step exists
+        T qv[2][W], pv[2][W];
+        if (k != tid) {
+            ld_pack<T>(r, k, rv[0]);
+            ld_pack<T>(x, k, xv[0]);
+            ldg_pack<T>(d, k, dv[0]);
+            if (two) {
+                ld_pack<T>(r, k2, rv[1]);
+                ld_pack<T>(x, k2, xv[1]);
+                ldg_pack<T>(d, k2, dv[1]);
+            }
+        }
+        ld_pack<T>(q, k, qv[0]);
+        ld_pack<T>(p, k, pv[0]);
+        if (two) {
+            ld_pack<T>(q, k2, qv[1]);
+            ld_pack<T>(p, k2, pv[1]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (h == 1 && !two) break;
+            T zv[W];
+#pragma unroll
+            for (int c = 0; c < W; c++) {
+                rv[h][c] = rv[h][c] - a * qv[h][c];
+                xv[h][c] = fma(a, pv[h][c], xv[h][c]);
+                zv[c] = rv[h][c] * dv[h][c];
+                drz = fma(rv[h][c], zv[c], drz);
+                drr = fma(rv[h][c], rv[h][c], drr);
+            }
+            const uint64_t kk = h ? k2 : k;
+            st_pack<T>(r, kk, rv[h]);
+            st_pack<T>(x, kk, xv[h]);
+            st_pack<T>(z, kk, zv);
+        }
+    }
+    for (uint64_t i = npk * W + tid; i < n; i += stride) {   // tail, or everything when not aligned
+        const T ri = r[i] - a * q[i];
+        x[i] = fma(a, p[i], x[i]);
+        r[i] = ri;
+        const T zi = ri * d[i];
+        z[i] = zi;
+        drz = fma(ri, zi, drz);
+        drr = fma(ri, ri, drr);
+    }
+    double brz, brr;
+    block_sum2_v<T>(drz, drr, sh, brz, brr);
+    if (threadIdx.x == 0) {
+        parts.rz[blockIdx.x] = brz;
+        parts.rr[blockIdx.x] = brr;
+    }
+    if (!last_cta(&ctl->ticket, &flag, gridDim.x)) return;
+    // the totals (same order as ordered_sum2) and the control fields in one round
+    int64_t it = 0, maxit = 0;
+    double rz_old = 0.0, tol2 = 0.0;
+    if (threadIdx.x == 0) {
+        it = ctl->iterations + 1;
+        maxit = ctl->maxit;
+        rz_old = ctl->rz;
+        tol2 = ctl->tol2;
+    }
+    double sa = 0.0, sb = 0.0;
+    for (uint32_t i = threadIdx.x; i < gridDim.x; i += kVecThreads) {
+        sa += __ldcg(parts.rz + i);
+        sb += __ldcg(parts.rr + i);
+    }
+    double rz_new, rr;
+    block_sum2_v<double>(sa, sb, sh, rz_new, rr);
+    if (threadIdx.x == 0) {
+        ctl->iterations = it;
+        ctl->rr = rr;
+        ctl->rz_prev = rz_old;
+        const bool stop = rr <= tol2 || it >= maxit || !(rr == rr);
+        if (stop) {
+            ctl->done = 1;
+        } else {
+            ctl->beta = rz_old != 0.0 ? rz_new / rz_old : 0.0;
+        }
+        ctl->rz = rz_new;
+        if (v.p2) ctl->pcur = pcur ^ 1;   // this iteration's p is now the latest
+        ctl->ticket = 0;
+    }
 }
 
 // Kernel C: p = z + beta p, two packs per thread per step.
