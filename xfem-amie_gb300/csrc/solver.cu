@@ -57,6 +57,8 @@ struct SolverState {
     DevArray<double> parts;       // 4 * stride: pq, rz, rr, spare
     DevArray<PcgCtl> ctl;
     PcgCtl *h_ctl = nullptr;      // pinned
+    PcgCtl *h_ring = nullptr;     // pinned, 2: control block after each of two graph launches in flight
+    cudaEvent_t ring_ev[2] = {nullptr, nullptr};
     cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
     int graph_iters = 0;
     ~SolverState()
@@ -64,6 +66,9 @@ struct SolverState {
         if (graph64) cudaGraphExecDestroy(graph64);
         if (graph32) cudaGraphExecDestroy(graph32);
         if (h_ctl) cudaFreeHost(h_ctl);
+        if (h_ring) cudaFreeHost(h_ring);
+        for (cudaEvent_t e : ring_ev)
+            if (e) cudaEventDestroy(e);
     }
 };
 
@@ -287,6 +292,8 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->stride));
         AMIE_TRY(s->ctl.alloc(t->ctx, 1));
         AMIE_CUDA(cudaMallocHost((void **)&s->h_ctl, sizeof(PcgCtl)));
+        AMIE_CUDA(cudaMallocHost((void **)&s->h_ring, 2 * sizeof(PcgCtl)));
+        for (cudaEvent_t &e : s->ring_ev) AMIE_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         const uint64_t n = t->n;
         AMIE_TRY(t->r.alloc(t->ctx, n));
         AMIE_TRY(t->z.alloc(t->ctx, n));
@@ -416,18 +423,33 @@ amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iter
     // Host watchdog: the device sets `done` by maxit at the latest, so more
     // launches than maxit / kGraphIters + 2 mean the control block is not advancing.
     const int64_t max_launches = maxit / kGraphIters + 2;
-    for (int64_t launch = 0;; launch++) {
+    // Two graph launches stay in flight: the host reads the control block copied
+    // after launch k while launch k + 1 runs, so the GPU does not idle during the
+    // check.  A launch queued after the stop finds `done` set and its kernels
+    // return at once.  Each ring slot is read only after its event completed.
+    const int pi = sizeof(T) == 8 ? 1 : 0;
+    auto launch = [&](int64_t k) -> amie_status {
         AMIE_CUDA(cudaGraphLaunch(*g, st));
-        g_launches += s->graph_kernels[sizeof(T) == 8 ? 1 : 0] * kGraphIters;
-        AMIE_CUDA(cudaMemcpyAsync(s->h_ctl, s->ctl.p, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
-        AMIE_CUDA(cudaStreamSynchronize(st));
-        if (s->h_ctl->done) break;
-        if (launch >= max_launches) {
+        g_launches += s->graph_kernels[pi] * kGraphIters;
+        AMIE_CUDA(cudaMemcpyAsync(s->h_ring + (k & 1), s->ctl.p, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaEventRecord(s->ring_ev[k & 1], st));
+        return AMIE_OK;
+    };
+    AMIE_TRY(launch(0));
+    AMIE_TRY(launch(1));
+    for (int64_t k = 0;; k++) {
+        AMIE_CUDA(cudaEventSynchronize(s->ring_ev[k & 1]));
+        const PcgCtl h = s->h_ring[k & 1];
+        if (h.done) {
+            *s->h_ctl = h;
+            break;
+        }
+        if (k >= max_launches) {
             set_error("PCG control block stalled: %lld launches, iterations %lld, maxit %lld, rr %g, tol2 %g",
-                      (long long)launch, (long long)s->h_ctl->iterations, (long long)s->h_ctl->maxit,
-                      s->h_ctl->rr, s->h_ctl->tol2);
+                      (long long)k, (long long)h.iterations, (long long)h.maxit, h.rr, h.tol2);
             return AMIE_TIMEOUT;
         }
+        AMIE_TRY(launch(k + 2));
     }
     *iters = s->h_ctl->iterations;
     *rr_out = s->h_ctl->rr;
