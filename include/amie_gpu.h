@@ -282,25 +282,32 @@ AMIE_API amie_status amie_server_query(amie_server *srv, amie_server_stats *stat
  * (PositionOperation::eval, polynomial/vm_token.cpp:258-271).
  * corners [n*6]: the corner vertices (x, y) at reference coordinates (0,1),
  * (0,0), (1,0); line [n_line*2]: the polyline (n_line >= 2, first segment not
- * empty).  Out: count [n] (points of the rule, 0 unless status is AMIE_CUT_OK),
- * status [n] (AMIE_CUT_*), rule [n*AMIE_CUT_MAX_POINTS*3] (xi, eta, weight times
- * det J), h_point [n*AMIE_CUT_MAX_POINTS] (Heaviside +-1 at each point),
- * h_vertex [n*3] (Heaviside at the corners, whatever the status).  The jump of
- * the enrichment function of corner k at point g is h_point[g] - h_vertex[k].
- * A status other than AMIE_CUT_OK leaves the element to the caller's own rule:
- * AMIE_CUT_MONTE_CARLO is where the reference falls back to 512 random points. */
+ * empty); flags: 0 or AMIE_CUT_REPLACE_MONTE_CARLO.  Out: count [n] (points of
+ * the rule, 0 unless status is AMIE_CUT_OK or AMIE_CUT_REPLACED), status [n]
+ * (AMIE_CUT_*), rule [n*AMIE_CUT_MAX_POINTS*3] (xi, eta, weight times det J),
+ * h_point [n*AMIE_CUT_MAX_POINTS] (Heaviside +-1 at each point), h_vertex [n*3]
+ * (Heaviside at the corners, whatever the status).  The jump of the enrichment
+ * function of corner k at point g is h_point[g] - h_vertex[k].
+ * Without the flag, a status other than AMIE_CUT_OK leaves the element to the
+ * caller's own rule (AMIE_CUT_MONTE_CARLO is where the reference falls back to
+ * 512 random points).  With AMIE_CUT_REPLACE_MONTE_CARLO those elements, and the
+ * order-dependent ones, get a deterministic crack-conforming rule instead
+ * (AMIE_CUT_REPLACED): exact for the Heaviside integrand, so the element
+ * matrices differ from the reference's Monte-Carlo ones by that method's error. */
 #define AMIE_CUT_MAX_HINTS 6
 #define AMIE_CUT_MAX_POINTS 52
+#define AMIE_CUT_REPLACE_MONTE_CARLO 1u
 enum {
     AMIE_CUT_OK = 0,
     AMIE_CUT_NOT_CUT = 1,           /* the polyline neither crosses the element nor ends in it */
     AMIE_CUT_MONTE_CARLO = 2,       /* fewer than three sub-triangles once close hints are dropped */
     AMIE_CUT_ORDER_DEPENDENT = 3,   /* two hints closer than the insertion tolerance 0.05 */
-    AMIE_CUT_TOO_MANY_HINTS = 4     /* more than AMIE_CUT_MAX_HINTS hints */
+    AMIE_CUT_TOO_MANY_HINTS = 4,    /* more than AMIE_CUT_MAX_HINTS hints */
+    AMIE_CUT_REPLACED = 5           /* deterministic rule where the reference uses Monte-Carlo */
 };
 AMIE_API amie_status amie_cut_rules(amie_ctx *ctx, uint32_t n, const double *corners, uint32_t n_line,
-                                    const double *line, uint32_t *count, int8_t *status, double *rule,
-                                    int8_t *h_point, int8_t *h_vertex);
+                                    const double *line, uint32_t flags, uint32_t *count, int8_t *status,
+                                    double *rule, int8_t *h_point, int8_t *h_vertex);
 
 /* ------------------------------------------------------------------ fields and damage
  * Per-element strain (Voigt, engineering shear: xx yy xy in 2D, xx yy zz yz xz xy

@@ -22,6 +22,13 @@ What it restates (paths relative to the AMIE source tree):
   on every sub-triangle, weights scaled to the element's area;
 * the crack's Heaviside function, PositionOperation (polynomial/vm_token.cpp:242-271)
   with the witness of Segment::normal(const Point &) (geometry/geometry_base.cpp:4010-4022).
+
+With REPLACE_MONTE_CARLO, elements the reference would integrate by
+Monte-Carlo (or insertion-order dependently) are triangulated with no insertion
+tolerance instead (status REPLACED).  `split_rule_degree4` is an independent
+exact rule for a straight crossing (three crack-conforming pieces, Dunavant's
+6-point degree-4 rule), used by the tests to check that the replaced rules
+integrate exactly.
 """
 from __future__ import annotations
 
@@ -31,7 +38,8 @@ import numpy as np
 
 MAX_HINTS = 6
 MAX_POINTS = 52
-OK, NOT_CUT, MONTE_CARLO, ORDER_DEPENDENT, TOO_MANY_HINTS = 0, 1, 2, 3, 4
+OK, NOT_CUT, MONTE_CARLO, ORDER_DEPENDENT, TOO_MANY_HINTS, REPLACED = 0, 1, 2, 3, 4, 5
+REPLACE_MONTE_CARLO = 1
 INSERT_TOL = 0.05
 FLAT = 1e-12
 W_EDGE, W_CENTRE = 0.260416666666667, -0.28125
@@ -92,14 +100,15 @@ def _hints(X, line):
     return hints
 
 
-def _delaunay(V, n_hints):
+def _delaunay(V, n_hints, tol=INSERT_TOL):
     """Sub-triangles (vertex index triples, counter-clockwise) of the corner
-    triangle after inserting V[3:] in order."""
+    triangle after inserting V[3:] in order; a hint within `tol` of a vertex of
+    a triangle it conflicts with is dropped."""
     tris = [(1, 2, 0)]
     for h in range(3, 3 + n_hints):
         p = V[h]
         con = [_incircle(V[t[0]], V[t[1]], V[t[2]], p) > 0.0 for t in tris]
-        if any(c and min(math.dist(V[v], p) for v in t) < INSERT_TOL for c, t in zip(con, tris)):
+        if any(c and min(math.dist(V[v], p) for v in t) < tol for c, t in zip(con, tris)):
             continue
         edges = {}
         for c, t in zip(con, tris):
@@ -116,7 +125,7 @@ def _delaunay(V, n_hints):
     return tris
 
 
-def element_rule(corners, line):
+def element_rule(corners, line, flags=0):
     """(status, [(xi, eta, weight, h), ...], [h at the three corners]) of one element."""
     X = [(corners[0], corners[1]), (corners[2], corners[3]), (corners[4], corners[5])]
     line = [tuple(p) for p in line]
@@ -127,14 +136,17 @@ def element_rule(corners, line):
         return TOO_MANY_HINTS, [], hv
     if not hints:
         return NOT_CUT, [], hv
-    for i in range(len(hints)):
-        for j in range(i):
-            if math.dist(hints[i], hints[j]) < INSERT_TOL:
-                return ORDER_DEPENDENT, [], hv
+    close = any(math.dist(hints[i], hints[j]) < INSERT_TOL for i in range(len(hints)) for j in range(i))
     V = list(REF) + hints
-    tris = _delaunay(V, len(hints))
-    if len(tris) < 3:
-        return MONTE_CARLO, [], hv
+    status = ORDER_DEPENDENT if close else OK
+    tris = [] if close else _delaunay(V, len(hints))
+    if not close and len(tris) < 3:
+        status = MONTE_CARLO
+    if status != OK and flags & REPLACE_MONTE_CARLO:
+        tris = _delaunay(V, len(hints), 0.0)
+        status = REPLACED if len(tris) >= 3 else MONTE_CARLO
+    if status not in (OK, REPLACED):
+        return status, [], hv
     pts = []
     for t in tris:
         A, B, Cc = (V[v] for v in t)
@@ -154,10 +166,10 @@ def element_rule(corners, line):
         z = 1.0 - xi - eta
         p = (eta * X[0][0] + z * X[1][0] + xi * X[2][0], eta * X[0][1] + z * X[1][1] + xi * X[2][1])
         out.append((xi, eta, wq * scale, heaviside(p, line, w)))
-    return OK, out, hv
+    return status, out, hv
 
 
-def cut_rules(corners, line):
+def cut_rules(corners, line, flags=0):
     """Same outputs as amie_cut_rules: count [n], status [n], rule [n, 52, 3],
     h_point [n, 52], h_vertex [n, 3]."""
     c = np.asarray(corners, np.float64).reshape(-1, 6)
@@ -169,7 +181,7 @@ def cut_rules(corners, line):
     hp = np.zeros((n, MAX_POINTS), np.int8)
     hv = np.zeros((n, 3), np.int8)
     for e in range(n):
-        st, pts, h = element_rule(c[e], ln)
+        st, pts, h = element_rule(c[e], ln, flags)
         status[e] = st
         hv[e] = h
         count[e] = len(pts)
@@ -177,3 +189,51 @@ def cut_rules(corners, line):
             rule[e, g] = (xi, eta, wq)
             hp[e, g] = s
     return count, status, rule, hp, hv
+
+
+# Dunavant (1985), degree 4, positive weights: barycentric (a, b, b) and permutations
+_DUN = ((0.108103018168070, 0.445948490915965, 0.223381589678011),
+        (0.816847572980459, 0.091576213509771, 0.109951743655322))
+
+
+def split_rule_degree4(corners, line):
+    """Independent exact rule of an element crossed once by a straight piece of
+    the crack (two edge crossings, no polyline point inside): the corner alone
+    on its side with the two crossings, and the remaining quadrilateral as two
+    triangles, each with Dunavant's 6-point rule; Heaviside by the same ray
+    parity.  Returns [(xi, eta, weight, h), ...] or None when the element is not
+    crossed that way."""
+    X = [(corners[0], corners[1]), (corners[2], corners[3]), (corners[4], corners[5])]
+    line = [tuple(p) for p in line]
+    w = witness(line)
+    hits = {}
+    for s_ in range(len(line) - 1):
+        a, b = line[s_], line[s_ + 1]
+        for i in range(3):
+            j = (i + 1) % 3
+            fa, fb = _orient(a, b, X[i]), _orient(a, b, X[j])
+            if fa * fb < 0.0 and _orient(X[i], X[j], a) * _orient(X[i], X[j], b) < 0.0:
+                t = fa / (fa - fb)
+                hits[(i, j)] = (REF[i][0] + t * (REF[j][0] - REF[i][0]), REF[i][1] + t * (REF[j][1] - REF[i][1]))
+    if len(hits) != 2:
+        return None
+    (e1, p1), (e2, p2) = hits.items()
+    lone = (set(e1) & set(e2)).pop()
+    j1 = (set(e1) - {lone}).pop()
+    j2 = (set(e2) - {lone}).pop()
+    R = REF
+    pieces = [(R[lone], p1, p2), (p1, R[j1], R[j2]), (p1, R[j2], p2)]
+    area = 0.5 * abs(_orient(X[0], X[1], X[2]))
+    out = []
+    for A, B, Cc in pieces:
+        ar = 0.5 * abs(_orient(A, B, Cc)) * area / 0.5
+        for a_, b_, wt in _DUN:
+            for r in range(3):
+                lam = [b_, b_, b_]
+                lam[r] = a_
+                xi = lam[0] * A[0] + lam[1] * B[0] + lam[2] * Cc[0]
+                eta = lam[0] * A[1] + lam[1] * B[1] + lam[2] * Cc[1]
+                z = 1.0 - xi - eta
+                p = (eta * X[0][0] + z * X[1][0] + xi * X[2][0], eta * X[0][1] + z * X[1][1] + xi * X[2][1])
+                out.append((xi, eta, wt * ar, heaviside(p, line, w)))
+    return out

@@ -10,7 +10,10 @@ the CPU restatement (oracle/cut_rules.py) and the reference's fixtures.
 * seeded random triangles around a kinked polyline (crossed, tip, kink, not
   cut, hints near corners): status, points and Heaviside values as the
   restatement's;
-* a known answer: the right triangle cut at half height.
+* a known answer: the right triangle cut at half height;
+* with AMIE_CUT_REPLACE_MONTE_CARLO: the same as the restatement, the elements
+  the reference integrated by Monte-Carlo replaced by conforming rules whose
+  device element matrices equal an independent exact rule's to 1e-12.
 """
 import numpy as np
 import pytest
@@ -37,7 +40,7 @@ def assert_same_rules(dev, ref, scale):
     assert np.array_equal(st, rst)
     assert np.array_equal(cnt, rcnt)
     assert np.array_equal(hv, rhv)
-    for e in np.nonzero(st == CR.OK)[0]:
+    for e in np.nonzero(np.isin(st, (CR.OK, CR.REPLACED)))[0]:
         n = int(cnt[e])
         a, b = rule[e, :n], rrule[e, :n]
         d = np.abs(a[:, None, :2] - b[None, :, :2]).max(axis=2)
@@ -125,3 +128,54 @@ def test_cut_rules_known_answer(gpu_ctx):
     eta = rule[0, :n, 1]
     assert np.all((eta > 0.5) == (h == -1))
     assert abs(w[h == -1].sum() - 0.5) <= 1e-14 and abs(w[h == 1].sum() - 1.5) <= 1e-14
+
+
+@pytest.mark.parametrize("name", ["crack_p1", "crack_p2"])
+def test_cut_rules_replacement_golden(gpu_ctx, name):
+    import amie_gpu
+    d = load_golden(name)
+    m = am.from_golden(d, "auto")
+    elems = CC.heaviside_elements(m)
+    corners = CC.corners(d, m, elems)
+    line = CC.crack_line(d)
+    dev = gpu_ctx.cut_rules(corners, line, amie_gpu.CUT_REPLACE_MONTE_CARLO)
+    ref = CR.cut_rules(corners, line, CR.REPLACE_MONTE_CARLO)
+    area = np.array([m.gp[3 * m.gp_ptr[e] + 2:3 * m.gp_ptr[e + 1]:3].sum() for e in elems])
+    assert_same_rules(dev, ref, area)
+    cnt, st, rule, hp, hv = dev
+    ngp = np.diff(m.gp_ptr.astype(np.int64))[elems]
+    assert np.array_equal(st == amie_gpu.CUT_REPLACED, ngp == 512)
+    for i in np.nonzero(st == amie_gpu.CUT_REPLACED)[0]:
+        split = CR.split_rule_degree4(corners[i], line)
+        assert split is not None
+        e = elems[i:i + 1]
+        sub = CC.submesh(m, e, cnt[i:i + 1], rule[i:i + 1], hp[i:i + 1], hv[i:i + 1])
+        t = amie_gpu.Topology(gpu_ctx, sub)
+        try:
+            t.assemble()
+            _, ke = t.element_matrices()
+        finally:
+            t.close()
+        n = len(split)
+        srule = np.array([[(p[0], p[1], p[2]) for p in split]])
+        shp = np.array([[p[3] for p in split]], np.int8)
+        _, ks = O.element_matrices(CC.submesh(m, e, np.array([n]), srule, shp, hv[i:i + 1]))
+        assert rel(ke, ks) <= 1e-12, int(elems[i])
+
+
+def test_cut_rules_replacement_random(gpu_ctx):
+    import amie_gpu
+    corners, line = random_cases(3000, 7)
+    base = gpu_ctx.cut_rules(corners, line)
+    dev = gpu_ctx.cut_rules(corners, line, amie_gpu.CUT_REPLACE_MONTE_CARLO)
+    ref = CR.cut_rules(corners, line, CR.REPLACE_MONTE_CARLO)
+    X = corners.reshape(-1, 3, 2)
+    area = 0.5 * np.abs((X[:, 1, 0] - X[:, 0, 0]) * (X[:, 2, 1] - X[:, 0, 1])
+                        - (X[:, 1, 1] - X[:, 0, 1]) * (X[:, 2, 0] - X[:, 0, 0]))
+    assert_same_rules(dev, ref, area)
+    fell_back = np.isin(base[1], (CR.MONTE_CARLO, CR.ORDER_DEPENDENT))
+    assert (dev[1] == CR.REPLACED).sum() > 0
+    assert np.all(dev[1][~fell_back] == base[1][~fell_back])
+    assert np.all(np.isin(dev[1][fell_back], (CR.REPLACED, CR.MONTE_CARLO)))
+    ok = np.isin(dev[1], (CR.OK, CR.REPLACED))
+    assert rel(dev[2][ok, :, 2].sum(axis=1), area[ok]) <= 1e-12

@@ -172,3 +172,42 @@ def test_cut_rules_reproduce_reference_element_matrices(name):
     # weights add up to the element's area
     area = np.array([sub.gp[3 * sub.gp_ptr[i] + 2:3 * sub.gp_ptr[i + 1]:3].sum() for i in range(len(ok))])
     assert rel(area, np.array([m.gp[3 * m.gp_ptr[e] + 2:3 * m.gp_ptr[e + 1]:3].sum() for e in elems[ok]])) <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["crack_p1", "crack_p2"])
+def test_cut_rules_monte_carlo_replacement_is_exact(name):
+    """With the replacement option the elements the reference integrated by
+    Monte-Carlo get a crack-conforming rule; it integrates the Heaviside
+    integrand exactly, so it agrees with an independent exact rule (three
+    conforming pieces, Dunavant degree 4) to round-off, and every element the
+    reference sub-triangulated keeps exactly its rule."""
+    import crack_cases as CC
+    import cut_rules as CR
+    d = load_golden(name)
+    m = am.from_golden(d, "auto")
+    elems = CC.heaviside_elements(m)
+    corners = CC.corners(d, m, elems)
+    line = CC.crack_line(d)
+    base = CR.cut_rules(corners, line)
+    rep = CR.cut_rules(corners, line, CR.REPLACE_MONTE_CARLO)
+    ok = base[1] == CR.OK
+    assert np.array_equal(rep[1][ok], base[1][ok])
+    for a, b in zip(rep, base):
+        assert np.array_equal(a[ok], b[ok])
+    replaced = np.nonzero(rep[1] == CR.REPLACED)[0]
+    assert len(replaced) == int(np.sum(base[1] != CR.OK))
+    cnt, _, rule, hp, hv = rep
+    for i in replaced:
+        split = CR.split_rule_degree4(corners[i], line)
+        if split is None:
+            continue
+        e = elems[i:i + 1]
+        sub_r = CC.submesh(m, e, cnt[i:i + 1], rule[i:i + 1], hp[i:i + 1], hv[i:i + 1])
+        n = len(split)
+        srule = np.zeros((1, n, 3))
+        srule[0, :, :] = [(p[0], p[1], p[2]) for p in split]
+        shp = np.array([[p[3] for p in split]], np.int8)
+        sub_s = CC.submesh(m, e, np.array([n]), srule, shp, hv[i:i + 1])
+        _, ka = O.element_matrices(sub_r)
+        _, kb = O.element_matrices(sub_s)
+        assert rel(ka, kb) <= 1e-12, int(elems[i])

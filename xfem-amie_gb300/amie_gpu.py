@@ -45,7 +45,8 @@ class ServerStats(C.Structure):
 FIELD_STRAIN, FIELD_STRESS = 0, 1
 # amie_cut_rules: points per element at most, and the per-element status codes
 CUT_MAX_POINTS = 52
-CUT_OK, CUT_NOT_CUT, CUT_MONTE_CARLO, CUT_ORDER_DEPENDENT, CUT_TOO_MANY_HINTS = 0, 1, 2, 3, 4
+CUT_OK, CUT_NOT_CUT, CUT_MONTE_CARLO, CUT_ORDER_DEPENDENT, CUT_TOO_MANY_HINTS, CUT_REPLACED = 0, 1, 2, 3, 4, 5
+CUT_REPLACE_MONTE_CARLO = 1
 
 
 class DamageParams(C.Structure):
@@ -160,9 +161,10 @@ class Context:
     def timer_start(self):
         check(lib().amie_timer_start(self.ptr), "amie_timer_start")
 
-    def cut_rules(self, corners, line):
+    def cut_rules(self, corners, line, flags=0):
         """Rules of triangles crossed by the crack polyline `line` [(x, y), ...]:
-        (count [n], status [n], rule [n, CUT_MAX_POINTS, 3], h_point [n, CUT_MAX_POINTS], h_vertex [n, 3])."""
+        (count [n], status [n], rule [n, CUT_MAX_POINTS, 3], h_point [n, CUT_MAX_POINTS], h_vertex [n, 3]).
+        flags = CUT_REPLACE_MONTE_CARLO: deterministic rules where the reference uses Monte-Carlo."""
         c = np.ascontiguousarray(corners, np.float64).reshape(-1, 6)
         ln = np.ascontiguousarray(line, np.float64).reshape(-1, 2)
         n = c.shape[0]
@@ -171,8 +173,9 @@ class Context:
         rule = np.zeros((n, CUT_MAX_POINTS, 3), np.float64)
         hp = np.zeros((n, CUT_MAX_POINTS), np.int8)
         hv = np.zeros((n, 3), np.int8)
-        check(lib().amie_cut_rules(self.ptr, C.c_uint32(n), _p(c), C.c_uint32(ln.shape[0]), _p(ln), _p(cnt),
-                                   _p(status), _p(rule), _p(hp), _p(hv)), "amie_cut_rules")
+        check(lib().amie_cut_rules(self.ptr, C.c_uint32(n), _p(c), C.c_uint32(ln.shape[0]), _p(ln),
+                                   C.c_uint32(flags), _p(cnt), _p(status), _p(rule), _p(hp), _p(hv)),
+              "amie_cut_rules")
         return cnt, status, rule, hp, hv
         return cnt, rule, side
 

@@ -27,6 +27,13 @@
 // The reference shuffles the hints before inserting them; the result does not
 // depend on the order unless two hints lie within the insertion tolerance of
 // each other, which is reported (AMIE_CUT_ORDER_DEPENDENT) instead of guessed.
+//
+// With AMIE_CUT_REPLACE_MONTE_CARLO the elements the reference would integrate
+// by Monte-Carlo (or in an insertion-order dependent way) get a deterministic
+// rule instead (status AMIE_CUT_REPLACED): the same triangulation with no
+// insertion tolerance, so every hint is a vertex and the sub-triangles conform
+// to the crack; the rule then integrates the piecewise-polynomial Heaviside
+// integrand exactly, where the reference's 512 random points do not.
 // Exact-arithmetic degeneracies (a corner on the polyline, a polyline point on
 // an edge, four co-circular points) are resolved by the strict orientation and
 // in-circle signs below, where the reference applies POINT_TOLERANCE.
@@ -74,18 +81,74 @@ __device__ int8_t heaviside(P2d p, P2d w, const double *line, uint32_t n_line)
     return (k & 1u) ? int8_t(1) : int8_t(-1);
 }
 
+// Incremental Delaunay (Bowyer-Watson) of the corners and the nh hints V[3..]
+// from the corner triangle, counter-clockwise in reference coordinates; a hint
+// within `tol` of a vertex of a triangle it conflicts with is dropped (the
+// reference's insertion tolerance; 0 keeps every hint that is not already a
+// vertex).  False when the triangle table would overflow.
+__device__ bool triangulate(const P2d (&V)[kMaxVerts], int nh, double tol, uint8_t (&T)[kMaxTris][3], int &nt)
+{
+    nt = 1;
+    T[0][0] = 1, T[0][1] = 2, T[0][2] = 0;
+    for (int h = 3; h < 3 + nh; h++) {
+        const P2d p = V[h];
+        bool con[kMaxTris];
+        bool skip = false;
+        for (int t = 0; t < nt; t++) {
+            con[t] = incircle(V[T[t][0]], V[T[t][1]], V[T[t][2]], p) > 0.0;
+            if (con[t])
+                for (int k = 0; k < 3; k++) skip |= dist(V[T[t][k]], p) < tol;
+        }
+        if (skip) continue;
+        // boundary of the cavity: edges of conflicting triangles not shared by two of them
+        uint8_t E[kMaxEdges][2];
+        int ne = 0;
+        for (int t = 0; t < nt; t++) {
+            if (!con[t]) continue;
+            for (int k = 0; k < 3; k++) {
+                const uint8_t u = T[t][k], v = T[t][(k + 1) % 3];
+                int found = -1;
+                for (int q = 0; q < ne; q++)
+                    if (E[q][0] == v && E[q][1] == u) found = q;
+                if (found >= 0) {
+                    E[found][0] = E[ne - 1][0], E[found][1] = E[ne - 1][1];
+                    ne--;
+                } else if (ne < kMaxEdges) {
+                    E[ne][0] = u, E[ne][1] = v;
+                    ne++;
+                } else {
+                    return false;
+                }
+            }
+        }
+        int w = 0;
+        for (int t = 0; t < nt; t++)
+            if (!con[t]) T[w][0] = T[t][0], T[w][1] = T[t][1], T[w][2] = T[t][2], w++;
+        nt = w;
+        for (int q = 0; q < ne; q++)
+            if (orient(V[E[q][0]], V[E[q][1]], p) > kFlat) {
+                if (nt == kMaxTris) return false;
+                T[nt][0] = E[q][0], T[nt][1] = E[q][1], T[nt][2] = (uint8_t)h;
+                nt++;
+            }
+    }
+    return true;
+}
+
 }  // namespace
 
 // corners: (x, y) of the corners at reference (0,1), (0,0), (1,0); line: the
-// polyline (n_line points).  Writes count (points of the rule, 0 unless
-// status is AMIE_CUT_OK), status, rule (xi, eta, weight), h_point (Heaviside at
-// each point) and h_vertex (Heaviside at the three corners, always).
+// polyline (n_line points).  Writes count (points of the rule, 0 unless the
+// status is AMIE_CUT_OK or AMIE_CUT_REPLACED), status, rule (xi, eta, weight),
+// h_point (Heaviside at each point) and h_vertex (Heaviside at the three
+// corners, always).
 __global__ void k_cut_rules(uint32_t n, const double *__restrict__ corners, uint32_t n_line,
-                            const double *__restrict__ line, uint32_t *count, int8_t *status, double *rule,
-                            int8_t *h_point, int8_t *h_vertex)
+                            const double *__restrict__ line, uint32_t flags, uint32_t *count, int8_t *status,
+                            double *rule, int8_t *h_point, int8_t *h_vertex)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
+    const bool replace = (flags & AMIE_CUT_REPLACE_MONTE_CARLO) != 0;
     const double *c = corners + (size_t)e * 6;
     const P2d X[3] = {{c[0], c[1]}, {c[2], c[3]}, {c[4], c[5]}};
     const P2d R[3] = {{0.0, 1.0}, {0.0, 0.0}, {1.0, 0.0}};
@@ -128,55 +191,21 @@ __global__ void k_cut_rules(uint32_t n, const double *__restrict__ corners, uint
     }
     if (overflow) { status[e] = AMIE_CUT_TOO_MANY_HINTS; return; }
     if (nh == 0) { status[e] = AMIE_CUT_NOT_CUT; return; }
+    bool close = false;   // two hints within the insertion tolerance
     for (int i = 1; i < nh; i++)
-        for (int j = 0; j < i; j++)
-            if (dist(V[3 + i], V[3 + j]) < kInsertTol) { status[e] = AMIE_CUT_ORDER_DEPENDENT; return; }
-
-    // incremental Delaunay (Bowyer-Watson) from the corner triangle, counter-clockwise
+        for (int j = 0; j < i; j++) close |= dist(V[3 + i], V[3 + j]) < kInsertTol;
     uint8_t T[kMaxTris][3];
-    int nt = 1;
-    T[0][0] = 1, T[0][1] = 2, T[0][2] = 0;
-    for (int h = 3; h < 3 + nh; h++) {
-        const P2d p = V[h];
-        bool con[kMaxTris];
-        bool skip = false;
-        for (int t = 0; t < nt; t++) {
-            con[t] = incircle(V[T[t][0]], V[T[t][1]], V[T[t][2]], p) > 0.0;
-            if (con[t])
-                for (int k = 0; k < 3; k++) skip |= dist(V[T[t][k]], p) < kInsertTol;
-        }
-        if (skip) continue;
-        // boundary of the cavity: edges of conflicting triangles not shared by two of them
-        uint8_t E[kMaxEdges][2];
-        int ne = 0;
-        for (int t = 0; t < nt; t++) {
-            if (!con[t]) continue;
-            for (int k = 0; k < 3; k++) {
-                const uint8_t u = T[t][k], v = T[t][(k + 1) % 3];
-                int found = -1;
-                for (int q = 0; q < ne; q++)
-                    if (E[q][0] == v && E[q][1] == u) found = q;
-                if (found >= 0) {
-                    E[found][0] = E[ne - 1][0], E[found][1] = E[ne - 1][1];
-                    ne--;
-                } else if (ne < kMaxEdges) {
-                    E[ne][0] = u, E[ne][1] = v;
-                    ne++;
-                }
-            }
-        }
-        int w = 0;
-        for (int t = 0; t < nt; t++)
-            if (!con[t]) T[w][0] = T[t][0], T[w][1] = T[t][1], T[w][2] = T[t][2], w++;
-        nt = w;
-        for (int q = 0; q < ne; q++)
-            if (orient(V[E[q][0]], V[E[q][1]], p) > kFlat) {
-                if (nt == kMaxTris) { status[e] = AMIE_CUT_TOO_MANY_HINTS; return; }
-                T[nt][0] = E[q][0], T[nt][1] = E[q][1], T[nt][2] = (uint8_t)h;
-                nt++;
-            }
+    int nt = 0;
+    int8_t st = AMIE_CUT_OK;
+    if (close) st = AMIE_CUT_ORDER_DEPENDENT;
+    else if (!triangulate(V, nh, kInsertTol, T, nt)) st = AMIE_CUT_TOO_MANY_HINTS;
+    else if (nt < 3) st = AMIE_CUT_MONTE_CARLO;
+    if ((st == AMIE_CUT_ORDER_DEPENDENT || st == AMIE_CUT_MONTE_CARLO) && replace) {
+        if (!triangulate(V, nh, 0.0, T, nt)) st = AMIE_CUT_TOO_MANY_HINTS;
+        else if (nt < 3) st = AMIE_CUT_MONTE_CARLO;
+        else st = AMIE_CUT_REPLACED;
     }
-    if (nt < 3) { status[e] = AMIE_CUT_MONTE_CARLO; return; }
+    if (st != AMIE_CUT_OK && st != AMIE_CUT_REPLACED) { status[e] = st; return; }
 
     // the 4-point rule on each sub-triangle, weights scaled to the element's area
     double *out = rule + (size_t)e * AMIE_CUT_MAX_POINTS * 3;
@@ -208,7 +237,7 @@ __global__ void k_cut_rules(uint32_t n, const double *__restrict__ corners, uint
         hp[q] = heaviside(p, W, line, n_line);
     }
     count[e] = (uint32_t)k;
-    status[e] = AMIE_CUT_OK;
+    status[e] = st;
 }
 
 }  // namespace amie
@@ -216,12 +245,13 @@ __global__ void k_cut_rules(uint32_t n, const double *__restrict__ corners, uint
 using namespace amie;
 
 extern "C" amie_status amie_cut_rules(amie_ctx *ctx, uint32_t n, const double *corners, uint32_t n_line,
-                                      const double *line, uint32_t *count, int8_t *status, double *rule,
-                                      int8_t *h_point, int8_t *h_vertex)
+                                      const double *line, uint32_t flags, uint32_t *count, int8_t *status,
+                                      double *rule, int8_t *h_point, int8_t *h_vertex)
 {
     if (!ctx || n_line < 2 || !line || (n && (!corners || !count || !status || !rule || !h_point || !h_vertex)))
         return AMIE_BAD_INPUT;
     if (line[0] == line[2] && line[1] == line[3]) return AMIE_BAD_INPUT;   // the witness needs a first segment
+    if (flags & ~(uint32_t)AMIE_CUT_REPLACE_MONTE_CARLO) return AMIE_BAD_INPUT;
     if (!n) return AMIE_OK;
     AMIE_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
@@ -238,7 +268,7 @@ extern "C" amie_status amie_cut_rules(amie_ctx *ctx, uint32_t n, const double *c
     AMIE_TRY(dhv.alloc(ctx, (size_t)n * 3));
     AMIE_CUDA(cudaMemcpyAsync(dc.p, corners, (size_t)n * 6 * 8, cudaMemcpyHostToDevice, st));
     AMIE_CUDA(cudaMemcpyAsync(dl.p, line, (size_t)n_line * 2 * 8, cudaMemcpyHostToDevice, st));
-    k_cut_rules<<<(n + 127) / 128, 128, 0, st>>>(n, dc.p, n_line, dl.p, dn.p, dst.p, dr.p, dhp.p, dhv.p);
+    k_cut_rules<<<(n + 127) / 128, 128, 0, st>>>(n, dc.p, n_line, dl.p, flags, dn.p, dst.p, dr.p, dhp.p, dhv.p);
     g_launches += 1;
     AMIE_CUDA(cudaGetLastError());
     AMIE_CUDA(cudaMemcpyAsync(count, dn.p, (size_t)n * 4, cudaMemcpyDeviceToHost, st));
