@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
     ap.add_argument("--serve", type=int, default=256, help="serving-mix requests (0 = skip)")
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving mix (--serve requests) and print "
+                                                              "its statistics (for an ncu launch list of the server)")
     ap.add_argument("--profile", action="store_true", help="assemble once and launch the SpMV kernels a few times "
                                                            "(for an ncu capture), print their timings, exit")
     ap.add_argument("--launch-list", action="store_true", help="run exactly one step without warm-up (for an ncu "
@@ -301,9 +303,13 @@ def run_ours(args, world, rank, local, dist):
     import amie_gpu as G
     import build as gpu_build
     gpu_build.build()
-    m, bcs, meta, name = make_workload(args.config, args.size)
     ctx = G.Context(local)
     solver = G.SOLVER_PCG_MIXED if args.solver == "mixed" else G.SOLVER_PCG_FP64
+    if args.serve_only:
+        print(json.dumps({"serving": run_serving(ctx, args.serve, args.serve_rate, solver)}))
+        ctx.close()
+        return 0
+    m, bcs, meta, name = make_workload(args.config, args.size)
     topo = G.Topology(ctx, m)
     topo.assemble()
     topo.apply_dirichlet(*bcs)
