@@ -137,6 +137,7 @@ struct SellView {
     const T *val;                // [slots * S * S] chunked as above
     const uint32_t *cta_first;   // [grid + 1] first slice of each CTA of the launch (slot-balanced ranges)
     T *slice_dot;                // [n_slices] per-slice partial of the fused dot product (scratch)
+    uint32_t prefetch_bytes = 0; // k_sell_dir: L2 prefetch of the start of each CTA's range before its wait
 };
 
 }  // namespace amie

@@ -53,6 +53,9 @@ struct SolverState {
     // L2 eviction hint of the matrix stream in k_sell_dir (see ld_stream);
     // AMIE_MATRIX_HINT overrides it for measurements
     int matrix_hint = kMatrixHint;
+    // bytes of each CTA's matrix range k_sell_dir prefetches into L2 before its wait
+    // (AMIE_PREFETCH_KB; cfg1 step: 0 KB 686 ms, 16 KB 673 ms, 32-64 KB 674 ms, 128 KB 688 ms)
+    uint32_t prefetch_bytes = 16u << 10;
     int graph_kernels[2] = {3, 3};   // kernels per iteration of the FP32 / FP64 graph
     DevArray<double> parts;       // 4 * stride: pq, rz, rr, spare
     DevArray<PcgCtl> ctl;
@@ -274,6 +277,7 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         s->grid_vec[0] = resident((const void *)k_update<float>, 0);
         s->grid_vec[1] = resident((const void *)k_update<double>, 0);
         if (const char *e = std::getenv("AMIE_MATRIX_HINT")) s->matrix_hint = std::min(2, std::max(0, std::atoi(e)));
+        if (const char *e = std::getenv("AMIE_PREFETCH_KB")) s->prefetch_bytes = (uint32_t)std::min(1024, std::max(0, std::atoi(e))) * 1024u;
         s->grid_dir[0] = resident(sell_dir_kernel<float>(t->s, s->matrix_hint), 0);
         s->grid_dir[1] = resident(sell_dir_kernel<double>(t->s, s->matrix_hint), 0);
         AMIE_CUDA(cudaGetLastError());
@@ -341,9 +345,10 @@ PcgVecs<float> vecs_of<float>(amie_topo *t)
 // k_sell_dir); false when the SELL copy or the CTA table for `grid` is missing.
 template <typename T>
 bool launch_spmv_dir(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, PcgCtl *ctl, bool fin,
-                     cudaStream_t st, bool pdl, int hint)
+                     cudaStream_t st, bool pdl, int hint, uint32_t prefetch_bytes = 0)
 {
     SellView<T> sv = sell_of<T>(t);
+    sv.prefetch_bytes = prefetch_bytes;
     auto it = t->sell_cta_first.find(grid);
     if (!sv.val || it == t->sell_cta_first.end() || !v.p2) return false;
     sv.cta_first = it->second.p;
@@ -374,7 +379,7 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     for (int it = 0; it < kGraphIters; it++) {
         // the first kernel follows the previous graph launch in plain stream order
         if (fold<T>(s)) {
-            launch_spmv_dir<T>(t, gd, v, parts.pq, ctl, true, st, s->pdl && it > 0, s->matrix_hint);
+            launch_spmv_dir<T>(t, gd, v, parts.pq, ctl, true, st, s->pdl && it > 0, s->matrix_hint, s->prefetch_bytes);
             launch_k(s->pdl, k_update<T>, gv, 0, st, v, n, parts, ctl);
         } else {
             PcgVecs<T> v1 = v;

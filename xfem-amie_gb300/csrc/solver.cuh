@@ -548,6 +548,19 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
     __shared__ double sh[33];
     __shared__ int flag;
     __shared__ uint32_t next_sl;
+    if (A.prefetch_bytes && threadIdx.x == 0) {
+        // the matrix does not change during a solve: start streaming the head of
+        // this CTA's contiguous slot range into L2 while the predecessor finishes
+        const uint32_t sb = __ldg(A.cta_first + blockIdx.x), se = __ldg(A.cta_first + blockIdx.x + 1);
+        const uint64_t g0 = __ldg(A.slice_ptr + sb), g1 = __ldg(A.slice_ptr + se);
+        // g0 is a multiple of 32 slots, so both starts are 128-byte aligned; sizes are whole 16-byte units
+        const uint64_t vfull = (g1 - g0) * (S * S * sizeof(T)), cfull = (g1 - g0) * 4;
+        const uint64_t vcap = A.prefetch_bytes, ccap = A.prefetch_bytes / (S * S);
+        const uint64_t vb = (vfull < vcap ? vfull : vcap) & ~uint64_t(15);
+        const uint64_t cbytes = (cfull < ccap ? cfull : ccap) & ~uint64_t(15);
+        if (vb) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(A.val + g0 * (S * S)), "r"((uint32_t)vb) : "memory");
+        if (cbytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(A.col + g0), "r"((uint32_t)cbytes) : "memory");
+    }
     pdl_wait();
     pdl_release();
     if (ctl->done) return;
