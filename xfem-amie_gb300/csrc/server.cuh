@@ -97,18 +97,144 @@ __global__ void __launch_bounds__(kVecThreads) kb_sell_pq(const SlotDesc *slots,
 }
 
 // Batched kernel B: per slot x, r, z updates, r.z, r.r; last CTA of the slot:
-// stop test and beta.
+// stop test and beta (update_body's work).  The slot table is written by the
+// host before the batch graph starts, so the slot, its vectors and the loads
+// of the CTA's first step that the SpMV does not produce (x and r, last
+// written by the previous update, which finished before the SpMV could start;
+// D^-1) are issued before the wait on the SpMV, as in k_update.
 template <typename T>
-__global__ void __launch_bounds__(kVecThreads) kb_update(const SlotDesc *slots, const int16_t *cta_slot)
+__global__ void __launch_bounds__(kVecThreads, 3) kb_update(const SlotDesc *slots, const int16_t *cta_slot)
 {
     __shared__ double sh[2 * (kVecThreads >> 5)];
     __shared__ int flag;
+    constexpr int W = Pack<T>::n;
+    const int s = cta_slot[blockIdx.x];
+    const SlotDesc *d = s >= 0 ? slots + s : nullptr;
+    const bool live = d && d->active;
+    T rv[2][W], xv[2][W], dv[2][W];
+    uint64_t tid = 0, stride = 1, npk = 0, n = 0;
+    Cta c{0, 1};
+    if (live) {
+        const PcgVecs<T> &v = slot_v<T>(*d);
+        n = d->n;
+        c = Cta{blockIdx.x - (uint32_t)d->c0, (uint32_t)(d->c1 - d->c0)};
+        const bool al = aligned16(v.x) && aligned16(v.r) && aligned16(v.z) && aligned16(v.p) && aligned16(v.q) &&
+                        aligned16(v.dinv) && (!v.p2 || aligned16(v.p2));
+        tid = (uint64_t)c.id * kVecThreads + threadIdx.x;
+        stride = (uint64_t)c.n * kVecThreads;
+        npk = al ? n / W : 0;
+        if (tid < npk) {
+            ld_pack<T>(v.r, tid, rv[0]);
+            ld_pack<T>(v.x, tid, xv[0]);
+            ldg_pack<T>(v.dinv, tid, dv[0]);
+            if (tid + stride < npk) {
+                ld_pack<T>(v.r, tid + stride, rv[1]);
+                ld_pack<T>(v.x, tid + stride, xv[1]);
+                ldg_pack<T>(v.dinv, tid + stride, dv[1]);
+            }
+        }
+    }
     pdl_wait();
     pdl_release();
-    Cta c;
-    const SlotDesc *d = slot_of(slots, cta_slot, &c);
-    if (!d) return;
-    update_body<T>(slot_v<T>(*d), d->n, d->parts, d->ctl, sh, &flag, c);
+    if (!live) return;
+    PcgCtl *ctl = d->ctl;
+    const int32_t done = ctl->done;
+    const T a = (T)ctl->alpha;
+    const int32_t pcur = ctl->pcur;
+    if (done) return;
+    const PcgVecs<T> &v = slot_v<T>(*d);
+    T *__restrict__ x = v.x;
+    T *__restrict__ r = v.r;
+    T *__restrict__ z = v.z;
+    const T *__restrict__ q = v.q;
+    const T *__restrict__ dinv = v.dinv;
+    // with two direction buffers the SpMV just wrote this iteration's p into the other one
+    const T *__restrict__ p = v.p2 ? (pcur ? v.p : v.p2) : v.p;
+    T drz = T(0), drr = T(0);
+    for (uint64_t k = tid; k < npk; k += 2 * stride) {
+        const uint64_t k2 = k + stride;
+        const bool two = k2 < npk;
+        T qv[2][W], pv[2][W];
+        if (k != tid) {
+            ld_pack<T>(r, k, rv[0]);
+            ld_pack<T>(x, k, xv[0]);
+            ldg_pack<T>(dinv, k, dv[0]);
+            if (two) {
+                ld_pack<T>(r, k2, rv[1]);
+                ld_pack<T>(x, k2, xv[1]);
+                ldg_pack<T>(dinv, k2, dv[1]);
+            }
+        }
+        ld_pack<T>(q, k, qv[0]);
+        ld_pack<T>(p, k, pv[0]);
+        if (two) {
+            ld_pack<T>(q, k2, qv[1]);
+            ld_pack<T>(p, k2, pv[1]);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (h == 1 && !two) break;
+            T zv[W];
+#pragma unroll
+            for (int e = 0; e < W; e++) {
+                rv[h][e] = rv[h][e] - a * qv[h][e];
+                xv[h][e] = fma(a, pv[h][e], xv[h][e]);
+                zv[e] = rv[h][e] * dv[h][e];
+                drz = fma(rv[h][e], zv[e], drz);
+                drr = fma(rv[h][e], rv[h][e], drr);
+            }
+            const uint64_t kk = h ? k2 : k;
+            st_pack<T>(r, kk, rv[h]);
+            st_pack<T>(x, kk, xv[h]);
+            st_pack<T>(z, kk, zv);
+        }
+    }
+    for (uint64_t i = npk * W + tid; i < n; i += stride) {   // tail, or everything when not aligned
+        const T ri = r[i] - a * q[i];
+        x[i] = fma(a, p[i], x[i]);
+        r[i] = ri;
+        const T zi = ri * dinv[i];
+        z[i] = zi;
+        drz = fma(ri, zi, drz);
+        drr = fma(ri, ri, drr);
+    }
+    double brz, brr;
+    block_sum2_v<T>(drz, drr, sh, brz, brr);
+    const PcgParts &parts = d->parts;
+    if (threadIdx.x == 0) {
+        parts.rz[c.id] = brz;
+        parts.rr[c.id] = brr;
+    }
+    if (!last_cta(&ctl->ticket, &flag, c.n)) return;
+    int64_t it = 0, maxit = 0;
+    double rz_old = 0.0, tol2 = 0.0;
+    if (threadIdx.x == 0) {
+        it = ctl->iterations + 1;
+        maxit = ctl->maxit;
+        rz_old = ctl->rz;
+        tol2 = ctl->tol2;
+    }
+    double sa = 0.0, sb = 0.0;
+    for (uint32_t i = threadIdx.x; i < c.n; i += kVecThreads) {
+        sa += __ldcg(parts.rz + i);
+        sb += __ldcg(parts.rr + i);
+    }
+    double rz_new, rr;
+    block_sum2_v<double>(sa, sb, sh, rz_new, rr);
+    if (threadIdx.x == 0) {
+        ctl->iterations = it;
+        ctl->rr = rr;
+        ctl->rz_prev = rz_old;
+        const bool stop = rr <= tol2 || it >= maxit || !(rr == rr);
+        if (stop) {
+            ctl->done = 1;
+        } else {
+            ctl->beta = rz_old != 0.0 ? rz_new / rz_old : 0.0;
+        }
+        ctl->rz = rz_new;
+        if (v.p2) ctl->pcur = pcur ^ 1;   // this iteration's p is now the latest
+        ctl->ticket = 0;
+    }
 }
 
 // Batched kernel C (FP64): per slot p = z + beta p.
