@@ -72,11 +72,15 @@ __device__ __forceinline__ const SlotDesc *slot_of(const SlotDesc *slots, const 
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads) kb_sell_dir(const SlotDesc *slots, const int16_t *cta_slot)
 {
+    // the slot table is the host's, fixed for the whole batch graph: look the
+    // slot up before waiting; only its control block depends on the predecessor
+    const int s = cta_slot[blockIdx.x];
+    const SlotDesc *d = s >= 0 ? slots + s : nullptr;
+    const bool live = d && d->active;
     pdl_wait();
     pdl_release();
-    Cta c;
-    const SlotDesc *d = slot_of(slots, cta_slot, &c);
-    if (!d) return;
+    if (!live || d->ctl->done) return;
+    const Cta c{blockIdx.x - (uint32_t)d->c0, (uint32_t)(d->c1 - d->c0)};
     sell_dir_body<2, T>(slot_A<T>(*d), slot_v<T>(*d), d->parts.pq, d->ctl, true, c);
 }
 
