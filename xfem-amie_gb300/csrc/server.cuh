@@ -138,14 +138,15 @@ __global__ void __launch_bounds__(kVecThreads, 3) kb_update(const SlotDesc *slot
             }
         }
     }
+    // done and pcur are written only by the previous update's last CTA (finished);
+    // alpha comes from the SpMV this kernel waits on
+    PcgCtl *ctl = live ? d->ctl : nullptr;
+    const int32_t done = live ? ctl->done : 1;
+    const int32_t pcur = live ? ctl->pcur : 0;
     pdl_wait();
     pdl_release();
-    if (!live) return;
-    PcgCtl *ctl = d->ctl;
-    const int32_t done = ctl->done;
-    const T a = (T)ctl->alpha;
-    const int32_t pcur = ctl->pcur;
     if (done) return;
+    const T a = (T)ctl->alpha;
     const PcgVecs<T> &v = slot_v<T>(*d);
     T *__restrict__ x = v.x;
     T *__restrict__ r = v.r;

@@ -1105,12 +1105,14 @@ __global__ void __launch_bounds__(kVecThreads, sizeof(T) == 4 ? 4 : 3)
             ldg_pack<T>(d, tid + stride, dv[1]);
         }
     }
+    // done and pcur are written only by the previous update's last CTA (finished,
+    // like x and r); alpha comes from the SpMV this kernel waits on
+    const int32_t done = ctl->done;
+    const int32_t pcur = ctl->pcur;
     pdl_wait();
     pdl_release();
-    const int32_t done = ctl->done;
-    const T a = (T)ctl->alpha;
-    const int32_t pcur = ctl->pcur;
     if (done) return;
+    const T a = (T)ctl->alpha;
     // with two direction buffers the SpMV just wrote this iteration's p into the other one
     const T *__restrict__ p = v.p2 ? (pcur ? v.p : v.p2) : v.p;
     T drz = T(0), drr = T(0);   // per-thread partials in the vector precision, CTA sums in FP64
