@@ -309,6 +309,8 @@ __device__ __forceinline__ void row_spmv(const BsrView<T> &A, const T *__restric
 template <typename T, bool CG = false>
 __device__ __forceinline__ void finish_pq(T dot_t, double *part_pq, PcgCtl *fin, double *sh, int *flag, Cta c)
 {
+    // r.z was stored by the previous update: fetched now, it arrives during the reductions
+    const double rz = (fin && threadIdx.x == 0) ? ctl_ld<CG>(&fin->rz) : 0.0;
     const double dot = block_sum_v<T>(dot_t, sh);
     if (threadIdx.x == 0) part_pq[c.id] = dot;
     if (!fin) return;
@@ -316,7 +318,7 @@ __device__ __forceinline__ void finish_pq(T dot_t, double *part_pq, PcgCtl *fin,
     const double pq = ordered_sum(part_pq, c.n, sh);
     if (threadIdx.x == 0) {
         fin->pq = pq;
-        fin->alpha = pq != 0.0 ? ctl_ld<CG>(&fin->rz) / pq : 0.0;
+        fin->alpha = pq != 0.0 ? rz / pq : 0.0;
         fin->ticket = 0;
     }
 }
