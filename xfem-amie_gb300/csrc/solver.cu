@@ -54,7 +54,8 @@ struct SolverState {
     // AMIE_MATRIX_HINT overrides it for measurements
     int matrix_hint = kMatrixHint;
     // bytes of each CTA's matrix range k_sell_dir prefetches into L2 before its wait
-    // (AMIE_PREFETCH_KB; cfg1 step: 0 KB 686 ms, 16 KB 673 ms, 32-64 KB 674 ms, 128 KB 688 ms)
+    // (AMIE_PREFETCH_KB; mixed solve of the 1.2 M-DOF P2 problem: 0 KB 686 ms, 16 KB 673 ms,
+    // 32-64 KB 674 ms, 128 KB 688 ms)
     uint32_t prefetch_bytes = 16u << 10;
     int graph_kernels[2] = {3, 3};   // kernels per iteration of the FP32 / FP64 graph
     DevArray<double> parts;       // 4 * stride: pq, rz, rr, spare

@@ -368,7 +368,8 @@ __global__ void __launch_bounds__(kVecThreads) k_spmv_pq(PcgVecs<T> v, double *p
 // vectors out of L2.  Measured on the 1.2 M-DOF P2 problem (FP32 matrix 150 MB,
 // vectors 29 MB): the SpMV+direction kernel takes 32.1 us with 0, 26.7 us
 // with 1 (the vector gathers and the next kernel's reads stay in L2) and
-// 45 us with 2; 1 is the default everywhere.
+// 45 us with 2.  1 is the default of the single-solve kernels; the batched
+// server passes 0, its small matrices being re-read from L2 every iteration.
 constexpr int kMatrixHint = 1;
 template <int HINT>
 __device__ __forceinline__ uint64_t stream_policy()
@@ -638,7 +639,8 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
 // iteration from L2, and evict-first lines there raised the serving p99 from
 // 0.28 s to 0.45 s).  The single-solve kernel below is kept as its own copy: with the
 // group position and the views held as values the compiler keeps fewer loads in
-// flight at the kernel's 64-register budget (49 us instead of 33 us on cfg1).
+// flight at the kernel's 64-register budget (49 us instead of 33 us on the
+// 1.2 M-DOF P2 problem).
 template <int S, typename T, bool CG = false>
 __device__ __forceinline__ void sell_dir_body(const SellView<T> &A, const PcgVecs<T> &v, double *part_pq, PcgCtl *ctl,
                                               bool fin, Cta cta)
