@@ -516,7 +516,8 @@ def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 6
     each load step updates the scalar damage on the device from the last
     solution (Mazars equivalent strain, eps0 = 1e-4, exponential softening),
     re-integrates (1 - d) C, eliminates the new imposed deflection and solves
-    warm-started from the previous displacement (all device-resident)."""
+    warm-started as Assembly::cgsolve does, from the extrapolated displacement
+    2 u_(k-1) - u_(k-2) (all device-resident)."""
     import amie_gpu as G
     m, bcs_at, meta = W.notched_beam()
     topo = G.Topology(ctx, m)
@@ -528,6 +529,8 @@ def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 6
             nc, _ = topo.damage_step(eps0=1e-4, softening=3000.0, d_max=0.999, want_damage=False)
             changed.append(nc)
         topo.apply_dirichlet(*bcs_at(deflection_max * k / steps))   # scatter (1-d) C + elimination
+        if k > 1:
+            topo.extrapolate()
         st = topo.solve_resident(solver, rtol=1e-10, use_x0=k > 1)
         iters.append(st["iterations"])
     ms = ctx.timer_stop()

@@ -200,6 +200,13 @@ AMIE_API amie_status amie_solve(amie_topo *topo, const amie_solve_opts *opts, do
  * copies); read the solution with amie_solution_download. */
 AMIE_API amie_status amie_solve_resident(amie_topo *topo, const amie_solve_opts *opts, amie_solve_stats *stats);
 AMIE_API amie_status amie_solution_download(const amie_topo *topo, double *x);
+/* Warm start of the next amie_solve_resident (with use_x0) by the reference's
+ * displacement-history extrapolation, Assembly::extrapolate (factor 1,
+ * solvers/assembly.cpp:1772-1814) as cgsolve uses it (:1850-1867): the device
+ * solution x becomes 2 x - x_prev and x_prev becomes x.  x_prev starts at zero,
+ * like the history [0, u1] the reference keeps after its first solve; call it
+ * once between consecutive solves of the same topology. */
+AMIE_API amie_status amie_extrapolate(amie_topo *topo);
 
 /* Jacobi-PCG (FP64, relative-residual stop) on a block-CSR matrix the caller
  * already holds in device memory, without allocating any device memory.  No

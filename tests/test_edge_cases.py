@@ -6,7 +6,9 @@
 * a single element: pattern, matrix and right-hand side as the oracle's;
 * a zero right-hand side: every solver returns x = 0 after no iteration;
 * every DOF prescribed: every solver returns the prescribed values;
-* the mixed solver at an iteration cap reports AMIE_NOT_CONVERGED.
+* the mixed solver at an iteration cap reports AMIE_NOT_CONVERGED;
+* the extrapolated warm start (amie_extrapolate) follows the reference's
+  displacement history.
 """
 import numpy as np
 import pytest
@@ -155,3 +157,31 @@ def test_mixed_iteration_cap_reports_not_converged(gpu_ctx):
     assert st["status"] == amie_gpu.AMIE_NOT_CONVERGED
     assert 0 < st["iterations"] <= 20 + 16
     assert np.all(np.isfinite(x))
+
+
+def test_extrapolated_warm_start(gpu_ctx):
+    """amie_extrapolate follows Assembly::extrapolate: after the first solve the
+    next start is 2 u1 (history [0, u1]), then 2 u2 - u1; on a linear problem
+    loaded proportionally the extrapolated start is the solution, so the warm
+    solve needs far fewer iterations than the first."""
+    import amie_gpu
+    d = load_golden("incl_p1")
+    m = am.from_golden(d, "tabulated")
+    ids, vals, kinds = am.golden_bcs(d)
+    t = amie_gpu.Topology(gpu_ctx, m)
+    try:
+        t.assemble()
+        t.apply_dirichlet(ids, vals, kinds)
+        st1 = t.solve_resident(amie_gpu.SOLVER_PCG_FP64, rtol=1e-12)
+        u1 = t.solution()
+        t.apply_dirichlet(ids, 2 * vals, kinds)
+        t.extrapolate()
+        assert np.array_equal(t.solution(), u1 + u1)
+        st2 = t.solve_resident(amie_gpu.SOLVER_PCG_FP64, rtol=1e-12, use_x0=True)
+        u2 = t.solution()
+        assert rel(u2, 2 * u1) <= 1e-10
+        assert st2["iterations"] < st1["iterations"] // 4
+        t.extrapolate()
+        assert np.array_equal(t.solution(), u2 + (u2 - u1))
+    finally:
+        t.close()

@@ -35,7 +35,7 @@ EXPORTED = [
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
     "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step", "amie_pcg_solve_noalloc",
     "amie_topology_spmv_lanes", "amie_profile_stream", "amie_average_field", "amie_set_imposed_strain",
-    "amie_server_query", "amie_cut_rules",
+    "amie_server_query", "amie_cut_rules", "amie_extrapolate",
 ]
 
 
@@ -291,6 +291,10 @@ class Topology:
         check(rc, "amie_solve_resident", ok=accept)
         return st.as_dict()
 
+    def extrapolate(self):
+        """Device warm start 2 x - x_prev for the next resident solve (Assembly::extrapolate)."""
+        check(lib().amie_extrapolate(self.ptr), "amie_extrapolate")
+
     def solution(self):
         x = np.zeros(self.n, np.float64)
         check(lib().amie_solution_download(self.ptr, _p(x)), "amie_solution_download")
@@ -485,9 +489,11 @@ class Assembly:
         self.topo.apply_dirichlet(ids, vals, kinds)
 
     def extrapolate(self):
+        """Assembly::extrapolate (factor 1): 2 u_k - u_(k-1) from the two-entry
+        history, which the reference starts as [0, u_1] after its first solve."""
         if len(self.history) < 2:
             return self.displacements if len(self.displacements) else None
-        a, b = self.history[-2], self.history[-1]
+        a, b = self.history[-2], np.nan_to_num(self.history[-1], nan=0.0)
         return b + (b - a)
 
     def cgsolve(self, maxit: int = -1) -> bool:
@@ -498,7 +504,7 @@ class Assembly:
         x, st = self.topo.solve(self.solver, rtol=self.rtol, x0=x0, maxit=max(maxit, 0), eps=self.epsilon,
                                 nssor=self.nssor, accept=(AMIE_OK, AMIE_NOT_CONVERGED))
         self.displacements = x
-        self.history = (self.history + [x])[-2:]
+        self.history = [self.history[-1], x] if len(self.history) == 2 else [np.zeros_like(x), x]
         self.last_stats = st
         return st["status"] == AMIE_OK
 

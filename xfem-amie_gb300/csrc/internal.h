@@ -201,6 +201,7 @@ struct amie_topo {
     amie::DevArray<uint8_t> fixed;
     amie::DevArray<double> fixval;
     amie::DevArray<double> strain, damage, cscale_base;   // field recovery and damage loop
+    amie::DevArray<double> x_hist;    // previous solution for amie_extrapolate (zero until first used)
     // imposed strain (per element) and its induced forces: staged per element
     // function, gathered per block row through fmap (contributions in element order)
     amie::DevArray<double> imposed, fstage;

@@ -670,6 +670,36 @@ extern "C" amie_status amie_solve(amie_topo *t, const amie_solve_opts *o, double
     return (amie_status)sp->status;
 }
 
+namespace amie {
+
+// x <- 2 x - x_hist, x_hist <- x (a NaN entry of x counts as 0): the
+// displacement history step of Assembly::extrapolate with factor 1.
+__global__ void k_extrapolate(uint64_t n, double *x, double *hist)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double u = x[i] == x[i] ? x[i] : 0.0;
+        x[i] = u + (u - hist[i]);
+        hist[i] = u;
+    }
+}
+
+}  // namespace amie
+
+extern "C" amie_status amie_extrapolate(amie_topo *t)
+{
+    if (!t || !t->x.p) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    cudaStream_t st = t->ctx->stream;
+    if (!t->x_hist.p) {
+        AMIE_TRY(t->x_hist.alloc(t->ctx, t->n));
+        AMIE_CUDA(cudaMemsetAsync(t->x_hist.p, 0, t->n * 8, st));
+    }
+    k_extrapolate<<<t->ctx->num_sms * 4, 256, 0, st>>>(t->n, t->x.p, t->x_hist.p);
+    AMIE_LAUNCHED();
+    AMIE_CUDA(cudaGetLastError());
+    return AMIE_OK;
+}
+
 extern "C" amie_status amie_solution_download(const amie_topo *t, double *x)
 {
     if (!t || !x) return AMIE_BAD_INPUT;

@@ -1,6 +1,8 @@
 // gpu_assembly.cpp -- see gpu_assembly.hpp.
 #include "gpu_assembly.hpp"
 
+#include <cmath>
+
 #include <algorithm>
 
 namespace gpu {
@@ -173,7 +175,10 @@ std::vector<double> Assembly::extrapolate() const
     if (history_.size() < 2) return displacements_;
     const auto &a = history_[history_.size() - 2], &b = history_.back();
     std::vector<double> x(b.size());
-    for (size_t i = 0; i < b.size(); i++) x[i] = b[i] + (b[i] - a[i]);
+    for (size_t i = 0; i < b.size(); i++) {
+        const double u = std::isnan(b[i]) ? 0.0 : b[i];
+        x[i] = u + (u - a[i]);
+    }
     return x;
 }
 
@@ -196,8 +201,13 @@ bool Assembly::cgsolve(int maxit, bool verbose)
     amie_status s = amie_solve(topo_, &o, x.data(), &stats_);
     if (s != AMIE_OK && s != AMIE_NOT_CONVERGED) check(s, "amie_solve");
     displacements_ = x;
-    history_.push_back(x);
-    if (history_.size() > 2) history_.erase(history_.begin());
+    // the reference keeps two entries and starts them as [0, u1] (solvers/assembly.cpp:1859-1867)
+    if (history_.size() == 2) {
+        history_[0] = history_[1];
+        history_[1] = x;
+    } else {
+        history_.assign({std::vector<double>(x.size(), 0.0), x});
+    }
     return s == AMIE_OK;
 }
 
