@@ -67,7 +67,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample length")
-    ap.add_argument("--serve", type=int, default=256, help="serving-mix requests (0 = skip)")
+    ap.add_argument("--serve", type=int, default=4096, help="serving-mix requests (0 = skip)")
+    ap.add_argument("--serve-iters", type=int, default=0, help="serving: PCG iterations per batch graph "
+                                                                "(0 = library default)")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving mix (--serve requests) and print "
                                                               "its statistics (for an ncu launch list of the server)")
     ap.add_argument("--profile", action="store_true", help="assemble once and launch the SpMV kernels a few times "
@@ -306,7 +308,7 @@ def run_ours(args, world, rank, local, dist):
     ctx = G.Context(local)
     solver = G.SOLVER_PCG_MIXED if args.solver == "mixed" else G.SOLVER_PCG_FP64
     if args.serve_only:
-        print(json.dumps({"serving": run_serving(ctx, args.serve, args.serve_rate, solver)}))
+        print(json.dumps({"serving": run_serving(ctx, args.serve, args.serve_rate, solver, iters=args.serve_iters)}))
         ctx.close()
         return 0
     m, bcs, meta, name = make_workload(args.config, args.size)
@@ -446,7 +448,7 @@ def run_ours(args, world, rank, local, dist):
 
     # serving mix (config 4): p50 / p99 latency next to throughput
     if args.serve > 0:
-        result["serving"] = run_serving(ctx, args.serve, args.serve_rate, solver)
+        result["serving"] = run_serving(ctx, args.serve, args.serve_rate, solver, iters=args.serve_iters)
     # damage loop (config 3)
     if args.damage_steps > 0:
         result["damage_loop"] = run_damage_loop(ctx, solver, args.damage_steps)
@@ -468,13 +470,13 @@ def run_ours(args, world, rank, local, dist):
     return 0
 
 
-def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, pool: int = 32):
+def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, pool: int = 32, iters: int = 0):
     """Config-4 serving mix: Poisson arrivals of independent homogenisation solves
     (log-uniform 2k-200k DOF, inclusion fraction U[0.2, 0.6]) into the
     continuous-batching server.  Returns p50/p99 latency and solves/s."""
     import amie_gpu as G
     meshes, arrivals, which = W.serving_mix(n_requests, rate, seed=seed, pool=pool)
-    srv = G.Server(ctx, solver=solver, rtol=1e-10)
+    srv = G.Server(ctx, solver=solver, rtol=1e-10, iters_per_launch=iters)
     # warm the server (graph, first allocations) with one request
     t = srv.submit(meshes[0][0], *meshes[0][1])
     srv.drain(60.0)

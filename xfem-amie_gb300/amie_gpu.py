@@ -344,10 +344,11 @@ class Topology:
 class Server:
     """Continuous-batching solve server (amie_server_* of the C-ABI)."""
 
-    def __init__(self, ctx: Context, solver=SOLVER_PCG_MIXED, rtol=1e-10, hbm_budget_bytes=0, max_slots=0):
+    def __init__(self, ctx: Context, solver=SOLVER_PCG_MIXED, rtol=1e-10, hbm_budget_bytes=0, max_slots=0,
+                 iters_per_launch=0):
         self.ctx = ctx
         self.ptr = C.c_void_p()
-        cfg = ServerConfig(solver, rtol, hbm_budget_bytes, max_slots, 0)
+        cfg = ServerConfig(solver, rtol, hbm_budget_bytes, max_slots, iters_per_launch)
         check(lib().amie_server_start(ctx.ptr, C.byref(cfg), C.byref(self.ptr)), "amie_server_start")
         self._keep = {}
         self._n = {}

@@ -681,7 +681,7 @@ struct ServerOps {
         const int g = srv->grid;
         cudaGraph_t graph;
         AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        for (int it = 0; it < kBatchIters; it++) {
+        for (int it = 0; it < srv->cfg.iters_per_launch; it++) {
             const bool pdl = it > 0;   // the first kernel follows the host's updates in plain stream order
             if (srv->mixed) {
                 launch_k(pdl, kb_sell_dir<float>, g, 0, st, sl, cs);
@@ -785,7 +785,7 @@ struct ServerOps {
                     cudaMemsetAsync(srv->d_bar.p, 0, srv->slot_req.size() * sizeof(uint32_t), st);
                     const SlotDesc *sl = srv->d_slots.p;
                     const int16_t *cs = srv->d_cta_slot.p;
-                    int iters = kBatchIters;
+                    int iters = srv->cfg.iters_per_launch;
                     uint32_t *bar = srv->d_bar.p;
                     int32_t *err = srv->d_err.p;
                     void *args[] = {(void *)&sl, (void *)&cs, (void *)&iters, (void *)&bar, (void *)&err};
@@ -807,7 +807,7 @@ struct ServerOps {
                     cudaMemcpyAsync(srv->h_err, srv->d_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
                 } else {
                     cudaGraphLaunch(srv->graph, st);
-                    g_launches += (srv->mixed ? 2 : 3) * kBatchIters;
+                    g_launches += (srv->mixed ? 2 : 3) * srv->cfg.iters_per_launch;
                 }
                 cudaMemcpyAsync(srv->h_ctl, srv->d_ctl.p, srv->slot_req.size() * sizeof(PcgCtl), cudaMemcpyDeviceToHost,
                                 st);
@@ -908,7 +908,8 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
     if (c.rtol <= 0) c.rtol = 1e-10;
     if (c.max_slots <= 0) c.max_slots = 256;
     c.max_slots = std::min(c.max_slots, 1024);
-    c.iters_per_launch = kBatchIters;
+    if (c.iters_per_launch <= 0) c.iters_per_launch = kBatchIters;
+    c.iters_per_launch = std::min(c.iters_per_launch, 256);
     if (c.solver != AMIE_SOLVER_PCG_MIXED && c.solver != AMIE_SOLVER_PCG_FP64) {
         delete srv;
         set_error("server solver must be PCG_FP64 or PCG_MIXED");
