@@ -416,7 +416,6 @@ __global__ void k_sell_fill(uint32_t n_rows, uint32_t n_slices, const uint32_t *
 template <int S, typename T>
 __global__ void k_to_sell(uint64_t n_slots, const uint32_t *sell_blk, const double *val, T *out)
 {
-    constexpr int V = kSellVec<S, T>;
     for (uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots;
          slot += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t blk = sell_blk[slot];
@@ -425,7 +424,7 @@ __global__ void k_to_sell(uint64_t n_slots, const uint32_t *sell_blk, const doub
 #pragma unroll
         for (int c = 0; c < S * S; c++) {
             const double v = blk != kSellNone ? val[(uint64_t)blk * (S * S) + c] : 0.0;
-            group[32 * V * (c / V) + V * lane + c % V] = (T)v;
+            group[sell_off<S, T>(c, (int)lane)] = (T)v;
         }
     }
 }

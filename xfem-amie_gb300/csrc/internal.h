@@ -120,13 +120,23 @@ struct BsrView {
 // cut into slices of 32; slice k holds 32 rows padded to its longest row, its
 // slots stored j-major (slot = slice_ptr[k] + 32 j + lane) so a warp reads the
 // j-th block of its 32 rows from one contiguous run.  Values of the 32 blocks
-// of one j are stored in chunks of kSellVec<S,T> components: component c of
-// lane l at val[32*S*S*(group) + 32*V*(c / V) + V*l + c % V].  Padding slots
+// of one j are stored in chunks of kSellVec<S,T> components, each chunk lane
+// by lane: chunk k holds components kV .. kV+w-1 (w = min(V, S*S - kV)), and
+// component c of lane l sits at val[32*S*S*(group) + 32*V*(c / V) + w*l + c % V]
+// (sell_off), so a lane loads a chunk with one 16-byte access.  Padding slots
 // have zero values and the row's own column (no effect on the result).
 constexpr uint32_t kSellSigma = 128;
 constexpr uint32_t kSellNone = 0xffffffffu;
 template <int S, typename T>
-constexpr int kSellVec = S == 2 ? int(16 / sizeof(T)) : 1;
+constexpr int kSellVec = int(16 / sizeof(T)) > S * S ? 1 : (S == 2 || sizeof(T) == 4 ? int(16 / sizeof(T)) : 1);
+template <int S, typename T>
+__host__ __device__ constexpr int sell_off(int c, int lane)
+{
+    constexpr int V = kSellVec<S, T>;
+    const int k = c / V;
+    const int w = (S * S - k * V) < V ? (S * S - k * V) : V;
+    return 32 * V * k + w * lane + c % V;
+}
 
 template <typename T>
 struct SellView {

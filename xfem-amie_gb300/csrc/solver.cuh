@@ -417,9 +417,16 @@ __device__ __forceinline__ void load_sell_block(const T *__restrict__ group, uin
         const double2 a = ld_stream<HINT>(reinterpret_cast<const double2 *>(group) + lane, pol);
         const double2 b = ld_stream<HINT>(reinterpret_cast<const double2 *>(group + 64) + lane, pol);
         blk[0] = a.x; blk[1] = a.y; blk[2] = b.x; blk[3] = b.y;
+    } else if constexpr (S == 3 && V == 4) {
+        // components 0-3 and 4-7 as two 16-byte chunks, component 8 on its own
+        const float4 a = ld_stream<HINT>(reinterpret_cast<const float4 *>(group) + lane, pol);
+        const float4 b = ld_stream<HINT>(reinterpret_cast<const float4 *>(group + 128) + lane, pol);
+        blk[0] = a.x; blk[1] = a.y; blk[2] = a.z; blk[3] = a.w;
+        blk[4] = b.x; blk[5] = b.y; blk[6] = b.z; blk[7] = b.w;
+        blk[8] = ld_stream<HINT>(group + 256 + lane, pol);
     } else {
 #pragma unroll
-        for (int c = 0; c < S * S; c++) blk[c] = ld_stream<HINT>(group + 32 * c + lane, pol);
+        for (int c = 0; c < S * S; c++) blk[c] = ld_stream<HINT>(group + sell_off<S, T>(c, (int)lane), pol);
     }
 }
 
@@ -748,7 +755,7 @@ __device__ __forceinline__ void load_sell_block_sm(const T *group, uint32_t lane
         blk[0] = a.x; blk[1] = a.y; blk[2] = b.x; blk[3] = b.y;
     } else {
 #pragma unroll
-        for (int c = 0; c < S * S; c++) blk[c] = group[32 * c + lane];
+        for (int c = 0; c < S * S; c++) blk[c] = group[sell_off<S, T>(c, (int)lane)];
     }
 }
 
