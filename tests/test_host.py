@@ -66,3 +66,22 @@ def test_mesh_validation_and_offsets():
     bad.enr_ptr[-1] += 1
     with pytest.raises(AssertionError):
         bad.validate()
+
+
+def test_assembly_history_follows_the_reference():
+    """Assembly.extrapolate / the history kept after each solve, as
+    Assembly::extrapolate (solvers/assembly.cpp:1772-1814) and cgsolve
+    (:1856-1867): nothing before the first solve, 2 u1 after it (history
+    [0, u1]), then 2 u_k - u_(k-1); a NaN in the last solution counts as 0."""
+    import amie_gpu
+    a = object.__new__(amie_gpu.Assembly)   # no device needed for the history
+    a.history, a.displacements = [], np.zeros(0)
+    assert a.extrapolate() is None
+    u1 = np.array([1.0, -2.0, 0.5])
+    a._record(u1)
+    assert np.array_equal(a.extrapolate(), 2 * u1)
+    u2 = np.array([2.0, np.nan, 1.0])
+    a._record(u2)
+    assert np.array_equal(a.extrapolate(), np.array([3.0, 2.0, 1.5]))
+    a._record(u1)
+    assert len(a.history) == 2 and a.history[0] is u2

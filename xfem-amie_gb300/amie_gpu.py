@@ -497,6 +497,12 @@ class Assembly:
         a, b = self.history[-2], np.nan_to_num(self.history[-1], nan=0.0)
         return b + (b - a)
 
+    def _record(self, x):
+        """Displacements and history after a solve (solvers/assembly.cpp:1856-1867):
+        two entries, starting as [0, u_1]."""
+        self.displacements = x
+        self.history = [self.history[-1], x] if len(self.history) == 2 else [np.zeros_like(x), x]
+
     def cgsolve(self, maxit: int = -1) -> bool:
         self.make_final()
         x0 = self.extrapolate()
@@ -504,8 +510,7 @@ class Assembly:
             x0 = None
         x, st = self.topo.solve(self.solver, rtol=self.rtol, x0=x0, maxit=max(maxit, 0), eps=self.epsilon,
                                 nssor=self.nssor, accept=(AMIE_OK, AMIE_NOT_CONVERGED))
-        self.displacements = x
-        self.history = [self.history[-1], x] if len(self.history) == 2 else [np.zeros_like(x), x]
+        self._record(x)
         self.last_stats = st
         return st["status"] == AMIE_OK
 
