@@ -121,6 +121,23 @@ def spmv_bytes(nnzb: int, n_rows: int, s: int, w: int, fold: bool = False) -> in
     return nnzb * (s * s * w + 4) + 4 * (n_rows + 1) + (4 if fold else 2) * n_rows * s * w
 
 
+def assembly_bytes(m: am.MeshData, topo) -> dict:
+    """Algorithmic bytes of one assembly: staged element matrices written and
+    read ((nf s)^2 doubles each way), the scatter map read (4 B per staged
+    block), the block values written (nnzb s^2 doubles) and the element inputs
+    read once; plus the Dirichlet elimination's read and write of the blocks."""
+    s = m.stride
+    nf = np.diff(m.dof_ptr.astype(np.int64))
+    ke = int(((nf * s) ** 2).sum()) * 8
+    contrib = int((nf ** 2).sum())
+    vals = int(topo.nnzb) * s * s * 8
+    inputs = mesh_bytes(m)
+    parts = {"ke_write_read": 2 * ke, "map": 4 * contrib, "values_write": vals, "inputs": inputs,
+             "elimination": 2 * vals}
+    parts["total"] = sum(parts.values())
+    return parts
+
+
 def load_peaks():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -371,17 +388,21 @@ def run_ours(args, world, rank, local, dist):
     # FP64 plain path on the same matrix: throughput and the reference solution for the error statement
     ms64, st64 = step(G.SOLVER_PCG_FP64, args.rtol)
     x64 = topo.solution()
-    ms_tight, st_tight = step(G.SOLVER_PCG_FP64, 1e-12)
+    ms_tight, st_tight = step(G.SOLVER_PCG_FP64, 1e-13)
     x_tight = topo.solution()
     node_dofs = slice(0, meta.get("n_nodes", n // m.stride) * m.stride)
     err_mixed = float(np.abs(x_mixed[node_dofs] - x_tight[node_dofs]).max() / np.abs(x_tight[node_dofs]).max())
     err_fp64 = float(np.abs(x64[node_dofs] - x_tight[node_dofs]).max() / np.abs(x_tight[node_dofs]).max())
     fp64_value = n * st64["iterations"] / (ms64 / 1e3)
 
-    # assembly alone (quadrature + gather + elimination) and solve-only rates
-    ctx.timer_start()
-    topo.assemble()
-    ms_asm = ctx.timer_stop()
+    # assembly alone (quadrature + gather + elimination + solver copies), best of a few
+    ms_asm = []
+    for _ in range(5):
+        ctx.timer_start()
+        topo.assemble()
+        ms_asm.append(ctx.timer_stop())
+    ms_asm = min(ms_asm)
+    asm_alg = assembly_bytes(m, topo)
 
     # dominant kernel: block SpMV of the inner solve (FP32 for mixed, FP64 otherwise)
     prec = 32 if solver == G.SOLVER_PCG_MIXED else 64
@@ -408,12 +429,17 @@ def run_ours(args, world, rank, local, dist):
                    **_cfg_meta(meta)},
         "solve": {"iterations": iters, "refinements": [s["refinements"] for s in stats],
                   "relres": [s["relres"] for s in stats], "ms_per_step": times,
-                  "err_vs_fp64_1e-12": err_mixed},
+                  "err_vs_fp64_1e-13": err_mixed, "err_bound": 1e-8, "err_margin": 1e-8 / max(err_mixed, 1e-300)},
         "fp64": {"value": fp64_value, "iterations": st64["iterations"], "ms": ms64, "relres": st64["relres"],
-                 "err_vs_fp64_1e-12": err_fp64},
+                 "err_vs_fp64_1e-13": err_fp64, "err_bound": 1e-9, "err_margin": 1e-9 / max(err_fp64, 1e-300)},
+        "time_to_solution_vs_fp64": ms64 / (t_local * 1e3 / args.steps) if solver == G.SOLVER_PCG_MIXED else 1.0,
         "mixed_vs_fp64_dof_it": value / world / fp64_value if solver == G.SOLVER_PCG_MIXED else 1.0,
         "mixed_vs_fp64_solve_time": ms64 / (t_local * 1e3 / args.steps) if solver == G.SOLVER_PCG_MIXED else 1.0,
         "assembly_ms": ms_asm,
+        "roofline_assembly": {"bound": "hbm", "alg_bytes": asm_alg["total"], "parts": asm_alg,
+                              "achieved": asm_alg["total"] / (ms_asm / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                              "frac": asm_alg["total"] / (ms_asm / 1e3) / 1e9 / peak,
+                              "timed": "quadrature + gather + Dirichlet elimination + FP32/FP64 solver copies"},
         "roofline": {"bound": "hbm",
                      "kernel": f"{'k_sell_dir' if fold_dir() and w == 4 else 'k_sell_pq'}<{m.stride},{'float' if w == 4 else 'double'}>",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -211,13 +211,16 @@ AMIE_API amie_status amie_extrapolate(amie_topo *topo);
 /* Jacobi-PCG (FP64, relative-residual stop) on a block-CSR matrix the caller
  * already holds in device memory, without allocating any device memory.  No
  * counterpart in the reference.  For callers that cannot call cudaMalloc at
- * solve time: code running during a CUDA graph capture that forbids
- * allocation, applications whose own pool owns all device memory, real-time
- * loops that cannot take an allocation's implicit synchronisation.
+ * solve time: applications whose own pool allocator took all device memory at
+ * start-up (an allocation here would fail or break their accounting), and
+ * real-time loops that cannot take the device-wide synchronisation that
+ * cudaMalloc / cudaFree may cause.
  *   Matrix: row_ptr_dev [n_rows+1], col_dev [nnzb], val_dev [nnzb*s*s] (s x s
- *   blocks row-major, this library's device layout), b_dev, x_dev [n_rows*s];
- *   x_dev is the warm start if use_x0, the solution on return.  stream: a
- *   cudaStream_t, or NULL for the default stream.
+ *   blocks row-major, this library's device layout; columns of a row in any
+ *   order, each at most once), b_dev, x_dev [n_rows*s]; x_dev is the warm
+ *   start if use_x0, the solution on return.  stream: a cudaStream_t, or NULL
+ *   for the default stream.  The call returns when the solve is finished: it
+ *   synchronises `stream` to read the solver's progress.
  *   Limit: n_rows * stride <= 262144 scalar DOFs; larger systems return
  *   AMIE_BAD_INPUT.  The work vectors live in one static device array of about
  *   10.5 MB that every GPU loading this library reserves until exit.

@@ -25,8 +25,19 @@
 //   * the ConjugateGradient solution driven exactly as Assembly::cgsolve does
 //     (solvers/assembly.cpp:1829-1850), its iteration count and wall time.
 //
+// Case `damage` (config-3 family): a notched beam in three-point bending with
+// StiffnessAndFracture (physics/stiffness_and_fracture.cpp) graded by
+// NonLocalMazars (physics/fracturecriteria/mazars.cpp:73-147) and damaged by
+// FiberBasedIsotropicLinearDamage (the StiffnessAndFracture default,
+// physics/damagemodels/fiberbasedisotropiclineardamage.cpp) or
+// IsotropicLinearDamage (model=iso); FeatureTree::step per load step.  Exports
+// the element data of the undamaged beam, each element's centre, circumradius
+// and area, the supports and the load patch, and after every load step the
+// displacements, the damage (1 - C_eff/C), the criterion's score and the
+// smoothed principal stress and strain of every element.
+//
 // Usage:  ref_harness <case> <out.bin> [key=value ...]
-//   case = incl | crack | voxel
+//   case = incl | crack | voxel | plate | imposed | damage
 //   keys: sampling, order (1|2), ninc, seed, E, nu, Einc, disp, size, crack_y,
 //         n, nphase, sigma_log, strain
 
@@ -37,6 +48,11 @@
 #include "features/crack.h"
 #include "physics/stiffness.h"
 #include "physics/stiffness_with_imposed_deformation.h"
+#include "physics/stiffness_and_fracture.h"
+#include "physics/fracturecriteria/mazars.h"
+#include "physics/damagemodels/isotropiclineardamage.h"
+#include "physics/damagemodels/fiberbasedisotropiclineardamage.h"
+#include "physics/void_form.h"
 #include "utilities/placement.h"
 #include "solvers/assembly.h"
 #include "solvers/conjugategradient.h"
@@ -410,6 +426,114 @@ int run_voxel(Out &o, std::map<std::string, std::string> &kv)
     return 0;
 }
 
+
+// Config-3 family: notched beam, damage by load steps through FeatureTree::step.
+int run_damage(Out &o, std::map<std::string, std::string> &kv)
+{
+    const double Lb = getd(kv, "length", 0.08), Hb = getd(kv, "height", 0.02);
+    const double nw = getd(kv, "notch_w", 0.004), nh = getd(kv, "notch_h", 0.002);
+    const double E = getd(kv, "E", 35e9), nu = getd(kv, "nu", 0.2);
+    const double thr = getd(kv, "eps0", 1e-4), Gf = getd(kv, "Gf", 100.0), R = getd(kv, "radius", 0.002);
+    const double patch = getd(kv, "patch", 0.004);
+    const double dmax = getd(kv, "deflection", 2e-5);
+    const int steps = (int)getd(kv, "steps", 6);
+    const int model = (int)getd(kv, "model", 0);   // 0 FiberBasedIsotropicLinearDamage, 1 IsotropicLinearDamage
+    const double fibre = getd(kv, "fibre", 0.1), cutoff = getd(kv, "cutoff", 0.6);
+    const double sampling = getd(kv, "sampling", 32);
+    const int maxit = (int)getd(kv, "maxit", 200);
+
+    RectangularFeature box(nullptr, Lb, Hb, 0, 0);
+    DamageModel *dm = model == 1 ? (DamageModel *)new IsotropicLinearDamage()
+                                 : (DamageModel *)new FiberBasedIsotropicLinearDamage(fibre, cutoff);
+    box.setBehaviour(new StiffnessAndFracture(E, nu, new NonLocalMazars(thr, E, nu, Gf, R, PLANE_STRESS), dm,
+                                              SPACE_TWO_DIMENSIONAL, PLANE_STRESS));
+    FeatureTree F(&box);
+    // the notch: a void rectangle centred on the bottom edge at midspan (examples/main_tension_benchmark.cpp:124-127)
+    RectangularFeature *notch = new RectangularFeature(nullptr, nw, 2 * nh, 0., -Hb / 2);
+    notch->setBehaviour(new VoidForm());
+    F.addFeature(&box, notch);
+    F.setSamplingNumber(sampling);
+    F.setMaxIterationsPerStep(maxit);
+    F.addBoundaryCondition(new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, BOTTOM_LEFT));
+    F.addBoundaryCondition(new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM_LEFT));
+    F.addBoundaryCondition(new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM_RIGHT));
+    BoundingBoxAndRestrictionDefinedBoundaryCondition *load = new BoundingBoxAndRestrictionDefinedBoundaryCondition(
+        SET_ALONG_ETA, TOP, -patch / 2, patch / 2, -10., 10., 0.);
+    F.addBoundaryCondition(load);
+
+    // element data of the undamaged beam, in Assembly::element2d order
+    Assembly *K = F.getAssembly(true);
+    VirtualMachine vm;
+    ElementExport X;
+    std::vector<DelaunayTriangle *> elems;
+    std::vector<double> centre, radius, area;
+    for (size_t ie = 0; ie < K->element2d.size(); ie++) {
+        DelaunayTriangle *t = dynamic_cast<DelaunayTriangle *>(K->element2d[ie]);
+        elems.push_back(t);
+        export_element(t, 2, K->scales[ie], {t->first, t->second, t->third}, vm, X);
+        centre.push_back(t->getCenter().getX());
+        centre.push_back(t->getCenter().getY());
+        radius.push_back(t->getRadius());
+        area.push_back(t->area());
+    }
+    write_elements(o, X);
+    o.d("elem_centre", centre);
+    o.d("elem_radius", radius);
+    o.d("elem_area", area);
+    o.scalar("ndofmax", (double)K->ndofmax);
+    o.scalar("dim", 2);
+    o.scalar("eps0", thr);
+    o.scalar("Gf", Gf);
+    o.scalar("E", E);
+    o.scalar("nu", nu);
+    o.scalar("radius", R);
+    o.scalar("model", model);
+    o.scalar("fibre", fibre);
+    o.scalar("cutoff", cutoff);
+    o.scalar("steps", steps);
+    o.scalar("deflection", dmax);
+
+    const size_t ne = elems.size();
+    for (int k = 1; k <= steps; k++) {
+        load->setData(-dmax * k / steps);
+        double t0 = now_s();
+        F.step();
+        double t1 = now_s();
+        if (k == 1) {   // the multipliers of a load step (supports and the load patch at step 1)
+            Assembly *A = F.getAssembly(false);
+            write_multipliers(o, A);
+        }
+        const Vector &u = F.getDisplacements();
+        std::vector<double> uu(std::begin(u), std::end(u)), dmg(ne), score(ne), sm(4 * ne);
+        size_t damaged = 0;
+        for (size_t i = 0; i < ne; i++) {
+            Form *b = elems[i]->getBehaviour();
+            const Matrix Ceff = b->getTensor(Point());
+            dmg[i] = 1.0 - Ceff[0][0] / b->param[0][0];
+            damaged += dmg[i] > 0;
+            FractureCriterion *fc = b->getFractureCriterion();
+            score[i] = fc->getScoreAtState();
+            std::pair<Vector, Vector> f = fc->getSmoothedFields(PRINCIPAL_REAL_STRESS_FIELD, PRINCIPAL_TOTAL_STRAIN_FIELD,
+                                                                 elems[i]->getState(), 0.);
+            sm[4 * i] = f.first[0];
+            sm[4 * i + 1] = f.first[1];
+            sm[4 * i + 2] = f.second[0];
+            sm[4 * i + 3] = f.second[1];
+        }
+        const std::string sfx = "_" + std::to_string(k);
+        o.d("u" + sfx, uu);
+        o.d("damage" + sfx, dmg);
+        o.d("score" + sfx, score);
+        o.d("smoothed" + sfx, sm);
+        o.scalar("step_time_s" + sfx, t1 - t0);
+        o.scalar("average_damage" + sfx, F.averageDamage);
+        std::fprintf(stderr, "harness damage: step %d deflection %.3e damaged %zu avg %.3e time %.2fs\n", k,
+                     dmax * k / steps, damaged, F.averageDamage, t1 - t0);
+    }
+    o.scalar("n_elem", (double)ne);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -424,6 +548,7 @@ int main(int argc, char **argv)
     if (!o.f) return 3;
     if (which == "incl" || which == "crack" || which == "plate" || which == "imposed") return run_2d(which, o, kv);
     if (which == "voxel") return run_voxel(o, kv);
+    if (which == "damage") return run_damage(o, kv);
     std::fprintf(stderr, "unknown case %s\n", which.c_str());
     return 2;
 }

@@ -1,15 +1,15 @@
 // noalloc.cu -- a Jacobi-PCG solve that allocates no device memory.
 //
-// Who needs it: callers that cannot call cudaMalloc at solve time -- code that
-// runs while a CUDA graph is being captured in a mode that forbids
-// allocation, applications that hand every byte of device memory to their own
-// pool allocator at start-up, and real-time loops that cannot afford the
-// implicit device synchronisation an allocation may cause.  They keep the
-// matrix, the right-hand side and the solution in their own device memory; the
-// work vectors of the solve (r, z, p, q, the inverse diagonal, the per-CTA
-// partial sums and the control block) live in one file-scope __device__ array
-// of fixed size, which every GPU that loads this library reserves until the
-// process exits.
+// Who needs it: callers that cannot call cudaMalloc at solve time --
+// applications that hand every byte of device memory to their own pool
+// allocator at start-up, and real-time loops that cannot afford the implicit
+// device synchronisation an allocation may cause.  They keep the matrix, the
+// right-hand side and the solution in their own device memory; the work
+// vectors of the solve (r, z, p, q, the inverse diagonal, the per-CTA partial
+// sums and the control block) live in one file-scope __device__ array of fixed
+// size, which every GPU that loads this library reserves until the process
+// exits.  The solve is driven from the host: it synchronises the caller's
+// stream to read the norms and the control block every 16 iterations.
 //
 // The array is shared by every call on a device and keeps the last call's
 // contents: each call initialises everything it reads before reading it.
@@ -41,23 +41,22 @@ struct NoAllocDevice {
 static std::mutex g_noalloc_mu;
 static NoAllocDevice g_noalloc_dev[128];
 
-// Inverse diagonal of a block-CSR matrix (diagonal block found by binary search):
-// 1/A_ii if |A_ii| > 1e-12 else 0 (sparse/sparse_matrix.cpp:216-231).
+// Inverse diagonal of a block-CSR matrix: 1/A_ii if |A_ii| > 1e-12 else 0
+// (sparse/sparse_matrix.cpp:216-231).  The diagonal block is found by a scan of
+// the row (10-30 blocks), so the caller's columns need not be sorted; a row
+// without a diagonal block gets 0, as the reference's zero diagonal does.
 template <int S>
 __global__ void k_noalloc_invdiag(uint32_t n_rows, const uint32_t *row_ptr, const uint32_t *col, const double *val,
                                   double *dinv)
 {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_rows) return;
-    uint32_t lo = row_ptr[k], hi = row_ptr[k + 1];
-    const uint32_t end = hi;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (col[mid] < k) lo = mid + 1; else hi = mid;
-    }
-    const bool found = lo < end && col[lo] == k;
+    const uint32_t end = row_ptr[k + 1];
+    uint32_t at = end;
+    for (uint32_t j = row_ptr[k]; j < end; j++)
+        if (col[j] == k) { at = j; break; }
     for (int r = 0; r < S; r++) {
-        const double v = found ? val[(uint64_t)lo * S * S + r * S + r] : 0.0;
+        const double v = at < end ? val[(uint64_t)at * S * S + r * S + r] : 0.0;
         dinv[(uint64_t)k * S + r] = fabs(v) > 1e-12 ? 1.0 / v : 0.0;
     }
 }
@@ -159,7 +158,7 @@ amie_status noalloc_solve(const NoAllocDevice &dev, uint32_t n_rows, const uint3
         if (total >= maxit) break;
         PcgCtl c{};   // done = 0, ticket = 0, iterations = 0
         c.maxit = maxit - total;
-        c.tol2 = 0.25 * target2;
+        c.tol2 = (kFp64StopFraction * kFp64StopFraction) * target2;
         AMIE_CUDA(cudaMemcpyAsync(ctl, &c, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
         k_pcg_start<double><<<grid, kVecThreads, 0, st>>>(v, n, pp, ctl);
         AMIE_LAUNCHED();
@@ -216,7 +215,10 @@ extern "C" amie_status amie_pcg_solve_noalloc(int32_t stride, uint32_t n_rows, c
     }
     int device = 0;
     AMIE_CUDA(cudaGetDevice(&device));
-    if (device < 0 || device >= 128) return AMIE_BAD_INPUT;
+    if (device < 0 || device >= 128) {
+        set_error("amie_pcg_solve_noalloc: device %d, this library serves devices 0 to 127", device);
+        return AMIE_BAD_INPUT;
+    }
     NoAllocDevice dev;
     {
         // Set-up, once per device, with that device current: the device address of

@@ -522,12 +522,12 @@ struct ServerOps {
         const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
         c.maxit = std::max<int64_t>(1, maxit - r->iterations);
         if (srv->mixed) {
-            const double need = 0.3 * srv->cfg.rtol * r->bnorm / r->rnorm;
+            const double need = kMixedLastTarget * srv->cfg.rtol * r->bnorm / r->rnorm;
             const double inner = std::min(0.5, std::max(kInnerReduction, need));
             c.tol2 = inner * inner;
         } else {
             const double target = srv->cfg.rtol * r->bnorm;
-            c.tol2 = 0.25 * target * target;
+            c.tol2 = (kFp64StopFraction * kFp64StopFraction) * target * target;
         }
         srv->h_ctl[slot] = c;
         AMIE_CUDA(cudaMemcpyAsync(srv->d_ctl.p + slot, srv->h_ctl + slot, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
@@ -554,7 +554,7 @@ struct ServerOps {
         const SlotDesc &d = srv->h_slots[slot];
         const int nc = d.c1 - d.c0;
         const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
-        const double need = 0.3 * srv->cfg.rtol * r->bnorm / r->rnorm;
+        const double need = kMixedLastTarget * srv->cfg.rtol * r->bnorm / r->rnorm;
         const double inner = std::min(0.5, std::max(kInnerReduction, need));
         k_scale_to_f32<<<nc, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / r->rnorm, t->r32.p, t->d32.p);
         k_pcg_resume<float><<<nc, kVecThreads, 0, st>>>(d.v32, t->n, d.parts, d.ctl, ratio, inner * inner,

@@ -575,8 +575,9 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
         int64_t it = 0;
         double rr_in = 0.0;
         if (!mixed) {
-            // recursive residual target a little below the true one: the true residual is re-checked
-            AMIE_TRY(run_pcg<double>(t, s, target2 * 0.25, maxit - total, &it, &rr_in));
+            // recursive residual target below the true one (the true residual is re-checked)
+            AMIE_TRY(run_pcg<double>(t, s, target2 * (kFp64StopFraction * kFp64StopFraction), maxit - total,
+                                     &it, &rr_in));
         } else {
             // FP32 PCG on the residual scaled to unit norm; at each return the FP32
             // increment is added to x in FP64, r is replaced by the true FP64
@@ -585,7 +586,7 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
             k_scale_to_f32<<<s->grid, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / norm, t->r32.p, t->d32.p);
             AMIE_LAUNCHED();
             // reduce by inner_rtol, or by less when that is all the outer target still needs
-            const double need = 0.3 * rtol * bnorm / norm;
+            const double need = kMixedLastTarget * rtol * bnorm / norm;
             const double inner = std::min(0.5, std::max(inner_rtol, need));
             // keep the search direction only while replacements show real progress; a
             // true residual that fell by less than half means the FP32 recursion has
