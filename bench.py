@@ -539,36 +539,52 @@ def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, p
             "host_loop_s": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in loop_stats.items()}}
 
 
-def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 6e-5):
-    """Config-3 loop: notched beam in three-point bending, P1, ~250k DOF, E 35 GPa;
-    each load step updates the scalar damage on the device from the last
-    solution (Mazars equivalent strain, eps0 = 1e-4, exponential softening),
-    re-integrates (1 - d) C, eliminates the new imposed deflection and solves
-    warm-started as Assembly::cgsolve does, from the extrapolated displacement
-    2 u_(k-1) - u_(k-2) (all device-resident)."""
+def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 2e-4, max_passes: int = 2000):
+    """Config-3 loop: notched beam in three-point bending (400 x 100 mm, 20 x 2 mm
+    notch, P1, ~250k DOF, E 35 GPa, 20 mm loading plate) with the reference's
+    StiffnessAndFracture damage: NonLocalMazars (threshold 1e-4, Gf 100 N/m,
+    material radius 2 mm) graded on the device and FiberBasedIsotropicLinearDamage
+    (0.1 per event, fractured at 0.6).  Each load step raises the plate's
+    deflection and runs FeatureTree::stepInternal's passes on the device
+    (damaged stiffness, elimination, warm-started solve, grading, update) until
+    no element changes.  Reports where the damage lies relative to the notch."""
     import amie_gpu as G
     m, bcs_at, meta = W.notched_beam()
     topo = G.Topology(ctx, m)
     topo.assemble()
-    iters, changed = [], []
+    law = G.DamageLaw(G.DAMAGE_FIBER_ISOTROPIC, 1e-4, 35e9, 0.2, 100.0, 0.002, 2e-3, 0.1, 0.6, 1e-4)
+    t_setup = time.perf_counter()
+    topo.damage_setup(law, meta["corners"])
+    setup_s = time.perf_counter() - t_setup
+    per_step, total_passes, total_iters = [], 0, 0
     ctx.timer_start()
     for k in range(1, steps + 1):
-        if k > 1:
-            nc, _ = topo.damage_step(eps0=1e-4, softening=3000.0, d_max=0.999, want_damage=False)
-            changed.append(nc)
-        topo.apply_dirichlet(*bcs_at(deflection_max * k / steps))   # scatter (1-d) C + elimination
-        if k > 1:
-            topo.extrapolate()
-        st = topo.solve_resident(solver, rtol=1e-10, use_x0=k > 1)
-        iters.append(st["iterations"])
+        topo.apply_dirichlet(*bcs_at(deflection_max * k / steps))
+        st = topo.damage_load_step(solver, rtol=1e-10, max_sub_iterations=max_passes, warm=k > 1,
+                                   accept=(G.AMIE_OK, G.AMIE_NOT_CONVERGED))
+        per_step.append((st["sub_iterations"], st["damaged"], st["fractured"]))
+        total_passes += st["sub_iterations"]
+        total_iters += st["cg_iterations"]
     ms = ctx.timer_stop()
-    _, dmg = topo.damage_step(eps0=1e-4, softening=3000.0, d_max=0.999)
+    dmg = topo.damage_state()
     topo.close()
     n = meta["n_dof"]
-    return {"steps": steps, "n_dof": int(n), "ms_total": ms, "ms_per_step": ms / steps,
-            "iterations_total": int(sum(iters)), "dof_iterations_per_s": n * sum(iters) / (ms / 1e3),
-            "damaged_elements": int((dmg > 0).sum()), "max_damage": float(dmg.max()),
-            "elements_changed_last_step": int(changed[-1]) if changed else 0}
+    cen = meta["corners"].reshape(-1, 3, 2).mean(1)
+    hit = dmg > 0
+    tip = meta["notch_tip"]
+    first = next((k + 1 for k, p in enumerate(per_step) if p[1] > 0), None)
+    out = {"steps": steps, "n_dof": int(n), "deflection_max_m": deflection_max, "ms_total": ms,
+           "ms_per_step": ms / steps, "setup_s": setup_s, "passes_total": int(total_passes),
+           "iterations_total": int(total_iters), "dof_iterations_per_s": n * total_iters / (ms / 1e3),
+           "first_damaged_step": first, "damaged_elements": int(hit.sum()),
+           "fractured_elements": int((dmg >= 0.6).sum()), "max_damage": float(dmg.max()),
+           "passes_per_step": [p[0] for p in per_step], "damaged_per_step": [p[1] for p in per_step],
+           "law": "NonLocalMazars(1e-4, 35e9, 0.2, 100, 0.002) + FiberBasedIsotropicLinearDamage(0.1, 0.6)"}
+    if hit.any():
+        out["damaged_x_range_mm"] = [float(1e3 * (cen[hit, 0].min() - tip[0])), float(1e3 * (cen[hit, 0].max() - tip[0]))]
+        out["damaged_y_range_mm"] = [float(1e3 * cen[hit, 1].min()), float(1e3 * cen[hit, 1].max())]
+        out["notch_tip_mm"] = [0.0, 1e3 * tip[1]]
+    return out
 
 
 def main():

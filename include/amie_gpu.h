@@ -336,21 +336,73 @@ AMIE_API amie_status amie_element_fields(amie_topo *topo, double *strain, double
 enum { AMIE_FIELD_STRAIN = 0, AMIE_FIELD_STRESS = 1 };
 AMIE_API amie_status amie_average_field(amie_topo *topo, int32_t field, double *avg, double *measure);
 
-/* One explicit scalar-damage update from the current solution
- * (StiffnessAndFracture::step, physics/stiffness_and_fracture.cpp:81-90): Mazars
- * equivalent strain eq = |<eps>_+| of the principal strains
- * (physics/fracturecriteria/mazars.cpp:153), d = 1 - (eps0/eq) exp(-B (eq - eps0))
- * above eps0, irreversible, capped at d_max; the factor on C becomes base (1 - d),
- * so the next amie_assemble integrates (1 - d) C (isotropiclineardamage.cpp:39-46).
- * 2D meshes.  n_changed: elements whose damage grew by more than change_tol. */
-typedef struct amie_damage_params {
-    double eps0;
-    double softening;    /* B */
-    double d_max;
-    double change_tol;
-} amie_damage_params;
-AMIE_API amie_status amie_damage_step(amie_topo *topo, const amie_damage_params *params, uint32_t *n_changed,
-                                      double *damage_out);
+/* ------------------------------------------------------------------ damage
+ * Non-local Mazars damage of StiffnessAndFracture (physics/stiffness_and_fracture.cpp:75-90)
+ * on 2D linear triangles in plane stress, stepped the way FeatureTree::step does
+ * it (features/features.cpp:6150-6270, stepElements :4875-5360):
+ *   grade   FractureCriterion::step of every element (physics/fracturecriteria/fracturecriterion.cpp:534-560):
+ *           the strain averaged over a smoothing neighbourhood (Mesh::getSmoothedFields,
+ *           mesher/mesh.h:1384-1790, QUARTIC_COMPACT kernel of the material radius,
+ *           neighbourhoods of FractureCriterion::initialiseCache, fracturecriterion.cpp:171-196),
+ *           the element's damaged stress from it, their principal values, and
+ *           NonLocalMazars::gradeAtTime (physics/fracturecriteria/mazars.cpp:73-147) -> score;
+ *   update  FiberBasedIsotropicLinearDamage::step of every element in mesh order
+ *           (physics/damagemodels/fiberbasedisotropiclineardamage.cpp:59-98): an element
+ *           whose criterion is met and whose score is within score_tolerance of the
+ *           largest score in its neighbourhood (FractureCriterion::getMaxScoreInNeighbourhood,
+ *           fracturecriterion.cpp:251-280) gains fibre_fraction of damage; at cutoff it is
+ *           fractured and keeps residual C (fiberbasedisotropiclineardamage.cpp:36-57).
+ * The factor on C of every element follows its damage, so the next amie_assemble
+ * integrates the damaged stiffness. */
+enum { AMIE_DAMAGE_FIBER_ISOTROPIC = 0 };   /* FiberBasedIsotropicLinearDamage */
+typedef struct amie_damage_law {
+    int32_t model;             /* AMIE_DAMAGE_FIBER_ISOTROPIC */
+    double threshold;          /* NonLocalMazars(thresh, E, nu, Gf, radius, PLANE_STRESS), mazars.cpp:27-35 */
+    double young;
+    double poisson;
+    double fracture_energy;
+    double radius;             /* material characteristic radius */
+    double score_tolerance;    /* FractureCriterion scoreTolerance; <= 0: 2e-3 (fracturecriterion.cpp:77) */
+    double fibre_fraction;     /* damage increment per event; <= 0: 0.1 */
+    double cutoff;             /* fractured at this damage; <= 0: 0.6 */
+    double residual;           /* stiffness fraction of a fractured element; <= 0: 1e-4 */
+} amie_damage_law;
+
+/* Geometry (centre, circumradius, area) and smoothing neighbourhoods of every
+ * element, built on the device; damage starts at zero.  corners [n_elem*6]:
+ * the three vertices (x, y) of each element in its local order.  Every element
+ * must be an AMIE_TRI3 with at most one Gauss point and no enrichment. */
+AMIE_API amie_status amie_damage_setup(amie_topo *topo, const amie_damage_law *law, const double *corners);
+/* Damage of every element [n_elem] (host): set (NULL = zeros) or read. */
+AMIE_API amie_status amie_damage_set_state(amie_topo *topo, const double *damage);
+AMIE_API amie_status amie_damage_get_state(amie_topo *topo, double *damage);
+/* Grade every element from the current solution; score [n_elem] (-1 for a
+ * fractured element) and smoothed [n_elem*4] (principal smoothed stress, then
+ * principal smoothed strain, each in toPrincipal's order) are optional host outputs. */
+AMIE_API amie_status amie_damage_grade(amie_topo *topo, double *score, double *smoothed);
+/* Step the damage model of every element from the last grade; n_changed:
+ * elements whose damage grew. */
+AMIE_API amie_status amie_damage_update(amie_topo *topo, uint32_t *n_changed);
+/* Replace the device solution (the state amie_damage_grade reads) by x [n] (host). */
+AMIE_API amie_status amie_solution_upload(amie_topo *topo, const double *x);
+
+/* One load step with the multipliers of the last amie_apply_dirichlet: repeat
+ * { assemble the damaged stiffness if the damage changed, eliminate, solve
+ * (warm-started from the last solution), grade, update } until no element
+ * changes or max_sub_iterations passes (FeatureTree::stepInternal's loop,
+ * features/features.cpp:6188-6248; the reference solves three times per pass,
+ * twice by CG and once by BiCGStab from the CG solution, this solves once). */
+typedef struct amie_damage_step_stats {
+    int32_t sub_iterations;    /* passes of the loop */
+    int32_t status;            /* amie_status: AMIE_NOT_CONVERGED if max_sub_iterations ran out */
+    int64_t cg_iterations;     /* solver iterations of all passes */
+    uint32_t damaged;          /* elements with damage > 0 at the end */
+    uint32_t fractured;        /* elements at the cutoff */
+    uint64_t changes;          /* damage increments of all passes */
+    double seconds;
+} amie_damage_step_stats;
+AMIE_API amie_status amie_damage_load_step(amie_topo *topo, const amie_solve_opts *opts, int32_t max_sub_iterations,
+                                           amie_damage_step_stats *stats);
 
 /* ------------------------------------------------------------------ timing
  * Device time on the context's stream (CUDA events) between start and stop;

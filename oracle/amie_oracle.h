@@ -100,6 +100,38 @@ int oracle_pcg(int32_t stride, uint32_t n_rows, const uint32_t *row_size, const 
  * features/features.cpp:4223, 3424).  strain, stress: [n_elem * nv]. */
 int oracle_element_fields(const oracle_mesh *m, const double *u, double *strain, double *stress);
 
+/* ---- non-local Mazars damage on linear triangles (damage_oracle.cpp) ---- */
+
+/* NonLocalMazars(threshold, young, poisson, fracture_energy, radius, PLANE_STRESS)
+ * (physics/fracturecriteria/mazars.cpp:27-35) with a FiberBasedIsotropicLinearDamage
+ * (physics/damagemodels/fiberbasedisotropiclineardamage.cpp:17-24): damage grows
+ * by `fibre` per event, the element is fractured at `cutoff` and keeps
+ * `residual` C; score_tolerance is FractureCriterion's scoreTolerance. */
+typedef struct oracle_damage_law {
+    double threshold, young, poisson, fracture_energy, radius;
+    double score_tolerance, fibre, cutoff, residual;
+} oracle_damage_law;
+
+/* Centre, circumradius and area of each triangle from its corners [n*6]
+ * (geometry/geometry_2D.cpp:480-515, 653-659). */
+int oracle_damage_geometry(uint32_t n, const double *xy, double *centre, double *radius, double *area);
+/* Smoothing cache of every element (Mesh::generateCache through
+ * FractureCriterion::initialiseCache): CSR ptr [n+1], idx, normalised coef.
+ * idx == NULL counts only. */
+int oracle_damage_cache(uint32_t n, double R, const double *xy, const double *centre, const double *radius,
+                        const double *area, uint64_t *ptr, uint32_t *idx, double *coef);
+/* FractureCriterion::step of every element: score [n] (-1 fractured) and the
+ * smoothed principal stress and strain [n*4], from element strains [n*3]
+ * (Voigt, engineering shear), each element's undamaged C [n*9], damage state,
+ * area and one-point Gauss weight gpw (weight times det J). */
+int oracle_damage_grade(uint32_t n, const oracle_damage_law *law, const double *strain, const double *cmat,
+                        const double *state, const double *area, const double *gpw, const uint64_t *ptr,
+                        const uint32_t *idx, const double *coef, double *score, double *smoothed);
+/* FiberBasedIsotropicLinearDamage::step of every element from the scores;
+ * state updated in place, changed [n] set to 1 where it grew. */
+int oracle_damage_update(uint32_t n, const oracle_damage_law *law, const double *centre, const double *radius,
+                         const double *score, double *state, uint8_t *changed);
+
 /* Number of OpenMP threads the oracle uses (for reporting). */
 int oracle_threads(void);
 

@@ -158,3 +158,60 @@ def assemble(m, bc_ids, bc_values, bc_kinds, rhs0=None):
     dirichlet(m.stride, rs, ci, arr, np.ascontiguousarray(bc_ids, np.uint32),
               np.ascontiguousarray(bc_values, np.float64), np.ascontiguousarray(bc_kinds, np.uint8), rhs)
     return dict(off=off, ke=ke, row_size=rs, column_index=ci, array=arr, rhs=rhs)
+
+
+# ---------------------------------------------------------------- damage (damage_oracle.cpp)
+
+class DamageLaw(C.Structure):
+    """NonLocalMazars + FiberBasedIsotropicLinearDamage parameters (oracle_damage_law)."""
+    _fields_ = [(k, C.c_double) for k in ("threshold", "young", "poisson", "fracture_energy", "radius",
+                                           "score_tolerance", "fibre", "cutoff", "residual")]
+
+
+def damage_geometry(xy):
+    """(centre [n,2], circumradius [n], area [n]) of triangles with corners xy [n,6]."""
+    xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 6)
+    n = len(xy)
+    c, r, a = np.zeros(2 * n), np.zeros(n), np.zeros(n)
+    lib().oracle_damage_geometry(C.c_uint32(n), _p(xy), _p(c), _p(r), _p(a))
+    return c.reshape(n, 2), r, a
+
+
+def damage_cache(R, xy, centre, radius, area):
+    """Smoothing caches (ptr, idx, coef) of every element."""
+    xy = np.ascontiguousarray(xy, np.float64).reshape(-1, 6)
+    n = len(xy)
+    centre = np.ascontiguousarray(centre, np.float64)
+    radius = np.ascontiguousarray(radius, np.float64)
+    area = np.ascontiguousarray(area, np.float64)
+    ptr = np.zeros(n + 1, np.uint64)
+    lib().oracle_damage_cache(C.c_uint32(n), C.c_double(R), _p(xy), _p(centre), _p(radius), _p(area), _p(ptr),
+                              None, None)
+    idx = np.zeros(int(ptr[-1]), np.uint32)
+    coef = np.zeros(int(ptr[-1]), np.float64)
+    lib().oracle_damage_cache(C.c_uint32(n), C.c_double(R), _p(xy), _p(centre), _p(radius), _p(area), _p(ptr),
+                              _p(idx), _p(coef))
+    return ptr, idx, coef
+
+
+def damage_grade(law, strain, cmat, state, area, gpw, cache):
+    """(score [n], smoothed principal stress and strain [n,4])."""
+    n = len(state)
+    ptr, idx, coef = cache
+    score = np.zeros(n)
+    sm = np.zeros(4 * n)
+    lib().oracle_damage_grade(C.c_uint32(n), C.byref(law), _p(np.ascontiguousarray(strain, np.float64)),
+                              _p(np.ascontiguousarray(cmat, np.float64)), _p(np.ascontiguousarray(state, np.float64)),
+                              _p(np.ascontiguousarray(area, np.float64)), _p(np.ascontiguousarray(gpw, np.float64)),
+                              _p(ptr), _p(idx), _p(coef), _p(score), _p(sm))
+    return score, sm.reshape(n, 4)
+
+
+def damage_update(law, centre, radius, score, state):
+    """FiberBasedIsotropicLinearDamage::step of every element; returns (new state, changed mask)."""
+    st = np.array(state, np.float64, copy=True)
+    ch = np.zeros(len(st), np.uint8)
+    lib().oracle_damage_update(C.c_uint32(len(st)), C.byref(law), _p(np.ascontiguousarray(centre, np.float64)),
+                               _p(np.ascontiguousarray(radius, np.float64)),
+                               _p(np.ascontiguousarray(score, np.float64)), _p(st), _p(ch))
+    return st, ch.astype(bool)

@@ -427,6 +427,21 @@ int run_voxel(Out &o, std::map<std::string, std::string> &kv)
 }
 
 
+// Read access to a criterion's cache ids (FractureCriterion::cachecoreID /
+// cacheID, protected) for the export of the smoothing neighbourhoods.
+struct CriterionCaches : public FractureCriterion {
+    static int core(FractureCriterion *f) { return static_cast<CriterionCaches *>(f)->cachecoreID; }
+    static int all(FractureCriterion *f) { return static_cast<CriterionCaches *>(f)->cacheID; }
+};
+
+// Read access to the smoothing weights of a cache (Mesh::coefs, protected).
+struct MeshCoefs : public Mesh<DelaunayTriangle, DelaunayTreeItem> {
+    static const std::vector<std::vector<double>> &of(Mesh<DelaunayTriangle, DelaunayTreeItem> *m, int id)
+    {
+        return static_cast<MeshCoefs *>(m)->coefs[id];
+    }
+};
+
 // Config-3 family: notched beam, damage by load steps through FeatureTree::step.
 int run_damage(Out &o, std::map<std::string, std::string> &kv)
 {
@@ -454,12 +469,12 @@ int run_damage(Out &o, std::map<std::string, std::string> &kv)
     F.addFeature(&box, notch);
     F.setSamplingNumber(sampling);
     F.setMaxIterationsPerStep(maxit);
-    F.addBoundaryCondition(new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, BOTTOM_LEFT));
-    F.addBoundaryCondition(new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM_LEFT));
-    F.addBoundaryCondition(new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM_RIGHT));
     BoundingBoxAndRestrictionDefinedBoundaryCondition *load = new BoundingBoxAndRestrictionDefinedBoundaryCondition(
         SET_ALONG_ETA, TOP, -patch / 2, patch / 2, -10., 10., 0.);
-    F.addBoundaryCondition(load);
+    std::vector<BoundaryCondition *> bcs = {new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, BOTTOM_LEFT),
+                                            new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM_LEFT),
+                                            new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM_RIGHT), load};
+    for (auto bc : bcs) F.addBoundaryCondition(bc);
 
     // element data of the undamaged beam, in Assembly::element2d order
     Assembly *K = F.getAssembly(true);
@@ -477,6 +492,16 @@ int run_damage(Out &o, std::map<std::string, std::string> &kv)
         area.push_back(t->area());
     }
     write_elements(o, X);
+    {
+        // the multipliers of one load step, applied to a scratch Assembly with the
+        // load patch at -1 (load step k sets it to -deflection * k / steps)
+        Assembly A;
+        A.add(elems[0]);
+        load->setData(-1.0);
+        for (auto bc : bcs) bc->apply(&A, F.get2DMesh(), &vm);
+        load->setData(0.0);
+        write_multipliers(o, &A);
+    }
     o.d("elem_centre", centre);
     o.d("elem_radius", radius);
     o.d("elem_area", area);
@@ -499,12 +524,8 @@ int run_damage(Out &o, std::map<std::string, std::string> &kv)
         double t0 = now_s();
         F.step();
         double t1 = now_s();
-        if (k == 1) {   // the multipliers of a load step (supports and the load patch at step 1)
-            Assembly *A = F.getAssembly(false);
-            write_multipliers(o, A);
-        }
         const Vector &u = F.getDisplacements();
-        std::vector<double> uu(std::begin(u), std::end(u)), dmg(ne), score(ne), sm(4 * ne);
+        std::vector<double> uu(std::begin(u), std::end(u)), dmg(ne), score(ne), sm(4 * ne), eps(3 * ne);
         size_t damaged = 0;
         for (size_t i = 0; i < ne; i++) {
             Form *b = elems[i]->getBehaviour();
@@ -519,17 +540,40 @@ int run_damage(Out &o, std::map<std::string, std::string> &kv)
             sm[4 * i + 1] = f.first[1];
             sm[4 * i + 2] = f.second[0];
             sm[4 * i + 3] = f.second[1];
+            Vector es(3);
+            elems[i]->getState().getAverageField(MECHANICAL_STRAIN_FIELD, es, &vm, 0.);
+            for (int c = 0; c < 3; c++) eps[3 * i + c] = es[c];
         }
         const std::string sfx = "_" + std::to_string(k);
         o.d("u" + sfx, uu);
         o.d("damage" + sfx, dmg);
         o.d("score" + sfx, score);
         o.d("smoothed" + sfx, sm);
+        o.d("strain" + sfx, eps);
         o.scalar("step_time_s" + sfx, t1 - t0);
         o.scalar("average_damage" + sfx, F.averageDamage);
         std::fprintf(stderr, "harness damage: step %d deflection %.3e damaged %zu avg %.3e time %.2fs\n", k,
                      dmax * k / steps, damaged, F.averageDamage, t1 - t0);
     }
+    // the smoothing neighbourhood of every element (Mesh::generateCache through
+    // FractureCriterion::initialiseCache), as positions in the element order above
+    std::map<int, uint32_t> pos;
+    for (size_t i = 0; i < ne; i++) pos[elems[i]->index] = (uint32_t)i;
+    std::vector<uint32_t> cptr{0}, cidx, aptr{0}, aidx;
+    std::vector<double> ccoef;
+    for (size_t i = 0; i < ne; i++) {
+        FractureCriterion *fc = elems[i]->getBehaviour()->getFractureCriterion();
+        for (int id : F.get2DMesh()->getCache(CriterionCaches::core(fc))) cidx.push_back(pos.count(id) ? pos[id] : 0xffffffffu);
+        cptr.push_back((uint32_t)cidx.size());
+        for (const auto &w : MeshCoefs::of(F.get2DMesh(), CriterionCaches::core(fc))) ccoef.push_back(w.empty() ? -1.0 : w[0]);
+        for (int id : F.get2DMesh()->getCache(CriterionCaches::all(fc))) aidx.push_back(pos.count(id) ? pos[id] : 0xffffffffu);
+        aptr.push_back((uint32_t)aidx.size());
+    }
+    o.u("cache_ptr", cptr);
+    o.u("cache_idx", cidx);
+    o.d("cache_coef", ccoef);
+    o.u("cache_all_ptr", aptr);
+    o.u("cache_all_idx", aidx);
     o.scalar("n_elem", (double)ne);
     return 0;
 }

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import argparse
 import os
+import re
 import struct
 import subprocess
 import sys
@@ -44,6 +45,10 @@ CASES = {
     # config-2 style: voxel file -> 6 linear tets per voxel, 16 lognormal phases,
     # uniaxial imposed strain 1e-4
     "voxel_t4": ("voxel", ["n=6", "nphase=16", "seed=5", "strain=1e-4"]),
+    # config-3 style: 80 x 20 mm notched beam in three-point bending, P1,
+    # StiffnessAndFracture + NonLocalMazars (eps0 1e-4, Gf 100 N/m, radius 2 mm)
+    # + FiberBasedIsotropicLinearDamage; six load steps up to 40 um deflection
+    "damage_p1": ("damage", ["sampling=16", "steps=6", "deflection=4e-5"]),
 }
 
 _TYPES = {"d": np.float64, "i": np.int32, "u": np.uint32, "q": np.int64, "b": np.int8}
@@ -87,10 +92,16 @@ def main() -> int:
             print(r.stderr[-2000:], file=sys.stderr)
             return r.returncode
         rec = read_records(tmp)
+        if case == "damage":
+            # passes of FeatureTree::stepInternal per load step, as the reference prints them
+            # ("<passes>/<maxit>." before the step line of the harness)
+            log = r.stderr.replace("\r", "\n")
+            rec["sub_iterations"] = np.array([int(p) for p, _ in re.findall(r"(\d+)/\d+\.harness damage: step (\d+)", log)],
+                                             np.int32)
         rec["harness_case"] = np.array(case)
         rec["harness_args"] = np.array(" ".join(kv))
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
-        line = [l for l in r.stderr.splitlines() if l.startswith("harness:")]
+        line = [l for l in r.stderr.replace("\r", "\n").splitlines() if "harness" in l]
         print(name, line[-1] if line else "")
         os.remove(tmp)
     return 0

@@ -247,37 +247,35 @@ def test_imposed_strain_induced_forces(gpu_ctx):
         t.close()
 
 
-def test_damage_step_and_reassembly(gpu_ctx):
-    """Damage update on the device, then (1-d) C re-integration: matches the damage law
-    applied to the oracle's strains and the oracle's K_e with cscale = 1 - d."""
+def test_damage_state_and_reassembly(gpu_ctx):
+    """The damage state sets the factor on C (1 - d, or the residual 1e-4 for a
+    fractured element): re-assembly integrates (1 - d) C exactly as the oracle does
+    with that factor, and the damaged system still solves."""
     import amie_gpu
-    d = load_golden("incl_p1")
-    m = am.from_golden(d, "tabulated")
-    ids, vals, kinds = am.golden_bcs(d)
-    vals = vals * 30.0        # strains well above eps0 near the loaded edge
+    d = load_golden("damage_p1")
+    m = am.from_golden(d, "auto")
+    n = m.n_elem
     t = amie_gpu.Topology(gpu_ctx, m)
-    t.assemble()
-    t.apply_dirichlet(ids, vals, kinds)
-    x, _ = t.solve(amie_gpu.SOLVER_PCG_FP64, rtol=1e-12)
-    eps0, B = 1e-4, 5000.0
-    n_changed, dmg = t.damage_step(eps0=eps0, softening=B, d_max=0.99)
-    eo, _ = O.element_fields(m, x)
-    c = 0.5 * (eo[:, 0] + eo[:, 1])
-    rad = np.sqrt(0.25 * (eo[:, 0] - eo[:, 1]) ** 2 + 0.25 * eo[:, 2] ** 2)
-    eq = np.hypot(np.maximum(c + rad, 0), np.maximum(c - rad, 0))
-    dref = np.where(eq > eps0, 1 - eps0 / np.maximum(eq, 1e-300) * np.exp(-B * (eq - eps0)), 0.0)
-    dref = np.minimum(dref, 0.99)
-    assert np.allclose(dmg, dref, rtol=0, atol=1e-12)
-    assert n_changed == int((dref > 1e-6).sum()) and n_changed > 0
-    t.assemble()                                   # re-integrates (1 - d) C, keeps the multipliers
-    off, ke = t.element_matrices()
-    m2 = am.from_golden(d, "tabulated")
-    m2.cscale = 1.0 - dref
-    _, ko = O.element_matrices(m2)
-    assert rel(ke, ko) <= 1e-12
-    x2, st2 = t.solve(amie_gpu.SOLVER_PCG_FP64, rtol=1e-10, x0=x)
-    assert st2["relres"] <= 1e-10
-    t.close()
+    try:
+        t.assemble()
+        law = amie_gpu.DamageLaw(amie_gpu.DAMAGE_FIBER_ISOTROPIC, 1e-4, 35e9, 0.2, 100.0, 0.002, 2e-3, 0.1, 0.6, 1e-4)
+        t.damage_setup(law, d["elem_xy"])
+        rng = np.random.default_rng(3)
+        state = np.round(rng.integers(0, 7, n) * 0.1, 12)
+        t.damage_set_state(state)
+        assert np.array_equal(t.damage_state(), state)
+        t.assemble()
+        off, ke = t.element_matrices()
+        m2 = am.from_golden(d, "auto")
+        m2.cscale = np.where(state >= 0.6, 1e-4, 1.0 - state)
+        _, ko = O.element_matrices(m2)
+        assert rel(ke, ko) <= 1e-12
+        ids = d["bc_ids"].astype(np.uint32)
+        t.apply_dirichlet(ids, d["bc_values"] * 1e-5, np.zeros(len(ids), np.uint8))
+        x, st = t.solve(amie_gpu.SOLVER_PCG_FP64, rtol=1e-10)
+        assert st["relres"] <= 1e-10
+    finally:
+        t.close()
 
 
 def test_solve_is_deterministic(golden_topos):

@@ -33,9 +33,11 @@ EXPORTED = [
     "amie_element_matrices", "amie_apply_dirichlet", "amie_matrix_download", "amie_spmv", "amie_solve",
     "amie_solve_resident", "amie_solution_download", "amie_server_start", "amie_submit", "amie_poll",
     "amie_cancel", "amie_server_drain", "amie_server_stop", "amie_kernel_launches", "amie_timer_start",
-    "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_damage_step", "amie_pcg_solve_noalloc",
+    "amie_timer_stop", "amie_profile_spmv", "amie_element_fields", "amie_pcg_solve_noalloc",
     "amie_topology_spmv_lanes", "amie_profile_stream", "amie_average_field", "amie_set_imposed_strain",
-    "amie_server_query", "amie_cut_rules", "amie_extrapolate",
+    "amie_server_query", "amie_cut_rules", "amie_extrapolate", "amie_damage_setup", "amie_damage_set_state",
+    "amie_damage_get_state", "amie_damage_grade", "amie_damage_update", "amie_damage_load_step",
+    "amie_solution_upload",
 ]
 
 
@@ -49,9 +51,24 @@ CUT_OK, CUT_NOT_CUT, CUT_MONTE_CARLO, CUT_ORDER_DEPENDENT, CUT_TOO_MANY_HINTS, C
 CUT_REPLACE_MONTE_CARLO = 1
 
 
-class DamageParams(C.Structure):
-    _fields_ = [("eps0", C.c_double), ("softening", C.c_double), ("d_max", C.c_double),
-                ("change_tol", C.c_double)]
+DAMAGE_FIBER_ISOTROPIC = 0
+
+
+class DamageLaw(C.Structure):
+    """amie_damage_law: NonLocalMazars(threshold, young, poisson, fracture_energy, radius, PLANE_STRESS)
+    with FiberBasedIsotropicLinearDamage(fibre_fraction, cutoff), residual stiffness fraction."""
+    _fields_ = [("model", C.c_int32), ("threshold", C.c_double), ("young", C.c_double), ("poisson", C.c_double),
+                ("fracture_energy", C.c_double), ("radius", C.c_double), ("score_tolerance", C.c_double),
+                ("fibre_fraction", C.c_double), ("cutoff", C.c_double), ("residual", C.c_double)]
+
+
+class DamageStepStats(C.Structure):
+    _fields_ = [("sub_iterations", C.c_int32), ("status", C.c_int32), ("cg_iterations", C.c_int64),
+                ("damaged", C.c_uint32), ("fractured", C.c_uint32), ("changes", C.c_uint64),
+                ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class AmieError(RuntimeError):
@@ -325,13 +342,46 @@ class Topology:
         check(lib().amie_average_field(self.ptr, C.c_int32(field), _p(avg), C.byref(w)), "amie_average_field")
         return avg, w.value
 
-    def damage_step(self, eps0=1e-4, softening=5000.0, d_max=0.9999, change_tol=1e-6, want_damage=True):
-        """One damage update from the device solution; returns (elements changed, damage or None)."""
-        prm = DamageParams(eps0, softening, d_max, change_tol)
+    def solution_upload(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        check(lib().amie_solution_upload(self.ptr, _p(x)), "amie_solution_upload")
+
+    def damage_setup(self, law: DamageLaw, corners):
+        """Non-local Mazars damage of the (P1, 2D) mesh; corners [n_elem, 6] vertex coordinates."""
+        cr = np.ascontiguousarray(corners, np.float64).reshape(-1)
+        check(lib().amie_damage_setup(self.ptr, C.byref(law), _p(cr)), "amie_damage_setup")
+        self._law = law
+
+    def damage_set_state(self, damage=None):
+        dm = None if damage is None else np.ascontiguousarray(damage, np.float64)
+        check(lib().amie_damage_set_state(self.ptr, _p(dm)), "amie_damage_set_state")
+
+    def damage_state(self):
+        dm = np.zeros(self.mesh.n_elem, np.float64)
+        check(lib().amie_damage_get_state(self.ptr, _p(dm)), "amie_damage_get_state")
+        return dm
+
+    def damage_grade(self):
+        """(score [n_elem], smoothed principal stress and strain [n_elem, 4]) from the device solution."""
+        sc = np.zeros(self.mesh.n_elem, np.float64)
+        sm = np.zeros(self.mesh.n_elem * 4, np.float64)
+        check(lib().amie_damage_grade(self.ptr, _p(sc), _p(sm)), "amie_damage_grade")
+        return sc, sm.reshape(-1, 4)
+
+    def damage_update(self) -> int:
         n = C.c_uint32()
-        d = np.zeros(self.mesh.n_elem, np.float64) if want_damage else None
-        check(lib().amie_damage_step(self.ptr, C.byref(prm), C.byref(n), _p(d)), "amie_damage_step")
-        return n.value, d
+        check(lib().amie_damage_update(self.ptr, C.byref(n)), "amie_damage_update")
+        return n.value
+
+    def damage_load_step(self, solver=SOLVER_PCG_FP64, rtol=1e-10, max_sub_iterations=0, inner_rtol=0.0,
+                         warm=True, accept=(AMIE_OK,)):
+        """Solve-grade-update passes until no element changes (FeatureTree::stepInternal); returns stats.
+        warm: the first pass starts from the current device solution (else from zero)."""
+        opts = SolveOpts(solver, rtol, 1e-10, 32, 0, inner_rtol, 1 if warm else 0)
+        st = DamageStepStats()
+        rc = lib().amie_damage_load_step(self.ptr, C.byref(opts), C.c_int32(max_sub_iterations), C.byref(st))
+        check(rc, "amie_damage_load_step", ok=accept)
+        return st.as_dict()
 
     def profile_spmv(self, precision: int = 64, reps: int = 20) -> float:
         """Average device milliseconds of one q = A p (+ p.q) launch."""

@@ -17,7 +17,9 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libamie_gpu.so")
-SOURCES = ["common.cu", "assemble.cu", "solver.cu", "fields.cu", "noalloc.cu", "cut_rules.cu"]
+SOURCES = ["common.cu", "assemble.cu", "solver.cu", "fields.cu", "noalloc.cu", "cut_rules.cu", "damage.cu"]
+# per-file flags: the damage grading mirrors the reference's arithmetic operation by operation
+FILE_FLAGS = {"damage.cu": ["--fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I", os.path.join(REPO, "include"), "-I", CSRC]
@@ -32,7 +34,7 @@ def nvcc() -> str:
 
 def _compile(src: str, extra) -> str:
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc(), *ARCH, *FLAGS, *FILE_FLAGS.get(src, []), *extra, "-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr[-4000:]}")

@@ -23,9 +23,98 @@ namespace amie {
 
 // ------------------------------------------------------------------ kernels
 
+// Nonzeros of row r of the Voigt B of a function with physical gradient d
+// (polynomial/vm_base.cpp:2244-2255, 2278-2296): B[r][col] = d[comp], in
+// increasing column order.
+template <int DIM>
+struct BRow;
+template <>
+struct BRow<2> {
+    static constexpr int N = 2;
+    static __device__ constexpr int col(int r, int k) { return r == 0 ? (k == 0 ? 0 : 2) : (k == 0 ? 1 : 2); }
+    static __device__ constexpr int comp(int r, int k) { return r == 0 ? (k == 0 ? 0 : 1) : (k == 0 ? 1 : 0); }
+};
+template <>
+struct BRow<3> {
+    static constexpr int N = 3;
+    static __device__ constexpr int col(int r, int k) { return r == 0 ? (k == 0 ? 0 : k == 1 ? 4 : 5)
+                                                        : r == 1 ? (k == 0 ? 1 : k == 1 ? 3 : 5)
+                                                                 : (k == 0 ? 2 : k == 1 ? 3 : 4); }
+    static __device__ constexpr int comp(int r, int k) { return r == 0 ? (k == 0 ? 0 : k == 1 ? 2 : 1)
+                                                         : r == 1 ? (k == 0 ? 1 : k == 1 ? 2 : 0)
+                                                                  : (k == 0 ? 2 : k == 1 ? 1 : 0); }
+};
+
+// Default-rule element (NG points of its kind, inverse Jacobian at the
+// centroid): the physical gradient of every function at every point once, then
+// per column function j the products w_g C B_j^T, then every block
+// K_ij = sum_g B_i (w_g C B_j^T), i >= j, with the zero entries of B skipped.
+template <int DIM, int NF, int NG>
+__device__ __forceinline__ void quad_default(int kind, const double *C, const double *Je, double *K)
+{
+    constexpr int NV = DIM == 2 ? 3 : 6;
+    using B = BRow<DIM>;
+    const double inv_det = 1.0 / det_small<DIM>(Je);
+    double d[NF][NG][DIM], w[NG];
+#pragma unroll
+    for (int g = 0; g < NG; g++) {
+        double p[3];
+        default_rule(kind, g, p, &w[g]);
+        w[g] *= inv_det;   // weight / det(J^-1) (elements/elements.cpp:939-945)
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            double lg[3];
+            shape_grad(kind, f, p[0], p[1], lg);
+            phys_grad<DIM>(Je, lg, d[f][g]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NF; j++) {
+        double cb[NG][NV][DIM];   // w_g C B_j^T
+#pragma unroll
+        for (int g = 0; g < NG; g++)
+#pragma unroll
+            for (int l = 0; l < NV; l++)
+#pragma unroll
+                for (int c = 0; c < DIM; c++) {
+                    double a = 0.0;
+#pragma unroll
+                    for (int k = 0; k < B::N; k++) a += C[l * NV + B::col(c, k)] * d[j][g][B::comp(c, k)];
+                    cb[g][l][c] = w[g] * a;
+                }
+#pragma unroll
+        for (int i = j; i < NF; i++) {
+            double acc[DIM * DIM];
+#pragma unroll
+            for (int q = 0; q < DIM * DIM; q++) acc[q] = 0.0;
+#pragma unroll
+            for (int g = 0; g < NG; g++)
+#pragma unroll
+                for (int r = 0; r < DIM; r++)
+#pragma unroll
+                    for (int c = 0; c < DIM; c++) {
+                        double a = 0.0;
+#pragma unroll
+                        for (int k = 0; k < B::N; k++) a += d[i][g][B::comp(r, k)] * cb[g][B::col(r, k)][c];
+                        acc[r * DIM + c] += a;
+                    }
+            double *Kij = K + (size_t)(i * NF + j) * DIM * DIM;
+            double *Kji = K + (size_t)(j * NF + i) * DIM * DIM;
+#pragma unroll
+            for (int r = 0; r < DIM; r++)
+#pragma unroll
+                for (int c = 0; c < DIM; c++) {
+                    Kij[r * DIM + c] = acc[r * DIM + c];
+                    if (i != j) Kji[c * DIM + r] = acc[r * DIM + c];
+                }
+        }
+    }
+}
+
 // Thread per unenriched element: loops over lower block pairs (i >= j), and
 // for each pair over the Gauss points; writes block (i,j) and its transpose
-// (j,i), as the reference does (mesher/delaunay.cpp:2462-2467).
+// (j,i), as the reference does (mesher/delaunay.cpp:2462-2467).  Elements on
+// their kind's default rule take the hoisted path above.
 template <int DIM>
 __global__ void __launch_bounds__(128) k_quad_simple(MeshView m, const uint32_t *list, uint32_t count)
 {
@@ -45,25 +134,25 @@ __global__ void __launch_bounds__(128) k_quad_simple(MeshView m, const uint32_t 
     for (int i = 0; i < DIM * DIM; i++) Je[i] = m.jinv[(size_t)e * DIM * DIM + i];
     const uint32_t g0 = m.gp_ptr[e], g1 = m.gp_ptr[e + 1];
     const bool explicit_gp = g1 > g0;
-    const bool moved = explicit_gp && m.moved && m.moved[e];
-    const int ngp = explicit_gp ? (int)(g1 - g0) : (kind == AMIE_TRI6 ? 4 : 1);
-    const double inv_det = 1.0 / det_small<DIM>(Je);
     double *K = m.ke + m.blk_off[e] * DIM * DIM;
+    if (!explicit_gp) {
+        if (DIM == 2 && kind == AMIE_TRI6) quad_default<DIM, 6, 4>(kind, C, Je, K);
+        else if (DIM == 2) quad_default<DIM, 3, 1>(kind, C, Je, K);
+        else quad_default<DIM, 4, 1>(kind, C, Je, K);
+        return;
+    }
+    const bool moved = m.moved && m.moved[e];
+    const int ngp = (int)(g1 - g0);
     for (int i = 0; i < nf; i++) {
         for (int j = 0; j <= i; j++) {
             double acc[DIM * DIM];
 #pragma unroll
             for (int q = 0; q < DIM * DIM; q++) acc[q] = 0.0;
             for (int g = 0; g < ngp; g++) {
-                double p[3], w;
-                if (explicit_gp) {
-                    const double *gp = m.gp + (size_t)(g0 + g) * (DIM + 1);
-                    p[0] = gp[0]; p[1] = gp[1]; p[2] = DIM == 3 ? gp[2] : 0.0;
-                    w = gp[DIM];
-                } else {
-                    default_rule(kind, g, p, &w);
-                    w *= inv_det;   // weight / det(J^-1) (elements/elements.cpp:939-945)
-                }
+                double p[3];
+                const double *gp = m.gp + (size_t)(g0 + g) * (DIM + 1);
+                p[0] = gp[0]; p[1] = gp[1]; p[2] = DIM == 3 ? gp[2] : 0.0;
+                const double w = gp[DIM];
                 const double *J = moved ? m.jinv_gp + (size_t)(g0 + g) * DIM * DIM : Je;
                 double gi[3], gj[3], di[3], dj[3];
                 shape_grad(kind, i, p[0], p[1], gi);
@@ -85,43 +174,62 @@ __global__ void __launch_bounds__(128) k_quad_simple(MeshView m, const uint32_t 
     }
 }
 
-// Warp per enriched element (any number of functions <= kMaxFunctions and any
-// number of Gauss points).  Gauss points are processed in tiles: the lanes
-// first stage the physical gradients of every function at the tile's points
-// in shared memory, then each lane accumulates its own lower block pairs.
+// Warp quadrature of enriched elements (any number of functions <=
+// kMaxFunctions and any number of Gauss points).  Gauss points are processed in
+// tiles: the lanes first stage the physical gradients of every function at the
+// tile's points in shared memory, then each lane accumulates its own lower
+// block pairs.
 template <int DIM>
-__global__ void __launch_bounds__(32) k_quad_warp(MeshView m, const uint32_t *list, uint32_t count)
+struct WarpQuadSmem {
+    static constexpr int NV = DIM == 2 ? 3 : 6;
+    static constexpr int NPAIR = kMaxFunctions * (kMaxFunctions + 1) / 2;
+    double C[NV * NV];
+    double grad[kMaxGpWarpTile][kMaxFunctions][DIM];
+    double w[kMaxGpWarpTile];
+    double acc[NPAIR * DIM * DIM];
+};
+
+__device__ __forceinline__ void pair_of(int pidx, int &i, int &j)
 {
-    constexpr int NV = DIM == 2 ? 3 : 6;
+    // pair index -> (i, j), i >= j, row-major lower triangle
+    i = (int)((sqrt(8.0 * pidx + 1.0) - 1.0) * 0.5);
+    while ((i + 1) * (i + 2) / 2 <= pidx) i++;
+    while (i * (i + 1) / 2 > pidx) i--;
+    j = pidx - i * (i + 1) / 2;
+}
+
+// Stages C (times the element's factor) and zeroes the pair accumulators.
+template <int DIM>
+__device__ void warp_quad_begin(const MeshView &m, uint32_t e, int npair, WarpQuadSmem<DIM> &sm)
+{
+    constexpr int NV = WarpQuadSmem<DIM>::NV;
+    const int lane = threadIdx.x & 31;
+    const double cs = m.cscale ? m.cscale[e] : 1.0;
+    for (int i = lane; i < NV * NV; i += 32) sm.C[i] = cs * m.cmat_table[(size_t)m.mat[e] * NV * NV + i];
+    for (int i = lane; i < npair * DIM * DIM; i += 32) sm.acc[i] = 0.0;
+    __syncwarp();
+}
+
+// Accumulates the Gauss points [gb, ge) of element e into sm.acc.
+template <int DIM>
+__device__ void warp_quad_range(const MeshView &m, uint32_t e, int gb, int ge, WarpQuadSmem<DIM> &sm)
+{
     constexpr int T = kMaxGpWarpTile;
-    constexpr int NPAIR = kMaxFunctions * (kMaxFunctions + 1) / 2;
-    __shared__ double sC[NV * NV];
-    __shared__ double sGrad[T][kMaxFunctions][DIM];
-    __shared__ double sW[T];
-    __shared__ double sAcc[NPAIR * DIM * DIM];
-    const uint32_t w = blockIdx.x;
-    if (w >= count) return;
-    const int lane = threadIdx.x;
-    const uint32_t e = list[w];
+    const int lane = threadIdx.x & 31;
     const int kind = m.kind[e];
     const int nshape = nshape_of(kind);
     const uint32_t f0 = m.enr_ptr[e], f1 = m.enr_ptr[e + 1];
     const int nf = nshape + (int)(f1 - f0);
     const int npair = nf * (nf + 1) / 2;
-    const double cs = m.cscale ? m.cscale[e] : 1.0;
-    for (int i = lane; i < NV * NV; i += 32) sC[i] = cs * m.cmat_table[(size_t)m.mat[e] * NV * NV + i];
-    for (int i = lane; i < npair * DIM * DIM; i += 32) sAcc[i] = 0.0;
     double Je[DIM * DIM];
 #pragma unroll
     for (int i = 0; i < DIM * DIM; i++) Je[i] = m.jinv[(size_t)e * DIM * DIM + i];
     const uint32_t g0 = m.gp_ptr[e], g1 = m.gp_ptr[e + 1];
     const bool explicit_gp = g1 > g0;
     const bool moved = explicit_gp && m.moved && m.moved[e];
-    const int ngp = explicit_gp ? (int)(g1 - g0) : (kind == AMIE_TRI6 ? 4 : 1);
     const double inv_det = 1.0 / det_small<DIM>(Je);
-    __syncwarp();
-    for (int t0 = 0; t0 < ngp; t0 += T) {
-        const int nt = min(T, ngp - t0);
+    for (int t0 = gb; t0 < ge; t0 += T) {
+        const int nt = min(T, ge - t0);
         for (int item = lane; item < nt * nf; item += 32) {
             const int tg = item / nf, f = item % nf, g = t0 + tg;
             double p[3], wt;
@@ -156,42 +264,106 @@ __global__ void __launch_bounds__(32) k_quad_warp(MeshView m, const uint32_t *li
             double d[3];
             phys_grad<DIM>(J, lg, d);
 #pragma unroll
-            for (int c = 0; c < DIM; c++) sGrad[tg][f][c] = d[c];
-            if (f == 0) sW[tg] = wt;
+            for (int c = 0; c < DIM; c++) sm.grad[tg][f][c] = d[c];
+            if (f == 0) sm.w[tg] = wt;
         }
         __syncwarp();
         for (int pidx = lane; pidx < npair; pidx += 32) {
-            // pair index -> (i, j), i >= j, row-major lower triangle
-            int i = (int)((sqrt(8.0 * pidx + 1.0) - 1.0) * 0.5);
-            while ((i + 1) * (i + 2) / 2 <= pidx) i++;
-            while (i * (i + 1) / 2 > pidx) i--;
-            const int j = pidx - i * (i + 1) / 2;
+            int i, j;
+            pair_of(pidx, i, j);
             double acc[DIM * DIM];
 #pragma unroll
-            for (int q = 0; q < DIM * DIM; q++) acc[q] = sAcc[pidx * DIM * DIM + q];
-            for (int tg = 0; tg < nt; tg++) bcb<DIM>(sGrad[tg][i], sGrad[tg][j], sC, sW[tg], acc);
+            for (int q = 0; q < DIM * DIM; q++) acc[q] = sm.acc[pidx * DIM * DIM + q];
+            for (int tg = 0; tg < nt; tg++) bcb<DIM>(sm.grad[tg][i], sm.grad[tg][j], sm.C, sm.w[tg], acc);
 #pragma unroll
-            for (int q = 0; q < DIM * DIM; q++) sAcc[pidx * DIM * DIM + q] = acc[q];
+            for (int q = 0; q < DIM * DIM; q++) sm.acc[pidx * DIM * DIM + q] = acc[q];
         }
         __syncwarp();
     }
+}
+
+// Writes the accumulated pairs as blocks (i,j) and (j,i) of the staged K_e.
+template <int DIM>
+__device__ void warp_quad_store(const MeshView &m, uint32_t e, int nf, const double *acc)
+{
+    const int lane = threadIdx.x & 31;
+    const int npair = nf * (nf + 1) / 2;
     double *K = m.ke + m.blk_off[e] * DIM * DIM;
     for (int pidx = lane; pidx < npair; pidx += 32) {
-        int i = (int)((sqrt(8.0 * pidx + 1.0) - 1.0) * 0.5);
-        while ((i + 1) * (i + 2) / 2 <= pidx) i++;
-        while (i * (i + 1) / 2 > pidx) i--;
-        const int j = pidx - i * (i + 1) / 2;
+        int i, j;
+        pair_of(pidx, i, j);
         double *Kij = K + (size_t)(i * nf + j) * DIM * DIM;
         double *Kji = K + (size_t)(j * nf + i) * DIM * DIM;
 #pragma unroll
         for (int r = 0; r < DIM; r++)
 #pragma unroll
             for (int c = 0; c < DIM; c++) {
-                const double v = sAcc[pidx * DIM * DIM + r * DIM + c];
+                const double v = acc[pidx * DIM * DIM + r * DIM + c];
                 Kij[r * DIM + c] = v;
                 if (i != j) Kji[c * DIM + r] = v;
             }
     }
+}
+
+__device__ __forceinline__ int nf_of(const MeshView &m, uint32_t e)
+{
+    return nshape_of(m.kind[e]) + (int)(m.enr_ptr[e + 1] - m.enr_ptr[e]);
+}
+
+__device__ __forceinline__ int ngp_of(const MeshView &m, uint32_t e)
+{
+    const uint32_t g0 = m.gp_ptr[e], g1 = m.gp_ptr[e + 1];
+    return g1 > g0 ? (int)(g1 - g0) : (m.kind[e] == AMIE_TRI6 ? 4 : 1);
+}
+
+// Warp per enriched element with at most kLongGp Gauss points.
+template <int DIM>
+__global__ void __launch_bounds__(32) k_quad_warp(MeshView m, const uint32_t *list, uint32_t count)
+{
+    __shared__ WarpQuadSmem<DIM> sm;
+    const uint32_t w = blockIdx.x;
+    if (w >= count) return;
+    const uint32_t e = list[w];
+    const int nf = nf_of(m, e);
+    warp_quad_begin<DIM>(m, e, nf * (nf + 1) / 2, sm);
+    warp_quad_range<DIM>(m, e, 0, ngp_of(m, e), sm);
+    warp_quad_store<DIM>(m, e, nf, sm.acc);
+}
+
+// Elements with many Gauss points (the 512-point Monte-Carlo rule of a tip
+// element): one warp per chunk of kChunkGp points, each on its own SM, writes
+// its partial pair sums; k_quad_chunk_sum then adds the chunks of each element
+// in chunk order (a fixed order: the result does not depend on scheduling).
+template <int DIM>
+__global__ void __launch_bounds__(32) k_quad_chunk(MeshView m, const QuadChunk *chunks, uint32_t count,
+                                                   double *partial)
+{
+    __shared__ WarpQuadSmem<DIM> sm;
+    if (blockIdx.x >= count) return;
+    const QuadChunk c = chunks[blockIdx.x];
+    const int nf = nf_of(m, c.elem);
+    const int npair = nf * (nf + 1) / 2;
+    warp_quad_begin<DIM>(m, c.elem, npair, sm);
+    warp_quad_range<DIM>(m, c.elem, (int)c.gp_begin, (int)c.gp_end, sm);
+    for (int i = threadIdx.x; i < npair * DIM * DIM; i += 32) partial[c.out + i] = sm.acc[i];
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(32) k_quad_chunk_sum(MeshView m, const QuadLong *longs, uint32_t count,
+                                                       const QuadChunk *chunks, const double *partial)
+{
+    __shared__ double acc[WarpQuadSmem<DIM>::NPAIR * DIM * DIM];
+    if (blockIdx.x >= count) return;
+    const QuadLong L = longs[blockIdx.x];
+    const int nf = nf_of(m, L.elem);
+    const int n = nf * (nf + 1) / 2 * DIM * DIM;
+    for (int i = threadIdx.x; i < n; i += 32) {
+        double a = 0.0;
+        for (uint32_t c = L.chunk_first; c < L.chunk_first + L.chunk_count; c++) a += partial[chunks[c].out + i];
+        acc[i] = a;
+    }
+    __syncwarp();
+    warp_quad_store<DIM>(m, L.elem, nf, acc);
 }
 
 // Pattern keys: (row << 32 | col) for every (ids[j], ids[k]) of every element
@@ -660,10 +832,26 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
     // staged block offsets and kernel partition
     std::vector<uint64_t> blk_off(E + 1, 0);
     std::vector<uint32_t> simple, warp;
+    std::vector<QuadChunk> chunks;
+    std::vector<QuadLong> longs;
+    uint64_t partial = 0;
     for (uint32_t e = 0; e < E; e++) {
         blk_off[e + 1] = blk_off[e] + (uint64_t)nf[e] * nf[e];
         const uint32_t ne = mesh->enr_ptr ? mesh->enr_ptr[e + 1] - mesh->enr_ptr[e] : 0;
-        (ne ? warp : simple).push_back(e);
+        const uint32_t ngp = mesh->gp_ptr[e + 1] - mesh->gp_ptr[e];
+        if (!ne) {
+            simple.push_back(e);
+        } else if (ngp <= (uint32_t)kLongGp) {
+            warp.push_back(e);
+        } else {   // many Gauss points: chunks on separate SMs, summed in chunk order
+            QuadLong L{e, (uint32_t)chunks.size(), 0};
+            const uint64_t n_acc = (uint64_t)nf[e] * (nf[e] + 1) / 2 * s * s;
+            for (uint32_t g = 0; g < ngp; g += kChunkGp, L.chunk_count++) {
+                chunks.push_back(QuadChunk{e, g, std::min<uint32_t>(ngp, g + kChunkGp), partial});
+                partial += n_acc;
+            }
+            longs.push_back(L);
+        }
     }
     t->n_blocks_staged = blk_off[E];
     if (t->n_blocks_staged >= 0xffffffffull) {
@@ -707,6 +895,13 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
     UP(t->blk_off, blk_off.data(), E + 1);
     UP(t->simple_list, simple.data(), simple.size());
     UP(t->warp_list, warp.data(), warp.size());
+    t->n_chunks = (uint32_t)chunks.size();
+    t->n_long = (uint32_t)longs.size();
+    if (t->n_long) {
+        UP(t->quad_chunks, chunks.data(), chunks.size());
+        UP(t->quad_long, longs.data(), longs.size());
+        if ((rc = t->quad_partial.alloc(ctx, partial)) != AMIE_OK) return fail(rc);
+    }
     if (mesh->scale) {
         bool all_one = true;
         for (uint32_t e = 0; e < E; e++) all_one &= mesh->scale[e] == 1.0;
@@ -863,6 +1058,7 @@ extern "C" amie_status amie_topology_destroy(amie_topo *t)
     cudaSetDevice(t->ctx->device);
     cudaStreamSynchronize(t->ctx->stream);
     release_solver_state(t);
+    release_damage(t);
     delete t;
     return AMIE_OK;
 }
@@ -914,6 +1110,18 @@ amie_status assemble_async(amie_topo *t)
         else
             k_quad_simple<3><<<blocks_for(t->n_simple, 128), 128, 0, st>>>(m, t->simple_list.p, t->n_simple);
         AMIE_LAUNCHED();
+    }
+    if (t->n_long) {
+        if (t->dim == 2) {
+            k_quad_chunk<2><<<t->n_chunks, 32, 0, st>>>(m, t->quad_chunks.p, t->n_chunks, t->quad_partial.p);
+            k_quad_chunk_sum<2><<<t->n_long, 32, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
+                                                           t->quad_partial.p);
+        } else {
+            k_quad_chunk<3><<<t->n_chunks, 32, 0, st>>>(m, t->quad_chunks.p, t->n_chunks, t->quad_partial.p);
+            k_quad_chunk_sum<3><<<t->n_long, 32, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
+                                                           t->quad_partial.p);
+        }
+        g_launches += 2;
     }
     if (t->n_warp) {
         if (t->dim == 2)

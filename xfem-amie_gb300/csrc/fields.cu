@@ -1,13 +1,9 @@
-// fields.cu -- strain / stress recovery and the scalar damage update of a
-// damage loop, on the device, from the device-resident solution.
+// fields.cu -- strain / stress recovery on the device from the device-resident
+// solution.
 //
 // Reference (paths relative to the AMIE source tree):
 //   strain   FeatureTree::strainFromDisplacements  features/features.cpp:4223
 //   stress   FeatureTree::stressFromDisplacements  features/features.cpp:3424
-//   damage   StiffnessAndFracture::step            physics/stiffness_and_fracture.cpp:81-90,
-//            the (1-d) C of IsotropicLinearDamage::apply (physics/damagemodels/isotropiclineardamage.cpp:39-46),
-//            a Mazars equivalent strain (physics/fracturecriteria/mazars.cpp:153) with
-//            exponential softening d = 1 - (eps0/eq) exp(-B (eq - eps0)).
 #include "element.cuh"
 
 #include <algorithm>
@@ -110,28 +106,6 @@ __global__ void k_element_fields(MeshView m, const double *x, double *strain, do
     }
 }
 
-// Mazars equivalent strain from the positive principal strains (2D plane
-// strain tensor [exx, exy/2; exy/2, eyy]), exponential softening, irreversible
-// damage, C factor = base * (1 - d).
-__global__ void k_damage(uint32_t n_elem, const double *strain, amie_damage_params prm, double *damage,
-                         const double *cscale_base, double *cscale, uint32_t *n_changed)
-{
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_elem) return;
-    const double exx = strain[(size_t)e * 3], eyy = strain[(size_t)e * 3 + 1], gxy = strain[(size_t)e * 3 + 2];
-    const double c = 0.5 * (exx + eyy);
-    const double rad = sqrt(0.25 * (exx - eyy) * (exx - eyy) + 0.25 * gxy * gxy);
-    const double e1 = fmax(c + rad, 0.0), e2 = fmax(c - rad, 0.0);
-    const double eq = sqrt(e1 * e1 + e2 * e2);
-    double dn = 0.0;
-    if (eq > prm.eps0) dn = 1.0 - (prm.eps0 / eq) * exp(-prm.softening * (eq - prm.eps0));
-    const double dold = damage[e];
-    const double d = fmin(prm.d_max, fmax(dold, dn));
-    damage[e] = d;
-    cscale[e] = (cscale_base ? cscale_base[e] : 1.0) * (1.0 - d);
-    if (d - dold > prm.change_tol) atomicAdd(n_changed, 1u);
-}
-
 // Per-CTA sums of v_e f_e (nv components) and v_e, v_e the element's area
 // (2D: 0.5 / |det J^-1|, the triangle of its corners) or volume (3D:
 // (1/6) / |det J^-1|), J^-1 at the centroid.  Each thread Kahan-sums its
@@ -174,6 +148,19 @@ __global__ void __launch_bounds__(256) k_average_parts(uint32_t n_elem, const do
 
 MeshView mesh_view(amie_topo *t);
 
+// t->strain = the element strains of the device solution (launch only).
+amie_status element_strain_async(amie_topo *t)
+{
+    if (!t->strain.p) AMIE_TRY(t->strain.alloc(t->ctx, (size_t)t->n_elem * t->nv));
+    const MeshView m = mesh_view(t);
+    const unsigned blocks = (t->n_elem + 127) / 128;
+    if (t->dim == 2) k_element_fields<2><<<blocks, 128, 0, t->ctx->stream>>>(m, t->x.p, t->strain.p, nullptr);
+    else k_element_fields<3><<<blocks, 128, 0, t->ctx->stream>>>(m, t->x.p, t->strain.p, nullptr);
+    AMIE_LAUNCHED();
+    AMIE_CUDA(cudaGetLastError());
+    return AMIE_OK;
+}
+
 }  // namespace amie
 
 using namespace amie;
@@ -195,44 +182,6 @@ extern "C" amie_status amie_element_fields(amie_topo *t, double *strain, double 
     if (strain) AMIE_CUDA(cudaMemcpyAsync(strain, t->strain.p, (size_t)t->n_elem * nv * 8, cudaMemcpyDeviceToHost, st));
     if (stress) AMIE_CUDA(cudaMemcpyAsync(stress, dstress.p, (size_t)t->n_elem * nv * 8, cudaMemcpyDeviceToHost, st));
     AMIE_CUDA(cudaStreamSynchronize(st));
-    return AMIE_OK;
-}
-
-extern "C" amie_status amie_damage_step(amie_topo *t, const amie_damage_params *prm, uint32_t *n_changed,
-                                        double *damage_out)
-{
-    if (!t || !prm) return AMIE_BAD_INPUT;
-    if (t->dim != 2) {
-        set_error("the damage update is implemented for 2D meshes");
-        return AMIE_BAD_INPUT;
-    }
-    AMIE_CUDA(cudaSetDevice(t->ctx->device));
-    cudaStream_t st = t->ctx->stream;
-    const uint32_t E = t->n_elem;
-    if (!t->damage.p) {
-        AMIE_TRY(t->damage.alloc(t->ctx, E));
-        AMIE_CUDA(cudaMemsetAsync(t->damage.p, 0, (size_t)E * 8, st));
-        if (t->has_cscale) {   // keep the caller's factor (per-element modulus) as the base
-            AMIE_TRY(t->cscale_base.alloc(t->ctx, E));
-            AMIE_CUDA(cudaMemcpyAsync(t->cscale_base.p, t->cscale.p, (size_t)E * 8, cudaMemcpyDeviceToDevice, st));
-        }
-        if (!t->cscale.p) AMIE_TRY(t->cscale.alloc(t->ctx, E));
-        t->has_cscale = true;
-    }
-    if (!t->strain.p) AMIE_TRY(t->strain.alloc(t->ctx, (size_t)E * t->nv));
-    DevArray<uint32_t> counter;
-    AMIE_TRY(counter.alloc(t->ctx, 1));
-    AMIE_CUDA(cudaMemsetAsync(counter.p, 0, 4, st));
-    MeshView m = mesh_view(t);
-    const unsigned blocks = (E + 127) / 128;
-    k_element_fields<2><<<blocks, 128, 0, st>>>(m, t->x.p, t->strain.p, nullptr);
-    k_damage<<<blocks, 128, 0, st>>>(E, t->strain.p, *prm, t->damage.p, t->cscale_base.p, t->cscale.p, counter.p);
-    g_launches += 2;
-    uint32_t changed = 0;
-    AMIE_CUDA(cudaMemcpyAsync(&changed, counter.p, 4, cudaMemcpyDeviceToHost, st));
-    if (damage_out) AMIE_CUDA(cudaMemcpyAsync(damage_out, t->damage.p, (size_t)E * 8, cudaMemcpyDeviceToHost, st));
-    AMIE_CUDA(cudaStreamSynchronize(st));
-    if (n_changed) *n_changed = changed;
     return AMIE_OK;
 }
 

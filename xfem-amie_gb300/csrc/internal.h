@@ -17,6 +17,18 @@ namespace amie {
 constexpr int kSMs = 152;          // GB300: 2 dies x 76 SMs
 constexpr int kMaxFunctions = 32;  // shape + enrichment functions per element
 constexpr int kMaxGpWarpTile = 8;  // Gauss points staged per tile in the warp quadrature kernel
+constexpr int kLongGp = 64;        // enriched elements with more Gauss points are split into chunks
+constexpr int kChunkGp = 16;       // Gauss points per chunk of a long element
+
+// One chunk of the Gauss points of a long enriched element and where its
+// partial pair sums go; a long element and its chunks.
+struct QuadChunk {
+    uint32_t elem, gp_begin, gp_end;
+    uint64_t out;
+};
+struct QuadLong {
+    uint32_t elem, chunk_first, chunk_count;
+};
 
 void set_error(const char *fmt, ...);
 extern std::atomic<uint64_t> g_launches;
@@ -152,6 +164,11 @@ struct SellView {
 
 }  // namespace amie
 
+namespace amie {
+struct DamageState;
+}
+void release_damage(amie_topo *t);   // damage.cu
+
 // Opaque handles of the C-ABI.
 struct amie_ctx : public amie::Ctx {};
 
@@ -171,6 +188,10 @@ struct amie_topo {
     amie::DevArray<uint64_t> blk_off;
     amie::DevArray<uint32_t> simple_list, warp_list;   // elements per quadrature kernel
     uint32_t n_simple = 0, n_warp = 0;
+    amie::DevArray<amie::QuadChunk> quad_chunks;         // long enriched elements, split by Gauss points
+    amie::DevArray<amie::QuadLong> quad_long;
+    amie::DevArray<double> quad_partial;
+    uint32_t n_chunks = 0, n_long = 0;
 
     // staging + scatter map
     amie::DevArray<double> ke;
@@ -210,7 +231,8 @@ struct amie_topo {
     amie::DevArray<float> p32_alt;
     amie::DevArray<uint8_t> fixed;
     amie::DevArray<double> fixval;
-    amie::DevArray<double> strain, damage, cscale_base;   // field recovery and damage loop
+    amie::DevArray<double> strain;    // element strains (field recovery, damage grading)
+    amie::DamageState *dmg = nullptr; // damage path (amie_damage_setup)
     amie::DevArray<double> x_hist;    // previous solution for amie_extrapolate (zero until first used)
     // imposed strain (per element) and its induced forces: staged per element
     // function, gathered per block row through fmap (contributions in element order)

@@ -710,6 +710,15 @@ extern "C" amie_status amie_solution_download(const amie_topo *t, double *x)
     return AMIE_OK;
 }
 
+extern "C" amie_status amie_solution_upload(amie_topo *t, const double *x)
+{
+    if (!t || !x) return AMIE_BAD_INPUT;
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    AMIE_CUDA(cudaMemcpyAsync(t->x.p, x, t->n * 8, cudaMemcpyHostToDevice, t->ctx->stream));
+    AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
+    return AMIE_OK;
+}
+
 extern "C" amie_status amie_timer_start(amie_ctx *ctx)
 {
     if (!ctx) return AMIE_BAD_INPUT;

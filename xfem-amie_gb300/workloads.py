@@ -462,12 +462,18 @@ def serving_mix(n_requests, rate, dof_min=2000, dof_max=200000, seed=7, pool=64)
 
 
 def notched_beam(nx=706, ny=176, Lx=0.4, Ly=0.1, notch_w=0.02, notch_h=0.002, E=35e9, nu=0.2, seed=3,
-                 jitter=0.1):
+                 jitter=0.1, patch=0.02, support=0.02):
     """Config-3 family: 400 x 100 mm beam, P1 triangles, a 20 x 2 mm notch at the
     bottom of midspan (elements inside removed, as a VoidForm feature leaves them
-    without stiffness; orphan nodes renumbered away), three-point bending:
-    bottom-left corner fixed in x and y, bottom-right corner fixed in y, the top
-    midspan node displaced downwards (the load of each step is a multiplier value)."""
+    without stiffness; orphan nodes renumbered away), three-point bending on
+    plates: the bottom nodes within `support` of either end fixed in y, the
+    bottom-left corner also in x, and the top nodes of a `patch`-wide loading
+    plate at midspan displaced downwards (the load of each step is a multiplier
+    value; BoundingBoxAndRestriction conditions in the reference).  Plates rather
+    than single nodes keep the strain at the supports finite, so damage starts
+    at the notch.  meta["corners"]: the vertices of every element (n_elem x 6)
+    for the damage setup; meta["notch_tip"]: (x, y) of the notch's top edge at
+    midspan."""
     rng = np.random.default_rng(seed)
     hx, hy = Lx / nx, Ly / ny
     M = nx + 1
@@ -502,13 +508,18 @@ def notched_beam(nx=706, ny=176, Lx=0.4, Ly=0.1, notch_w=0.02, notch_h=0.002, E=
                     mat=np.zeros(E_count, np.uint32), cmat_table=plane_stress(E, nu).reshape(-1), ndofmax=len(x))
     tol = 1e-12
     left = int(np.nonzero((np.abs(x) < tol) & (np.abs(y) < tol))[0][0])
-    right = int(np.nonzero((np.abs(x - Lx) < tol) & (np.abs(y) < tol))[0][0])
-    top = int(np.argmin(np.abs(x - Lx / 2) + 10 * np.abs(y - Ly)))
-    meta = dict(n_nodes=len(x), n_elem=E_count, n_dof=2 * len(x), load_node=top)
+    bottom = np.abs(y) < tol
+    supports = np.nonzero(bottom & ((x <= support + tol) | (x >= Lx - support - tol)))[0]
+    plate = np.nonzero((np.abs(y - Ly) < tol) & (np.abs(x - Lx / 2) <= patch / 2 + tol))[0]
+    corners = np.stack([vx, vy], 2).reshape(E_count, 6)   # (x0, y0, x1, y1, x2, y2) per element
+    meta = dict(n_nodes=len(x), n_elem=E_count, n_dof=2 * len(x), load_nodes=len(plate),
+                support_nodes=len(supports), corners=corners, notch_tip=(Lx / 2, notch_h))
+    fixed = sorted([2 * left] + (2 * supports + 1).tolist())
+    loaded = set((2 * plate + 1).tolist())
 
     def bcs(deflection):
-        ids = np.array(sorted([2 * left, 2 * left + 1, 2 * right + 1, 2 * top + 1]), np.uint32)
-        vals = np.array([-deflection if i == 2 * top + 1 else 0.0 for i in ids])
+        ids = np.array(sorted(fixed + sorted(loaded)), np.uint32)
+        vals = np.array([-deflection if int(i) in loaded else 0.0 for i in ids])
         return ids, vals, np.zeros(len(ids), np.uint8)
     return m, bcs, meta
 
