@@ -63,8 +63,9 @@ def test_device_grade_matches_reference(gpu_ctx):
 
 
 def test_device_update_matches_oracle(gpu_ctx):
-    """A pass far from equilibrium: the step-2 displacements doubled on the step-2
-    damage, with every element at 0.5 promoted so that increments fracture them."""
+    """A pass far from equilibrium: the step-2 displacements quadrupled, on the
+    step-2 damage with the criterion-meeting elements raised to 0.5, so that
+    their increments fracture them in this pass."""
     d = load_golden("damage_p1")
     n = int(d["n_elem"][0])
     law = law_of(d)
@@ -72,11 +73,14 @@ def test_device_update_matches_oracle(gpu_ctx):
     c, r, a = O.damage_geometry(xy)
     cache = O.damage_cache(law.radius, xy, c, r, a)
     state = state_of(d["damage_2"])
-    u = 2.0 * d["u_2"]
+    u = 4.0 * d["u_2"]
     t, m = damage_topology(gpu_ctx, d)
     try:
         t.damage_set_state(state)
         t.solution_upload(u)
+        met = t.damage_grade()[0] > 0
+        state = np.where(met, state_of(np.full(n, 0.5)), state)
+        t.damage_set_state(state)
         score, _ = t.damage_grade()
         eps, _ = O.element_fields(m, u)
         score_o, _ = O.damage_grade(law, eps, d["cmat"].reshape(n, 9), state, a, d["gp"].reshape(-1, 3)[:, 2], cache)

@@ -158,7 +158,7 @@ amie_status noalloc_solve(const NoAllocDevice &dev, uint32_t n_rows, const uint3
         if (total >= maxit) break;
         PcgCtl c{};   // done = 0, ticket = 0, iterations = 0
         c.maxit = maxit - total;
-        c.tol2 = (kFp64StopFraction * kFp64StopFraction) * target2;
+        c.tol2 = 0.25 * target2;
         AMIE_CUDA(cudaMemcpyAsync(ctl, &c, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
         k_pcg_start<double><<<grid, kVecThreads, 0, st>>>(v, n, pp, ctl);
         AMIE_LAUNCHED();

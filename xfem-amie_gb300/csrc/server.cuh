@@ -527,7 +527,7 @@ struct ServerOps {
             c.tol2 = inner * inner;
         } else {
             const double target = srv->cfg.rtol * r->bnorm;
-            c.tol2 = (kFp64StopFraction * kFp64StopFraction) * target * target;
+            c.tol2 = 0.25 * target * target;
         }
         srv->h_ctl[slot] = c;
         AMIE_CUDA(cudaMemcpyAsync(srv->d_ctl.p + slot, srv->h_ctl + slot, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));

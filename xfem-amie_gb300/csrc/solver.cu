@@ -38,6 +38,19 @@ const void *sell_dir_kernel(int s, int hint)
     return (const void *)k_sell_dir<3, T, 0>;
 }
 
+template <bool START>
+const void *sell_cgcg_kernel(int s, int hint)
+{
+    if (s == 2) {
+        if (hint == 1) return (const void *)k_sell_cgcg<2, float, 1, START>;
+        if (hint == 2) return (const void *)k_sell_cgcg<2, float, 2, START>;
+        return (const void *)k_sell_cgcg<2, float, 0, START>;
+    }
+    if (hint == 1) return (const void *)k_sell_cgcg<3, float, 1, START>;
+    if (hint == 2) return (const void *)k_sell_cgcg<3, float, 2, START>;
+    return (const void *)k_sell_cgcg<3, float, 0, START>;
+}
+
 struct SolverState {
     int grid = 0;                 // block-CSR SpMV, AMIE_CG and server kernels
     int grid_vec[2] = {0, 0};     // PCG vector kernels, FP32 / FP64 (resident CTAs of k_update)
@@ -65,10 +78,19 @@ struct SolverState {
     cudaEvent_t ring_ev[2] = {nullptr, nullptr};
     cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
     int graph_iters = 0;
+    DevArray<double> x_saved;        // FP64 solve: the first stage's iterate while the second runs
+    // FP32 inner runs of the mixed solver as single-reduction (Chronopoulos-Gear)
+    // PCG, one kernel per iteration (AMIE_CGCG=0: the two-kernel standard PCG)
+    bool cgcg = true;
+    int grid_cgcg = 0;
+    int cg_cur = 0;                  // buffer of r, w holding the current FP32 residual
+    DevArray<float> r32b, w32[2], s32[2], slice3;
+    cudaGraphExec_t graph_cg = nullptr;
     ~SolverState()
     {
         if (graph64) cudaGraphExecDestroy(graph64);
         if (graph32) cudaGraphExecDestroy(graph32);
+        if (graph_cg) cudaGraphExecDestroy(graph_cg);
         if (h_ctl) cudaFreeHost(h_ctl);
         if (h_ring) cudaFreeHost(h_ring);
         for (cudaEvent_t e : ring_ev)
@@ -281,7 +303,11 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         if (const char *e = std::getenv("AMIE_PREFETCH_KB")) s->prefetch_bytes = (uint32_t)std::min(1024, std::max(0, std::atoi(e))) * 1024u;
         s->grid_dir[0] = resident(sell_dir_kernel<float>(t->s, s->matrix_hint), 0);
         s->grid_dir[1] = resident(sell_dir_kernel<double>(t->s, s->matrix_hint), 0);
+        s->grid_cgcg = std::min(resident(sell_cgcg_kernel<false>(t->s, s->matrix_hint), 0),
+                                resident(sell_cgcg_kernel<true>(t->s, s->matrix_hint), 0));
+        if (const char *e = std::getenv("AMIE_CGCG")) s->cgcg = std::atoi(e) != 0;
         AMIE_CUDA(cudaGetLastError());
+        AMIE_TRY(ensure_sell_partition(t, s->grid_cgcg));
         AMIE_TRY(ensure_sell_partition(t, s->grid));
         AMIE_TRY(ensure_sell_partition(t, s->grid_sell[0]));
         AMIE_TRY(ensure_sell_partition(t, s->grid_sell[1]));
@@ -289,7 +315,7 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         AMIE_TRY(ensure_sell_partition(t, s->grid_dir[1]));
         s->stride = std::max(std::max(std::max(s->grid, std::max(s->grid_vec[0], s->grid_vec[1])),
                                       std::max(s->grid_sell[0], s->grid_sell[1])),
-                             std::max(s->grid_dir[0], s->grid_dir[1]));
+                             std::max(std::max(s->grid_dir[0], s->grid_dir[1]), s->grid_cgcg));
         // tuning overrides for measurements: AMIE_PDL=0 launches the PCG graph kernels plainly,
         // AMIE_FOLD_DIR=0 keeps the separate direction kernel (three kernels per iteration)
         if (const char *e = std::getenv("AMIE_PDL")) s->pdl = std::atoi(e) != 0;
@@ -314,6 +340,18 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         AMIE_TRY(t->q32.alloc(t->ctx, n));
         AMIE_TRY(t->d32.alloc(t->ctx, n));
         AMIE_TRY(t->p32_alt.alloc(t->ctx, n));
+    }
+    if (want32 && s->cgcg && !s->r32b.p) {
+        const uint64_t n = t->n;
+        AMIE_TRY(s->r32b.alloc(t->ctx, n));
+        for (int k = 0; k < 2; k++) {
+            AMIE_TRY(s->w32[k].alloc(t->ctx, n));
+            AMIE_TRY(s->s32[k].alloc(t->ctx, n));
+            AMIE_CUDA(cudaMemsetAsync(s->w32[k].p, 0, n * 4, t->ctx->stream));
+            AMIE_CUDA(cudaMemsetAsync(s->s32[k].p, 0, n * 4, t->ctx->stream));
+        }
+        AMIE_TRY(s->slice3.alloc(t->ctx, 3 * (size_t)std::max<uint32_t>(t->n_slices, 1)));
+        s->cg_cur = 0;
     }
     *out = s;
     return AMIE_OK;
@@ -360,6 +398,60 @@ bool launch_spmv_dir(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, 
 }
 
 constexpr int kGraphIters = 16;   // PCG iterations per graph launch
+
+CgcgVecs<float> cgcg_vecs(amie_topo *t, SolverState *s)
+{
+    CgcgVecs<float> v;
+    v.dinv = t->invdiag32.p;
+    v.x = t->d32.p;
+    v.p = t->p32.p;
+    v.r[0] = t->r32.p;
+    v.r[1] = s->r32b.p;
+    v.w[0] = s->w32[0].p;
+    v.w[1] = s->w32[1].p;
+    v.s[0] = s->s32[0].p;
+    v.s[1] = s->s32[1].p;
+    v.slice3 = s->slice3.p;
+    return v;
+}
+
+// One launch of k_sell_cgcg (start: the run's first pass).
+void launch_cgcg(amie_topo *t, SolverState *s, bool start, bool pdl, cudaStream_t st)
+{
+    SellView<float> sv = sell_of<float>(t);
+    sv.prefetch_bytes = s->prefetch_bytes;
+    sv.cta_first = t->sell_cta_first.find(s->grid_cgcg)->second.p;
+    auto kern = (void (*)(SellView<float>, CgcgVecs<float>, double *, PcgCtl *))(
+        start ? sell_cgcg_kernel<true>(t->s, s->matrix_hint) : sell_cgcg_kernel<false>(t->s, s->matrix_hint));
+    launch_k(pdl, kern, s->grid_cgcg, 0, st, sv, cgcg_vecs(t, s), parts_of(s).pq, s->ctl.p);
+    AMIE_LAUNCHED();
+}
+
+amie_status graph_cgcg(amie_topo *t, SolverState *s)
+{
+    if (s->graph_cg) return AMIE_OK;
+    cudaStream_t st = t->ctx->stream;
+    cudaGraph_t graph = nullptr;
+    AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const uint64_t before = g_launches.load();
+    for (int it = 0; it < kGraphIters; it++) launch_cgcg(t, s, false, s->pdl && it > 0, st);
+    g_launches = before;   // captured, not launched: counted per graph launch
+    AMIE_CUDA(cudaStreamEndCapture(st, &graph));
+    cudaError_t e = cudaGraphInstantiate(&s->graph_cg, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        s->graph_cg = nullptr;
+        set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        return AMIE_CUDA_ERROR;
+    }
+    return AMIE_OK;
+}
+
+// Whether the mixed solver's FP32 runs use k_sell_cgcg (needs the FP32 SELL copy).
+bool use_cgcg(amie_topo *t, SolverState *s)
+{
+    return s->cgcg && s->r32b.p && t->sell32_ok && t->sell_cta_first.count(s->grid_cgcg);
+}
 
 template <typename T>
 amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
@@ -421,11 +513,17 @@ amie_status read_sum(amie_topo *t, const double *dev, int n, double *out)
 
 // Launches the PCG graph until the control block reports done.
 template <typename T>
-amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iters, double *rr_out)
+amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iters, double *rr_out,
+                      bool cgcg = false)
 {
     cudaStream_t st = t->ctx->stream;
     cudaGraphExec_t *g = sizeof(T) == 8 ? &s->graph64 : &s->graph32;
-    AMIE_TRY(graph_for<T>(t, s, g));
+    if (cgcg) {
+        AMIE_TRY(graph_cgcg(t, s));
+        g = &s->graph_cg;
+    } else {
+        AMIE_TRY(graph_for<T>(t, s, g));
+    }
     // Host watchdog: the device sets `done` by maxit at the latest, so more
     // launches than maxit / kGraphIters + 2 mean the control block is not advancing.
     const int64_t max_launches = maxit / kGraphIters + 2;
@@ -434,9 +532,10 @@ amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iter
     // check.  A launch queued after the stop finds `done` set and its kernels
     // return at once.  Each ring slot is read only after its event completed.
     const int pi = sizeof(T) == 8 ? 1 : 0;
+    const int per_iter = cgcg ? 1 : s->graph_kernels[pi];
     auto launch = [&](int64_t k) -> amie_status {
         AMIE_CUDA(cudaGraphLaunch(*g, st));
-        g_launches += s->graph_kernels[pi] * kGraphIters;
+        g_launches += per_iter * kGraphIters;
         AMIE_CUDA(cudaMemcpyAsync(s->h_ring + (k & 1), s->ctl.p, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
         AMIE_CUDA(cudaEventRecord(s->ring_ev[k & 1], st));
         return AMIE_OK;
@@ -504,6 +603,37 @@ amie_status resume_pcg(amie_topo *t, SolverState *s, double ratio, double tol2, 
     }
     AMIE_CUDA(cudaGetLastError());
     return drive_pcg<T>(t, s, maxit, iters, rr_out);
+}
+
+// A single-reduction FP32 run from the residual in r[cg_cur]: scale = the
+// previous run's residual scale over the new one to keep the search direction
+// (reliable update), 0 for a fresh start.
+amie_status run_cgcg(amie_topo *t, SolverState *s, double scale, double tol2, int64_t maxit, int64_t *iters,
+                     double *rr_out)
+{
+    cudaStream_t st = t->ctx->stream;
+    PcgCtl c = *s->h_ctl;   // the previous run's final state (gamma, alpha)
+    c.done = 0;
+    c.ticket = 0;
+    c.iterations = 0;
+    c.maxit = maxit;
+    c.tol2 = tol2;
+    c.pcur = s->cg_cur;
+    c.pq = scale;
+    if (scale != 0.0) {
+        c.rz = c.rz * scale * scale;
+    } else {
+        c.rz = 0.0;
+        c.alpha = 0.0;
+    }
+    *s->h_ctl = c;
+    AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
+    launch_cgcg(t, s, true, false, st);
+    // the pinned copy is rewritten by drive_pcg only after this copy has completed
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    AMIE_TRY(drive_pcg<float>(t, s, maxit, iters, rr_out, true));
+    s->cg_cur = s->h_ctl->pcur;
+    return AMIE_OK;
 }
 
 __global__ void k_scale_to_f32(uint64_t n, const double *r, double inv, float *r32, float *d32)
@@ -575,15 +705,16 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
         int64_t it = 0;
         double rr_in = 0.0;
         if (!mixed) {
-            // recursive residual target below the true one (the true residual is re-checked)
-            AMIE_TRY(run_pcg<double>(t, s, target2 * (kFp64StopFraction * kFp64StopFraction), maxit - total,
-                                     &it, &rr_in));
+            // recursive residual target a little below the true one (the true residual is re-checked)
+            AMIE_TRY(run_pcg<double>(t, s, target2 * 0.25, maxit - total, &it, &rr_in));
         } else {
             // FP32 PCG on the residual scaled to unit norm; at each return the FP32
             // increment is added to x in FP64, r is replaced by the true FP64
             // residual and the FP32 run resumes with its search direction kept.
             const double norm = std::sqrt(rr);
-            k_scale_to_f32<<<s->grid, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / norm, t->r32.p, t->d32.p);
+            const bool cg = use_cgcg(t, s);
+            float *r32 = cg && s->cg_cur ? s->r32b.p : t->r32.p;
+            k_scale_to_f32<<<s->grid, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / norm, r32, t->d32.p);
             AMIE_LAUNCHED();
             // reduce by inner_rtol, or by less when that is all the outer target still needs
             const double need = kMixedLastTarget * rtol * bnorm / norm;
@@ -591,8 +722,9 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
             // keep the search direction only while replacements show real progress; a
             // true residual that fell by less than half means the FP32 recursion has
             // drifted from it, and the run restarts from the new residual instead
-            if (prev_norm == 0.0 || norm > 0.5 * prev_norm)
-                AMIE_TRY(run_pcg<float>(t, s, inner * inner, maxit - total, &it, &rr_in));
+            const bool fresh = prev_norm == 0.0 || norm > 0.5 * prev_norm;
+            if (cg) AMIE_TRY(run_cgcg(t, s, fresh ? 0.0 : prev_norm / norm, inner * inner, maxit - total, &it, &rr_in));
+            else if (fresh) AMIE_TRY(run_pcg<float>(t, s, inner * inner, maxit - total, &it, &rr_in));
             else AMIE_TRY(resume_pcg<float>(t, s, norm / prev_norm, inner * inner, maxit - total, &it, &rr_in));
             prev_norm = norm;
             k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, norm, t->x.p);
@@ -602,6 +734,27 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
         total += it;
         AMIE_TRY(true_residual(t, s, &rr));
         if (!mixed && it == 0) break;
+    }
+    if (!mixed && result == AMIE_OK && total > 0 && total < maxit &&
+        !(rr <= target2 * (kFp64StopFraction * kFp64StopFraction))) {
+        // Second stage of the FP64 stop: the same recursion continues (direction
+        // kept) towards kFp64StopFraction rtol within a quarter more iterations;
+        // its iterate is kept only if the true residual improved (a nearly
+        // singular system may not get there, and then the first stage stands).
+        if (!s->x_saved.p) AMIE_TRY(s->x_saved.alloc(t->ctx, t->n));
+        AMIE_CUDA(cudaMemcpyAsync(s->x_saved.p, t->x.p, t->n * 8, cudaMemcpyDeviceToDevice, st));
+        const int64_t extra = std::min<int64_t>(maxit - total, std::max<int64_t>(64, total / 4));
+        int64_t it2 = 0;
+        double rr_in = 0.0, rr2 = 0.0;
+        AMIE_TRY(resume_pcg<double>(t, s, 1.0, target2 * (kFp64StopFraction * kFp64StopFraction), extra, &it2,
+                                    &rr_in));
+        AMIE_TRY(true_residual(t, s, &rr2));
+        total += it2;
+        if (rr2 <= rr) {
+            rr = rr2;
+        } else {
+            AMIE_CUDA(cudaMemcpyAsync(t->x.p, s->x_saved.p, t->n * 8, cudaMemcpyDeviceToDevice, st));
+        }
     }
     AMIE_CUDA(cudaGetLastError());
     st_out->iterations = total;

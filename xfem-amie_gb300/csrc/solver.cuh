@@ -29,12 +29,13 @@ namespace amie {
 constexpr int kVecThreads = 256;
 
 // Stopping targets of the PCG drivers, as fractions of the requested relative
-// residual rtol.  FP64: the recursive residual is driven to kFp64StopFraction
-// rtol before the true residual is checked against rtol; at rtol = 1e-10 this
-// keeps node displacements within 1e-9 (relative to the largest) of a 1e-13
-// solve on the 1.2 M-DOF P2 workload (5.8e-10; 4.1e-9 when stopped at 0.5 rtol)
-// for 3.5 % more iterations.  Mixed: the last FP32 segment aims at
-// kMixedLastTarget rtol (displacements within 1e-8 with a margin of two).
+// residual rtol.  FP64: once the true residual meets rtol (first stage,
+// recursive target 0.5 rtol) the recursion continues towards kFp64StopFraction
+// rtol within a quarter more iterations; at rtol = 1e-10 this keeps node
+// displacements within 1e-9 (relative to the largest) of a 1e-13 solve on the
+// 1.2 M-DOF P2 workload (5.8e-10; 4.1e-9 when stopped at 0.5 rtol) for 3.5 %
+// more iterations.  Mixed: the last FP32 segment aims at kMixedLastTarget rtol
+// (displacements within 1e-8 with a margin of two).
 constexpr double kFp64StopFraction = 0.1;
 constexpr double kMixedLastTarget = 0.2;
 
@@ -1371,6 +1372,260 @@ __global__ void __launch_bounds__(kVecThreads) k_pcg_resume(PcgVecs<T> v, uint64
     __shared__ double sh[33];
     __shared__ int flag;
     resume_body<T>(v, n, parts, ctl, ratio, tol2, maxit, sh, &flag, grid_cta());
+}
+
+
+// ------------------------------------------------------------------ single-reduction PCG
+// Chronopoulos-Gear PCG (A. T. Chronopoulos and C. W. Gear, "s-step iterative
+// methods for symmetric linear systems", J. Comput. Appl. Math. 25 (1989)
+// 153-168; the s = 1 form): with u = D^-1 r and w = A u,
+//   p_i = u_i + beta_i p_(i-1),  s_i = w_i + beta_i s_(i-1)   (s_i = A p_i)
+//   x += alpha_i p_i,  r_(i+1) = r_i - alpha_i s_i,  u_(i+1) = D^-1 r_(i+1),  w_(i+1) = A u_(i+1)
+//   gamma = r.u, delta = w.u (both of iteration i+1, one reduction),
+//   beta_(i+1) = gamma_(i+1) / gamma_i,  alpha_(i+1) = gamma_(i+1) / (delta_(i+1) - beta_(i+1) gamma_(i+1) / alpha_i).
+// One kernel per iteration: every warp updates p, s, x, r of its own rows and
+// computes w = A u_(i+1) with u_(i+1) of the gathered columns formed from r_i,
+// w_i, s_(i-1) and D^-1 by the same expression as for its own rows, so the
+// gathered and the stored values agree bit for bit.  r, w and s have two
+// buffers each (read one, write the other; ctl->pcur selects), p and x are
+// touched by their own rows only.  Dots: per-slice partials in the vector
+// precision, summed in slice order per CTA, then in CTA order by the last CTA.
+template <typename T>
+struct CgcgVecs {
+    const T *dinv;
+    T *x, *p;
+    T *r[2], *w[2], *s[2];
+    T *slice3;   // [3 * n_slices]: gamma, delta, r.r partials of each slice
+};
+
+// u_(i+1) of one entry from r_i, w_i, s_(i-1), D^-1 (also returns r_(i+1)).
+template <typename T>
+__device__ __forceinline__ T cgcg_next_u(T r, T w, T sp, T d, T al, T bt, T &rn)
+{
+    const T sn = fma(bt, sp, w);
+    rn = fma(-al, sn, r);
+    return d * rn;
+}
+
+// Sums of three values per thread over the CTA (warp levels in T, per-warp in
+// FP64), valid in thread 0.
+template <typename T>
+__device__ __forceinline__ void block_sum3_v(T a, T b, T c, double *sh, double &ra, double &rb, double &rc)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    constexpr int NW = kVecThreads >> 5;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        sh[w] = (double)a;
+        sh[NW + w] = (double)b;
+        sh[2 * NW + w] = (double)c;
+    }
+    __syncthreads();
+    double x = 0.0, y = 0.0, z = 0.0;
+    if (w == 0) {
+        x = l < NW ? sh[l] : 0.0;
+        y = l < NW ? sh[NW + l] : 0.0;
+        z = l < NW ? sh[2 * NW + l] : 0.0;
+#pragma unroll
+        for (int o = NW >> 1; o > 0; o >>= 1) {
+            x += __shfl_xor_sync(0xffffffffu, x, o);
+            y += __shfl_xor_sync(0xffffffffu, y, o);
+            z += __shfl_xor_sync(0xffffffffu, z, o);
+        }
+    }
+    __syncthreads();
+    ra = x;
+    rb = y;
+    rc = z;
+}
+
+// One Chronopoulos-Gear iteration (START = false), or the start of a run:
+// w = A u for the residual in r[pcur] with p and s[pcur^1] multiplied by
+// ctl->pq (the previous run's residual scale over the new one; 0 = fresh start,
+// which zeroes them), no update of x or r; its last CTA sets alpha and beta from
+// the kept gamma (rescaled by the host) and alpha for a resumed run, or
+// alpha = gamma / delta for a fresh one.
+template <int S, typename T, int HINT = kMatrixHint, bool START = false>
+__global__ void __launch_bounds__(kVecThreads, 2) k_sell_cgcg(SellView<T> A, CgcgVecs<T> v, double *part, PcgCtl *ctl)
+{
+    constexpr bool start = START;
+    __shared__ double sh[3 * (kVecThreads >> 5)];
+    __shared__ int flag;
+    __shared__ uint32_t next_sl;
+    if (A.prefetch_bytes && threadIdx.x == 0) {
+        // the matrix does not change during a solve: stream the head of this CTA's
+        // slot range into L2 while the predecessor finishes (as k_sell_dir)
+        const uint32_t sb = __ldg(A.cta_first + blockIdx.x), se = __ldg(A.cta_first + blockIdx.x + 1);
+        const uint64_t g0 = __ldg(A.slice_ptr + sb), g1 = __ldg(A.slice_ptr + se);
+        const uint64_t vfull = (g1 - g0) * (S * S * sizeof(T)), cfull = (g1 - g0) * 4;
+        const uint64_t vcap = A.prefetch_bytes, ccap = A.prefetch_bytes / (S * S);
+        const uint64_t vb = (vfull < vcap ? vfull : vcap) & ~uint64_t(15);
+        const uint64_t cbytes = (cfull < ccap ? cfull : ccap) & ~uint64_t(15);
+        if (vb) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(A.val + g0 * (S * S)), "r"((uint32_t)vb) : "memory");
+        if (cbytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(A.col + g0), "r"((uint32_t)cbytes) : "memory");
+    }
+    pdl_wait();
+    pdl_release();
+    if (!start && ctl->done) return;
+    constexpr int U = kSpmvUnroll;
+    constexpr uint32_t WPB = kVecThreads / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    const int cur = ctl->pcur;
+    const T al = start ? T(0) : (T)ctl->alpha;
+    const T bt = start ? T(0) : (T)ctl->beta;
+    const double scale = start ? ctl->pq : 1.0;
+    // buffers by parity, selected without indexing (no local copy of the parameter block)
+    T *const r0 = cur ? v.r[1] : v.r[0], *const r1 = cur ? v.r[0] : v.r[1];
+    T *const w0 = cur ? v.w[1] : v.w[0], *const w1 = cur ? v.w[0] : v.w[1];
+    T *const s0 = cur ? v.s[1] : v.s[0], *const s1 = cur ? v.s[0] : v.s[1];
+    const T *__restrict__ rc = r0;
+    const T *__restrict__ wc = w0;
+    T *__restrict__ sp = s1;
+    const T *__restrict__ d = v.dinv;
+    T *__restrict__ rn_out = r1;
+    T *__restrict__ w_out = start ? w0 : w1;
+    T *__restrict__ s_out = s0;
+    const uint32_t s_beg = __ldg(A.cta_first + blockIdx.x), s_end = __ldg(A.cta_first + blockIdx.x + 1);
+    const uint64_t pol = stream_policy<HINT>();
+    if (threadIdx.x == 0) next_sl = s_beg + WPB;
+    __syncthreads();
+    for (uint32_t sl = s_beg + (threadIdx.x >> 5); sl < s_end;) {
+        const uint32_t row = __ldg(A.perm + (uint64_t)sl * 32 + lane);
+        const uint64_t g0 = __ldg(A.slice_ptr + sl);
+        const uint32_t len = (uint32_t)((__ldg(A.slice_ptr + sl + 1) - g0) >> 5);
+        T acc[S];
+#pragma unroll
+        for (int r = 0; r < S; r++) acc[r] = T(0);
+        uint32_t c[U];
+        T blk[U][S * S];
+        for (uint32_t j0 = 0; j0 < len; j0 += U) {
+            load_sell_group<S, U, T, HINT>(A, g0, j0, len, lane, c, blk, pol);
+            T rv[U][S], wv[U][S], sv[U][S], dv[U][S];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+                    load_x<S, T>(rc, c[u], rv[u]);
+                    load_x<S, T>(d, c[u], dv[u]);
+                    if (!start) {
+                        load_x<S, T>(wc, c[u], wv[u]);
+                        load_x<S, T>(sp, c[u], sv[u]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+#pragma unroll
+                    for (int cc = 0; cc < S; cc++) {
+                        T rn;
+                        const T un = start ? dv[u][cc] * rv[u][cc]
+                                           : cgcg_next_u<T>(rv[u][cc], wv[u][cc], sv[u][cc], dv[u][cc], al, bt, rn);
+#pragma unroll
+                        for (int r = 0; r < S; r++) acc[r] = fma(blk[u][r * S + cc], un, acc[r]);
+                    }
+                }
+            }
+        }
+        T g = T(0), dl = T(0), rr = T(0);
+        if (row < A.n_rows) {
+#pragma unroll
+            for (int r = 0; r < S; r++) {
+                const uint64_t i = (uint64_t)row * S + r;
+                const T ri = rc[i], di = d[i];
+                T un, rnext;
+                if (start) {   // the kept direction in the new residual's scale (zero for a fresh start)
+                    rnext = ri;
+                    un = di * ri;
+                    v.p[i] = scale != 0.0 ? (T)(scale * (double)v.p[i]) : T(0);
+                    sp[i] = scale != 0.0 ? (T)(scale * (double)sp[i]) : T(0);
+                } else {
+                    const T wi = wc[i], spi = sp[i];
+                    un = cgcg_next_u<T>(ri, wi, spi, di, al, bt, rnext);
+                    const T pn = fma(bt, v.p[i], di * ri);
+                    v.p[i] = pn;
+                    s_out[i] = fma(bt, spi, wi);
+                    v.x[i] = fma(al, pn, v.x[i]);
+                    rn_out[i] = rnext;
+                }
+                w_out[i] = acc[r];
+                g = fma(rnext, un, g);
+                dl = fma(acc[r], un, dl);
+                rr = fma(rnext, rnext, rr);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            g += __shfl_xor_sync(0xffffffffu, g, o);
+            dl += __shfl_xor_sync(0xffffffffu, dl, o);
+            rr += __shfl_xor_sync(0xffffffffu, rr, o);
+        }
+        if (lane == 0) {
+            v.slice3[3 * (uint64_t)sl] = g;
+            v.slice3[3 * (uint64_t)sl + 1] = dl;
+            v.slice3[3 * (uint64_t)sl + 2] = rr;
+        }
+        uint32_t nx = 0;
+        if (lane == 0) nx = atomicAdd(&next_sl, 1u);
+        sl = __shfl_sync(0xffffffffu, nx, 0);
+    }
+    __syncthreads();   // the CTA's slice partials are visible to all its threads
+    T g = T(0), dl = T(0), rr = T(0);
+    for (uint32_t i = s_beg + threadIdx.x; i < s_end; i += kVecThreads) {
+        g += v.slice3[3 * (uint64_t)i];
+        dl += v.slice3[3 * (uint64_t)i + 1];
+        rr += v.slice3[3 * (uint64_t)i + 2];
+    }
+    double bg, bd, br;
+    block_sum3_v<T>(g, dl, rr, sh, bg, bd, br);
+    const uint32_t nb = gridDim.x;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = bg;
+        part[nb + blockIdx.x] = bd;
+        part[2 * nb + blockIdx.x] = br;
+    }
+    if (!last_cta(&ctl->ticket, &flag, nb)) return;
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (uint32_t i = threadIdx.x; i < nb; i += kVecThreads) {
+        a += __ldcg(part + i);
+        b += __ldcg(part + nb + i);
+        c += __ldcg(part + 2 * nb + i);
+    }
+    block_sum3_v<double>(a, b, c, sh, bg, bd, br);
+    if (threadIdx.x == 0) {
+        const double gamma_old = ctl->rz, alpha_old = ctl->alpha;
+        ctl->rr = br;
+        ctl->pq = bd;
+        if (start) {
+            // a kept direction continues (gamma_old rescaled by the host), else alpha = gamma / delta
+            const double beta = (scale != 0.0 && gamma_old != 0.0) ? bg / gamma_old : 0.0;
+            const double den = beta != 0.0 && alpha_old != 0.0 ? bd - beta * bg / alpha_old : bd;
+            ctl->beta = beta;
+            ctl->alpha = den != 0.0 ? bg / den : 0.0;
+            ctl->iterations = 0;
+            ctl->done = (br <= ctl->tol2 || !(br == br)) ? 1 : 0;
+        } else {
+            const int64_t it = ctl->iterations + 1;
+            ctl->iterations = it;
+            const bool stop = br <= ctl->tol2 || it >= ctl->maxit || !(br == br);
+            if (stop) {
+                ctl->done = 1;
+            } else {
+                const double beta = gamma_old != 0.0 ? bg / gamma_old : 0.0;
+                const double den = alpha_old != 0.0 ? bd - beta * bg / alpha_old : bd;
+                ctl->beta = beta;
+                ctl->alpha = den != 0.0 ? bg / den : 0.0;
+            }
+            ctl->pcur = cur ^ 1;
+        }
+        ctl->rz_prev = gamma_old;
+        ctl->rz = bg;
+        ctl->ticket = 0;
+    }
 }
 
 }  // namespace amie
