@@ -77,7 +77,8 @@ def parse_args():
     ap.add_argument("--launch-list", action="store_true", help="run exactly one step without warm-up (for an ncu "
                                                                "launch list), print its timing, exit")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")
-    ap.add_argument("--damage-steps", type=int, default=60, help="config-3 damage-loop load steps (0 = skip)")
+    ap.add_argument("--damage-steps", type=int, default=30, help="config-3 damage-loop load steps of 1 um "
+                                                                 "deflection each (0 = skip)")
     return ap.parse_args()
 
 
@@ -115,10 +116,28 @@ def fold_dir() -> bool:
     return os.environ.get("AMIE_FOLD_DIR", "1") != "0"
 
 
-def spmv_bytes(nnzb: int, n_rows: int, s: int, w: int, fold: bool = False) -> int:
+def cgcg_on() -> bool:
+    """Whether the mixed solver's FP32 runs are single-reduction PCG, one kernel per
+    iteration (opt-in, AMIE_CGCG=1; the default is the two-kernel standard PCG)."""
+    return os.environ.get("AMIE_CGCG", "0") not in ("", "0")
+
+
+def spmv_bytes(nnzb: int, n_rows: int, s: int, w: int, fold: bool = False, cgcg: bool = False) -> int:
     """Algorithmic bytes of one block SpMV: blocks + column indices + row pointers + x read + y write;
-    with the direction update folded in, z and p_old are read and q and p_new written (4 vectors)."""
-    return nnzb * (s * s * w + 4) + 4 * (n_rows + 1) + (4 if fold else 2) * n_rows * s * w
+    with the direction update folded in, z and p_old are read and q and p_new written (4 vectors);
+    one single-reduction PCG iteration reads r, w, s_old, D^-1, p, x and writes p, s, x, r_new,
+    w_new (11 vectors)."""
+    vecs = 11 if cgcg else (4 if fold else 2)
+    return nnzb * (s * s * w + 4) + 4 * (n_rows + 1) + vecs * n_rows * s * w
+
+
+def spmv_kernel_key(w: int):
+    """(kernel name, traffic key suffix, cgcg, fold) of the dominant kernel of a solve in w-byte floats."""
+    if w == 4 and cgcg_on():
+        return "k_sell_cgcg", "sell_cgcg", True, False
+    if w == 4 and fold_dir():
+        return "k_sell_dir", "sell_dir", False, True
+    return "k_sell_pq", "sell_pq", False, False
 
 
 def assembly_bytes(m: am.MeshData, topo) -> dict:
@@ -359,8 +378,9 @@ def run_ours(args, world, rank, local, dist):
         ms32 = topo.profile_spmv(32, args.reps)
         ms64 = topo.profile_spmv(64, args.reps)
         print(json.dumps({"profile": name, "n_dof": int(n), "nnzb": int(topo.nnzb), "reps": args.reps, "ms_spmv32": ms32,
-                          "ms_spmv64": ms64, "fold_dir": fold_dir(),
-                          "alg_bytes32": spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 4, fold_dir()),
+                          "ms_spmv64": ms64, "kernel32": spmv_kernel_key(4)[0],
+                          "alg_bytes32": spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 4, fold=spmv_kernel_key(4)[3],
+                                                    cgcg=spmv_kernel_key(4)[2]),
                           "alg_bytes64": spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 8)}))
         topo.close()
         ctx.close()
@@ -421,11 +441,12 @@ def run_ours(args, world, rank, local, dist):
     ms_spmv = topo.profile_spmv(prec, 50)
     ms_spmv64 = topo.profile_spmv(64, 50)
     peak, peak_kind = load_peaks()
-    alg = spmv_bytes(topo.nnzb, topo.n_rows, m.stride, w, fold_dir() and w == 4)
+    kname, kkey, kcg, kfold = spmv_kernel_key(w)
+    alg = spmv_bytes(topo.nnzb, topo.n_rows, m.stride, w, kfold, kcg)
     alg64 = spmv_bytes(topo.nnzb, topo.n_rows, m.stride, 8)
     achieved = alg / (ms_spmv / 1e3) / 1e9
     achieved64 = alg64 / (ms_spmv64 / 1e3) / 1e9
-    traffic = load_traffic(f"{args.config}_{'sell_dir' if fold_dir() and w == 4 else 'sell_pq'}{prec}")
+    traffic = load_traffic(f"{args.config}_{kkey}{prec}")
     # what one plain streaming read of the same byte count reaches in one launch on this GPU
     ms_stream = ctx.profile_stream(alg, 10)
 
@@ -452,7 +473,7 @@ def run_ours(args, world, rank, local, dist):
                               "frac": asm_alg["total"] / (ms_asm / 1e3) / 1e9 / peak,
                               "timed": "quadrature + gather + Dirichlet elimination + FP32/FP64 solver copies"},
         "roofline": {"bound": "hbm",
-                     "kernel": f"{'k_sell_dir' if fold_dir() and w == 4 else 'k_sell_pq'}<{m.stride},{'float' if w == 4 else 'double'}>",
+                     "kernel": f"{kname}<{m.stride},{'float' if w == 4 else 'double'}>",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "alg_bytes_per_launch": alg,
                      "ms_per_launch": ms_spmv,
@@ -488,7 +509,7 @@ def run_ours(args, world, rank, local, dist):
         result["serving"] = run_serving(ctx, args.serve, args.serve_rate, solver, iters=args.serve_iters)
     # damage loop (config 3)
     if args.damage_steps > 0:
-        result["damage_loop"] = run_damage_loop(ctx, solver, args.damage_steps)
+        result["damage_loop"] = run_damage_loop(ctx, solver, args.damage_steps, 1e-6 * args.damage_steps)
 
     # CPU baseline: the oracle port on this machine's host cores, bounded sample, rank 0 at N = 1
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -507,30 +528,51 @@ def run_ours(args, world, rank, local, dist):
     return 0
 
 
-def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, pool: int = 32, iters: int = 0):
-    """Config-4 serving mix: Poisson arrivals of independent homogenisation solves
-    (log-uniform 2k-200k DOF, inclusion fraction U[0.2, 0.6]) into the
-    continuous-batching server.  Returns p50/p99 latency and solves/s."""
+def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, iters: int = 0, workers: int = 8):
+    """Config-4 serving mix: Poisson arrivals of independent homogenisation solves,
+    each with its own seeded microstructure (log-uniform 2k-200k DOF, inclusion
+    fraction U[0.2, 0.6]), into the continuous-batching server.  The meshes are
+    generated ahead of their arrival by `workers` spawned processes (a window of
+    256 requests); a request is submitted at its arrival time, or as soon as its
+    mesh is ready if that is later (counted in late_submissions).  Returns
+    p50/p99 latency (submit to result) and solves/s."""
+    import multiprocessing as mp
+    from collections import deque
+    from concurrent.futures import ProcessPoolExecutor
     import amie_gpu as G
-    meshes, arrivals, which = W.serving_mix(n_requests, rate, seed=seed, pool=pool)
-    srv = G.Server(ctx, solver=solver, rtol=1e-10, iters_per_launch=iters)
-    # warm the server (graph, first allocations) with one request
-    t = srv.submit(meshes[0][0], *meshes[0][1])
-    srv.drain(60.0)
-    srv.poll(t, want_x=False)
-    tickets = []
-    t0 = time.perf_counter()
-    for k in range(n_requests):
-        delay = arrivals[k] - (time.perf_counter() - t0)
-        if delay > 0:
-            time.sleep(delay)
-        m, bcs, _ = meshes[which[k]]
-        tickets.append(srv.submit(m, *bcs))
-    srv.drain(600.0)
-    wall = time.perf_counter() - t0
+    specs, arrivals = W.serving_mix(n_requests, rate, seed=seed)
+    window = 256
+    with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as pool:
+        futs = deque(pool.submit(W.serving_request, sp) for sp in specs[:window])
+        nxt = len(futs)
+        srv = G.Server(ctx, solver=solver, rtol=1e-10, iters_per_launch=iters)
+        # warm the server (graph, first allocations) with one request outside the stream
+        wm, wb = W.serving_request((20000, 0.4, seed - 1))
+        t = srv.submit(wm, *wb)
+        srv.drain(60.0)
+        srv.poll(t, want_x=False)
+        for f in list(futs)[:64]:   # the pool is running before the clock starts
+            f.result()
+        tickets, late, late_max = [], 0, 0.0
+        t0 = time.perf_counter()
+        for k in range(n_requests):
+            m, bcs = futs.popleft().result()
+            if nxt < n_requests:
+                futs.append(pool.submit(W.serving_request, specs[nxt]))
+                nxt += 1
+            delay = arrivals[k] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            elif delay < -0.005:
+                late += 1
+                late_max = max(late_max, -delay)
+            tickets.append(srv.submit(m, *bcs))
+            del m, bcs
+        srv.drain(600.0)
+        wall = time.perf_counter() - t0
     loop_stats = srv.stats()
-    lat, statuses, dofs, iters = [], [], [], []
-    for k, tk in enumerate(tickets):
+    lat, statuses, dofs, iters_done = [], [], [], []
+    for tk in tickets:
         r = srv.poll(tk, want_x=False)
         if r is None:
             continue
@@ -538,32 +580,37 @@ def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, p
         lat.append(res["latency_s"])
         statuses.append(res["status"])
         dofs.append(res["n"])
-        iters.append(res["iterations"])
+        iters_done.append(res["iterations"])
     srv.stop()
     lat = np.array(lat)
     ok = int(sum(1 for s in statuses if s == G.AMIE_OK))
     return {"requests": n_requests, "completed_ok": ok, "rate_req_s": rate, "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "solves_per_s": ok / wall, "wall_s": wall,
-            "mean_dof": float(np.mean(dofs)) if dofs else 0.0, "mean_iterations": float(np.mean(iters)) if iters else 0.0,
-            "distinct_microstructures": pool,
+            "mean_dof": float(np.mean(dofs)) if dofs else 0.0,
+            "mean_iterations": float(np.mean(iters_done)) if iters_done else 0.0,
+            "dof_iterations_per_s": float(np.sum(np.array(dofs, float) * np.array(iters_done, float)) / wall),
+            "distinct_microstructures": n_requests, "late_submissions": late, "late_max_s": late_max,
             "solver": "mixed" if solver == G.SOLVER_PCG_MIXED else "fp64",
             "host_loop_s": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in loop_stats.items()}}
 
 
-def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 2e-4, max_passes: int = 2000):
+def run_damage_loop(ctx, solver: int, steps: int = 30, deflection_max: float = 30e-6, max_passes: int = 400,
+                    radius: float = 0.005):
     """Config-3 loop: notched beam in three-point bending (400 x 100 mm, 20 x 2 mm
     notch, P1, ~250k DOF, E 35 GPa, 20 mm loading plate) with the reference's
     StiffnessAndFracture damage: NonLocalMazars (threshold 1e-4, Gf 100 N/m,
-    material radius 2 mm) graded on the device and FiberBasedIsotropicLinearDamage
+    material radius 5 mm) graded on the device and FiberBasedIsotropicLinearDamage
     (0.1 per event, fractured at 0.6).  Each load step raises the plate's
-    deflection and runs FeatureTree::stepInternal's passes on the device
-    (damaged stiffness, elimination, warm-started solve, grading, update) until
-    no element changes.  Reports where the damage lies relative to the notch."""
+    deflection by deflection_max / steps (1 um) and runs FeatureTree::stepInternal's
+    passes on the device (damaged stiffness, elimination, warm-started solve,
+    grading, update) until no element changes, at most max_passes per step.  The
+    beam stays elastic up to about 27 um; damage then starts at the notch tip and
+    grows upwards as a band.  Reports where the damage lies relative to the notch."""
     import amie_gpu as G
     m, bcs_at, meta = W.notched_beam()
     topo = G.Topology(ctx, m)
     topo.assemble()
-    law = G.DamageLaw(G.DAMAGE_FIBER_ISOTROPIC, 1e-4, 35e9, 0.2, 100.0, 0.002, 2e-3, 0.1, 0.6, 1e-4)
+    law = G.DamageLaw(G.DAMAGE_FIBER_ISOTROPIC, 1e-4, 35e9, 0.2, 100.0, radius, 2e-3, 0.1, 0.6, 1e-4)
     t_setup = time.perf_counter()
     topo.damage_setup(law, meta["corners"])
     setup_s = time.perf_counter() - t_setup
@@ -590,7 +637,9 @@ def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 2
            "first_damaged_step": first, "damaged_elements": int(hit.sum()),
            "fractured_elements": int((dmg >= 0.6).sum()), "max_damage": float(dmg.max()),
            "passes_per_step": [p[0] for p in per_step], "damaged_per_step": [p[1] for p in per_step],
-           "law": "NonLocalMazars(1e-4, 35e9, 0.2, 100, 0.002) + FiberBasedIsotropicLinearDamage(0.1, 0.6)"}
+           "max_passes_per_step": max_passes,
+           "steps_at_pass_cap": int(sum(1 for p in per_step if p[0] >= max_passes)),
+           "law": f"NonLocalMazars(1e-4, 35e9, 0.2, 100, {radius}) + FiberBasedIsotropicLinearDamage(0.1, 0.6)"}
     if hit.any():
         out["damaged_x_range_mm"] = [float(1e3 * (cen[hit, 0].min() - tip[0])), float(1e3 * (cen[hit, 0].max() - tip[0]))]
         out["damaged_y_range_mm"] = [float(1e3 * cen[hit, 1].min()), float(1e3 * cen[hit, 1].max())]

@@ -243,6 +243,10 @@ typedef struct amie_server_config {
     uint64_t hbm_budget_bytes;   /* admission limit; 0 = 90% of free memory */
     int32_t max_slots;           /* concurrent solves; 0 = 256 */
     int32_t iters_per_launch;    /* PCG iterations per graph launch; 0 = 16 */
+    uint32_t barrier_polls;      /* persistent batches (AMIE_SERVER_PERSISTENT=1): polls of a slot barrier
+                                    before it gives up, ~64 ns each; 0 = 4,194,304 (~0.3 s).  A barrier that
+                                    gives up ends the launch; the batch's requests end with AMIE_TIMEOUT and
+                                    the server goes on serving. */
 } amie_server_config;
 
 typedef struct amie_request {

@@ -71,3 +71,28 @@ def test_folded_direction_is_bitwise_identical(gpu_ctx, monkeypatch, name):
     (x1, s1), (x0, s0) = out
     assert s1["iterations"] == s0["iterations"]
     assert np.array_equal(x1, x0)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_single_reduction_pcg_solves(gpu_ctx, monkeypatch, name):
+    """The opt-in single-reduction (Chronopoulos-Gear) FP32 runs of the mixed
+    solver (AMIE_CGCG=1, one kernel per iteration, reliable updates with the
+    direction kept) reach the oracle's solution, and repeat bit for bit."""
+    import amie_gpu
+    monkeypatch.setenv("AMIE_CGCG", "1")
+    d = load_golden(name)
+    m = am.from_golden(d, "tabulated")
+    t = amie_gpu.Topology(gpu_ctx, m)
+    try:
+        t.assemble()
+        t.apply_dirichlet(*am.golden_bcs(d))
+        x1, st1 = t.solve(amie_gpu.SOLVER_PCG_MIXED, rtol=1e-10)
+        x2, st2 = t.solve(amie_gpu.SOLVER_PCG_MIXED, rtol=1e-10)
+        assert st1["relres"] <= 1e-10 and relres(d, m, x1) <= 2e-10
+        assert st1["refinements"] >= 2   # at least one resumed run
+        assert np.array_equal(x1, x2) and st1["iterations"] == st2["iterations"]
+        xo, _, _, _ = O.pcg(m.stride, d["row_size"], d["column_index"], d["array"], d["rhs"], rtol=1e-13)
+        s = node_dofs(m)
+        assert np.abs(x1[s] - xo[s]).max() <= 1e-8 * np.abs(xo[s]).max()
+    finally:
+        t.close()

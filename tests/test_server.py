@@ -118,3 +118,34 @@ def test_failure_statuses(gpu_ctx):
     assert res[tc][0]["status"] in (G.AMIE_CANCELLED, G.AMIE_OK)
     assert all(res[t][0]["status"] == G.AMIE_OK for t in big)
     srv.stop()
+
+
+def test_persistent_barrier_gives_up_and_server_recovers(gpu_ctx, monkeypatch):
+    """A persistent batch whose slot barrier cannot be reached ends by itself:
+    the host claims one CTA more for the first request's slot than it launches
+    (AMIE_SERVER_SHORT_SLOT=1, a host-side fault), the slot barrier gives up after
+    barrier_polls polls (~1 ms here), that request ends with AMIE_TIMEOUT, and
+    the next request on the same server solves to 1e-10 and matches a direct solve."""
+    import amie_gpu as G
+    monkeypatch.setenv("AMIE_SERVER_PERSISTENT", "1")
+    monkeypatch.setenv("AMIE_SERVER_ROWS_PER_CTA", "64")   # several CTAs per slot, one of them left out
+    monkeypatch.setenv("AMIE_SERVER_SHORT_SLOT", "1")
+    m, bcs, _ = _requests()[0]
+    srv = G.Server(gpu_ctx, solver=G.SOLVER_PCG_MIXED, rtol=1e-10, barrier_polls=1 << 14)
+    try:
+        t1 = srv.submit(m, *bcs)
+        r1 = _wait(srv, [t1], timeout=60)
+        assert t1 in r1 and r1[t1][0]["status"] == G.AMIE_TIMEOUT, r1
+        t2 = srv.submit(m, *bcs)
+        r2 = _wait(srv, [t2], timeout=60)
+        assert t2 in r2
+        res, x = r2[t2]
+        assert res["status"] == G.AMIE_OK and res["relres"] <= 1e-10, res
+    finally:
+        srv.stop()
+    topo = G.Topology(gpu_ctx, m)
+    topo.assemble()
+    topo.apply_dirichlet(*bcs)
+    x_ref, _ = topo.solve(G.SOLVER_PCG_FP64, rtol=1e-12)
+    topo.close()
+    assert rel(x, x_ref) <= 1e-8

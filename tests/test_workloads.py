@@ -56,6 +56,28 @@ def test_homogenisation_request_sizes():
         m, bcs, meta = W.homogenisation_request(dof, 0.4, seed=1)
         assert 0.8 * dof < meta["n_dof"] < 1.25 * dof
         assert 0.3 < meta["fraction"] < 0.5
-    meshes, arrivals, which = W.serving_mix(64, 200.0, pool=4)
-    assert len(meshes) == 4 and len(arrivals) == 64
+    specs, arrivals = W.serving_mix(64, 200.0)
+    assert len(specs) == 64 and len(arrivals) == 64
+    assert len({sp[2] for sp in specs}) == 64   # every request its own microstructure
+    assert all(2000 <= sp[0] <= 200000 and 0.2 <= sp[1] <= 0.6 for sp in specs)
     assert 0.15 < arrivals[-1] < 0.6      # 64 Poisson arrivals at 200/s
+    m, (ids, vals, kinds) = W.serving_request(specs[0])
+    m.validate()
+    assert len(ids) == len(vals) == len(kinds)
+
+
+def test_fast_inclusion_helpers_match_the_plain_ones():
+    import numpy as np
+    rng = np.random.default_rng(3)
+    x, y, conn, vx, vy, M = W.structured_triangles(60, 0.04, 1, 0.15, rng)
+    cx, cy, cr = W.place_inclusions(np.random.default_rng(5), np.random.default_rng(6).uniform(0.3e-3, 1.5e-3, 120),
+                                    0.04)
+    gx, gy = vx.mean(1), vy.mean(1)
+    h = 0.04 / 60
+    assert np.array_equal(W._in_inclusions(gx, gy, cx, cy, cr, h, 60), W._in_circles_structured(gx, gy, 60, h, cx, cy, cr))
+    J1, _ = W._tri_jinv(vx, vy)
+    assert np.abs(J1 - W._jinv_closed(vx, vy)).max() <= 1e-14 * np.abs(J1).max()
+    cx2, cy2, cr2 = W._place_inclusions_batched(np.random.default_rng(9), np.full(150, 1e-3), 0.04)
+    d2 = (cx2[:, None] - cx2[None]) ** 2 + (cy2[:, None] - cy2[None]) ** 2
+    np.fill_diagonal(d2, np.inf)
+    assert (d2 > (2e-3) ** 2).all()   # no overlaps

@@ -108,7 +108,7 @@ class SolveStats(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("solver", C.c_int32), ("rtol", C.c_double), ("hbm_budget_bytes", C.c_uint64),
-                ("max_slots", C.c_int32), ("iters_per_launch", C.c_int32)]
+                ("max_slots", C.c_int32), ("iters_per_launch", C.c_int32), ("barrier_polls", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -395,10 +395,10 @@ class Server:
     """Continuous-batching solve server (amie_server_* of the C-ABI)."""
 
     def __init__(self, ctx: Context, solver=SOLVER_PCG_MIXED, rtol=1e-10, hbm_budget_bytes=0, max_slots=0,
-                 iters_per_launch=0):
+                 iters_per_launch=0, barrier_polls=0):
         self.ctx = ctx
         self.ptr = C.c_void_p()
-        cfg = ServerConfig(solver, rtol, hbm_budget_bytes, max_slots, iters_per_launch)
+        cfg = ServerConfig(solver, rtol, hbm_budget_bytes, max_slots, iters_per_launch, barrier_polls)
         check(lib().amie_server_start(ctx.ptr, C.byref(cfg), C.byref(self.ptr)), "amie_server_start")
         self._keep = {}
         self._n = {}

@@ -10,9 +10,12 @@
 // covering all slots through a CTA -> slot map (CTAs split between slots in
 // proportion to their size, so each slot's reductions are its own CTAs'
 // partials: deterministic, and the same alone and in a mix).  A slot whose
-// inner solve has converged stops doing work inside the graph; between graph
-// launches the host refines it in FP64 (mixed precision) or retires it.
-// There is no device-side waiting anywhere: the host decides between launches.
+// inner run has stopped does no more work in the batch; the kernels that end
+// each batch replace its residual in FP64 and decide, on the device, whether
+// the solve is finished, resumes its FP32 run or restarts it.  Between batch
+// launches the host only retires finished solves and joins admitted ones.
+// The batch graph has no device-side waiting (the opt-in persistent batch has
+// bounded slot barriers).
 #pragma once
 
 #include <condition_variable>
@@ -24,7 +27,25 @@
 namespace amie {
 
 constexpr int kBatchIters = 16;
-constexpr int kNormParts = 256;   // most CTAs of a slot's residual-norm launch
+
+// State of a slot's whole solve, kept on the device: the host writes it when
+// the request joins; afterwards only the last CTA of the slot in the refinement
+// kernels (kb_residual, kb_restart) changes it.
+struct SlotRun {
+    double bnorm;         // |b|
+    double target;        // rtol |b|
+    double rnorm;         // |b - A x| at the latest residual replacement (the inner run's scale)
+    double ratio;         // kRunResume: new / previous residual norm
+    int64_t iterations;   // inner iterations of all runs so far
+    int64_t maxit;        // cap on them
+    int32_t refinements;  // residual replacements (mixed)
+    int32_t status;       // AMIE_NOT_READY while the solve runs, then its result
+    int32_t mode;         // kRunIterating, or what kb_restart does next
+    int32_t pad_;
+};
+constexpr int32_t kRunIterating = 0;   // the inner run iterates (or stopped and awaits kb_residual)
+constexpr int32_t kRunResume = 1;      // continue the inner run from the replaced residual, direction kept
+constexpr int32_t kRunRestart = 2;     // start a fresh inner run from the replaced residual
 
 // Device view of one slot: the slot's SELL copies (CTA table for its own CTA
 // count), vectors, control block and its range of the batch's partial sums.
@@ -32,9 +53,11 @@ struct SlotDesc {
     SellView<float> A32;
     SellView<double> A64;
     PcgVecs<float> v32;      // inner vectors of the mixed solve (two direction buffers)
-    PcgVecs<double> v64;     // FP64 vectors (one direction buffer)
+    PcgVecs<double> v64;     // FP64 vectors (one direction buffer); v64.A is the FP64 block-CSR matrix
     PcgParts parts;          // the batch partials of CTAs c0 .. c1-1
     PcgCtl *ctl;             // the slot's control block
+    SlotRun *run;            // the slot's solve state
+    const double *rhs;       // b (after the Dirichlet elimination)
     uint64_t n;
     int32_t c0, c1;          // CTA range in the batch grid
     int32_t active;          // 1 = iterate
@@ -257,11 +280,13 @@ __global__ void __launch_bounds__(kVecThreads) kb_direction(const SlotDesc *slot
 // Persistent batch (mixed solver): one cooperative launch runs `iters` PCG
 // iterations of every active slot; the CTAs of a slot meet at a slot barrier
 // after each phase instead of at kernel boundaries.  Every wait is bounded:
-// a barrier that is not reached within kBarrierPolls polls sets *err, and a CTA
-// that sees *err set returns, so the launch always ends.
+// a barrier that is not reached within `polls` polls (the server's
+// barrier_polls, default kBarrierPolls) sets *err, and a CTA that sees *err
+// set returns, so the launch always ends.
 constexpr uint32_t kBarrierPolls = 1u << 22;   // ~0.3 s at 64 ns per poll
 
-__device__ __forceinline__ bool slot_barrier(uint32_t *count, uint32_t target, int32_t *err, int *sh_ok)
+__device__ __forceinline__ bool slot_barrier(uint32_t *count, uint32_t target, int32_t *err, int *sh_ok,
+                                             uint32_t max_polls)
 {
     __syncthreads();   // the CTA's work of the phase is done
     if (threadIdx.x == 0) {
@@ -274,7 +299,7 @@ __device__ __forceinline__ bool slot_barrier(uint32_t *count, uint32_t target, i
                 ok = 0;
                 break;
             }
-            if (polls >= kBarrierPolls) {
+            if (polls >= max_polls) {
                 atomicExch(err, 1);
                 ok = 0;
                 break;
@@ -290,7 +315,7 @@ __device__ __forceinline__ bool slot_barrier(uint32_t *count, uint32_t target, i
 
 template <typename T>
 __global__ void __launch_bounds__(kVecThreads) kb_persistent(const SlotDesc *slots, const int16_t *cta_slot, int iters,
-                                                             uint32_t *bar, int32_t *err)
+                                                             uint32_t *bar, int32_t *err, uint32_t polls)
 {
     __shared__ double sh[2 * (kVecThreads >> 5)];
     __shared__ int flag, ok;
@@ -306,10 +331,194 @@ __global__ void __launch_bounds__(kVecThreads) kb_persistent(const SlotDesc *slo
         if (ctl_ld<true>(&ctl->done)) break;
         sell_dir_body<2, T, true>(slot_A<T>(*d), slot_v<T>(*d), d->parts.pq, ctl, true, c);
         target += c.n;
-        if (!slot_barrier(bar + s, target, err, &ok)) return;
+        if (!slot_barrier(bar + s, target, err, &ok, polls)) return;
         update_body<T, true>(slot_v<T>(*d), d->n, d->parts, ctl, sh, &flag, c);
         target += c.n;
-        if (!slot_barrier(bar + s, target, err, &ok)) return;
+        if (!slot_barrier(bar + s, target, err, &ok, polls)) return;
+    }
+}
+
+// ------------------------------------------------------------------ device-side refinement
+// Appended to every batch: for each slot whose inner run stopped during the
+// batch, the FP64 residual replacement and the decision the single-solve
+// driver takes on the host (solve_pcg): retire (converged, NaN, iteration or
+// refinement cap), resume the FP32 run with its direction kept (the true
+// residual fell by at least half since the previous replacement), or restart
+// it.  The host only retires the slots whose SlotRun.status became final.
+
+// The slot of this CTA if its inner run stopped, its solve is open and its
+// run is in `mode`.
+__device__ __forceinline__ const SlotDesc *slot_stopped(const SlotDesc *slots, const int16_t *cta_slot, int32_t mode,
+                                                        Cta *c)
+{
+    const int s = cta_slot[blockIdx.x];
+    if (s < 0) return nullptr;
+    const SlotDesc *d = slots + s;
+    if (!d->active || !d->ctl->done || d->run->status != AMIE_NOT_READY || d->run->mode != mode) return nullptr;
+    *c = Cta{blockIdx.x - (uint32_t)d->c0, (uint32_t)(d->c1 - d->c0)};
+    return d;
+}
+
+// Mixed: x += rnorm * d (the FP32 run's increment, in the scale of its residual).
+__global__ void __launch_bounds__(kVecThreads) kb_accumulate(const SlotDesc *slots, const int16_t *cta_slot)
+{
+    Cta c;
+    const SlotDesc *d = slot_stopped(slots, cta_slot, kRunIterating, &c);
+    if (!d) return;
+    const double scale = d->run->rnorm;
+    const float *__restrict__ dx = d->v32.x;
+    double *__restrict__ x = d->v64.x;
+    for (uint64_t i = (uint64_t)c.id * kVecThreads + threadIdx.x; i < d->n; i += (uint64_t)c.n * kVecThreads)
+        x[i] += scale * (double)dx[i];
+}
+
+constexpr int kResidualGroup = 4;   // lanes per block row in kb_residual
+
+// r = b - A x in FP64 over the slot's CTAs, |r|^2 in CTA order; the slot's last
+// CTA counts the run's iterations and decides what follows.
+__global__ void __launch_bounds__(kVecThreads) kb_residual(const SlotDesc *slots, const int16_t *cta_slot)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    Cta c;
+    const SlotDesc *d = slot_stopped(slots, cta_slot, kRunIterating, &c);
+    if (!d) return;
+    constexpr int G = kResidualGroup;
+    constexpr int RPB = kVecThreads / G;
+    const BsrView<double> &A = d->v64.A;
+    const double *__restrict__ x = d->v64.x;
+    const double *__restrict__ b = d->rhs;
+    double *__restrict__ r = d->v64.r;
+    const int lane = threadIdx.x % G;
+    double dot = 0.0;
+    for (uint32_t base = c.id * RPB; base < A.n_rows; base += c.n * RPB) {
+        const uint32_t row = base + threadIdx.x / G;
+        const bool valid = row < A.n_rows;
+        const uint32_t rb = valid ? __ldg(A.row_ptr + row) : 0u, re = valid ? __ldg(A.row_ptr + row + 1) : 0u;
+        double acc[2];
+        row_spmv<2, G, double>(A, x, rb, re, lane, acc);
+        if (valid && lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const double y = b[(uint64_t)row * 2 + k] - acc[k];
+                r[(uint64_t)row * 2 + k] = y;
+                dot += y * y;
+            }
+        }
+    }
+    dot = block_sum(dot, sh);
+    if (threadIdx.x == 0) d->parts.spare[c.id] = dot;
+    PcgCtl *ctl = d->ctl;
+    if (!last_cta(&ctl->ticket, &flag, c.n)) return;
+    const double rr = ordered_sum(d->parts.spare, c.n, sh);
+    if (threadIdx.x == 0) {
+        SlotRun *run = d->run;
+        run->iterations += ctl->iterations;
+        if (d->mixed) run->refinements++;
+        const double prev = run->rnorm, rn = sqrt(rr);
+        run->rnorm = rn;
+        if (!(rr == rr)) {
+            run->status = AMIE_NAN;
+        } else if (rn <= run->target) {
+            run->status = AMIE_OK;
+        } else if (run->iterations >= run->maxit || run->refinements > 200) {
+            run->status = AMIE_NOT_CONVERGED;
+        } else if (d->mixed && rn <= 0.5 * prev) {
+            run->mode = kRunResume;
+            run->ratio = rn / prev;
+        } else {
+            run->mode = kRunRestart;
+        }
+        ctl->ticket = 0;
+    }
+}
+
+// The next inner run from the replaced residual.  Mixed: r32 = r / |r|, d = 0,
+// z = D^-1 r32 (p = z for a restart); FP64: z = D^-1 r, p = z.  Last CTA: the
+// control block of the new run (a resume keeps the direction through
+// beta = ratio r.z / r.z_prev, as resume_body).
+__global__ void __launch_bounds__(kVecThreads) kb_restart(const SlotDesc *slots, const int16_t *cta_slot,
+                                                          double inner_reduction, double last_target)
+{
+    __shared__ double sh[2 * (kVecThreads >> 5)];
+    __shared__ int flag;
+    const int s = cta_slot[blockIdx.x];
+    if (s < 0) return;
+    const SlotDesc *d = slots + s;
+    if (!d->active || d->run->status != AMIE_NOT_READY) return;
+    const int32_t mode = d->run->mode;
+    if (mode == kRunIterating) return;
+    const Cta c{blockIdx.x - (uint32_t)d->c0, (uint32_t)(d->c1 - d->c0)};
+    const SlotRun *run = d->run;
+    const uint64_t n = d->n;
+    const uint64_t i0 = (uint64_t)c.id * kVecThreads + threadIdx.x, step = (uint64_t)c.n * kVecThreads;
+    double brz, brr;
+    if (d->mixed) {
+        const PcgVecs<float> &v = d->v32;
+        const double *__restrict__ r64 = d->v64.r;
+        const double inv = 1.0 / run->rnorm;
+        float drz = 0.0f, drr = 0.0f;
+        for (uint64_t i = i0; i < n; i += step) {
+            const float ri = (float)(r64[i] * inv);
+            const float zi = ri * v.dinv[i];
+            v.r[i] = ri;
+            v.x[i] = 0.0f;
+            v.z[i] = zi;
+            if (mode == kRunRestart) v.p[i] = zi;
+            drz = fmaf(ri, zi, drz);
+            drr = fmaf(ri, ri, drr);
+        }
+        block_sum2_v<float>(drz, drr, sh, brz, brr);
+    } else {
+        const PcgVecs<double> &v = d->v64;
+        double drz = 0.0, drr = 0.0;
+        for (uint64_t i = i0; i < n; i += step) {
+            const double ri = v.r[i];
+            const double zi = ri * v.dinv[i];
+            v.z[i] = zi;
+            v.p[i] = zi;
+            drz = fma(ri, zi, drz);
+            drr = fma(ri, ri, drr);
+        }
+        block_sum2_v<double>(drz, drr, sh, brz, brr);
+    }
+    const PcgParts &parts = d->parts;
+    if (threadIdx.x == 0) {
+        parts.rz[c.id] = brz;
+        parts.rr[c.id] = brr;
+    }
+    PcgCtl *ctl = d->ctl;
+    if (!last_cta(&ctl->ticket, &flag, c.n)) return;
+    double rz, rr;
+    ordered_sum2(parts.rz, parts.rr, c.n, sh, rz, rr);
+    if (threadIdx.x == 0) {
+        SlotRun *w = d->run;
+        double tol2;
+        if (d->mixed) {
+            const double need = last_target * w->target / w->rnorm;
+            const double inner = fmin(0.5, fmax(inner_reduction, need));
+            tol2 = inner * inner;
+        } else {
+            tol2 = 0.25 * w->target * w->target;
+        }
+        const int64_t left = w->maxit - w->iterations;
+        if (mode == kRunResume) {
+            ctl->beta = ctl->rz_prev != 0.0 ? w->ratio * rz / ctl->rz_prev : 0.0;
+        } else {
+            ctl->alpha = 0.0;
+            ctl->beta = 0.0;
+            ctl->pq = 0.0;
+            ctl->rz_prev = 0.0;
+            ctl->pcur = 0;
+        }
+        ctl->rz = rz;
+        ctl->rr = rr;
+        ctl->tol2 = tol2;
+        ctl->maxit = left > 1 ? left : 1;
+        ctl->iterations = 0;
+        ctl->done = 0;
+        ctl->ticket = 0;
+        w->mode = kRunIterating;
     }
 }
 
@@ -325,6 +534,12 @@ struct amie_server {
     int grid = 0, group = 8;
     int rows_per_cta = 512;   // block rows per CTA of a slot
     bool persistent = false;  // mixed batches as one cooperative launch (kb_persistent)
+    uint32_t polls = 0;       // slot-barrier poll limit of kb_persistent
+    // test hook (AMIE_SERVER_SHORT_SLOT=k): the k-th request to join gets one CTA
+    // fewer in the CTA -> slot table than its descriptor claims, so its first
+    // slot barrier in a persistent batch cannot be reached and gives up
+    int short_slot_at = 0, n_joined = 0;
+    uint64_t n_timeouts = 0;  // persistent batches ended by a barrier that gave up
     amie::DevArray<uint32_t> d_bar;   // per slot barrier counters of kb_persistent
     amie::DevArray<int32_t> d_err;    // barrier timeout flag
     int32_t *h_err = nullptr;         // pinned copy
@@ -370,9 +585,9 @@ struct amie_server {
     amie::DevArray<int16_t> d_cta_slot;
     amie::DevArray<double> d_parts;              // pq | rz | rr | spare, grid each
     amie::SlotDesc *h_slots = nullptr;           // pinned
-    amie::PcgCtl *h_ctl = nullptr;               // pinned
-    double *h_norm = nullptr;                    // pinned: residual partials of finishing slots
-    std::vector<int> h_norm_n;
+    amie::PcgCtl *h_ctl = nullptr;               // pinned: a joining slot's first control block
+    amie::DevArray<amie::SlotRun> d_run;         // per slot: the solve's state (device-side refinement)
+    amie::SlotRun *h_run = nullptr;              // pinned
     int16_t *h_cta_slot = nullptr;               // pinned
     cudaGraphExec_t graph = nullptr;
     std::string error;
@@ -500,6 +715,8 @@ struct ServerOps {
         double *pp = srv->d_parts.p;
         d.parts = PcgParts{pp + c0, pp + g + c0, pp + 2 * g + c0, pp + 3 * g + c0};
         d.ctl = srv->d_ctl.p + slot;
+        d.run = srv->d_run.p + slot;
+        d.rhs = t->rhs.p;
         d.n = t->n;
         d.c0 = c0;
         d.c1 = c1;
@@ -539,28 +756,8 @@ struct ServerOps {
             k_pcg_start<double><<<nc, kVecThreads, 0, st>>>(d.v64, t->n, d.parts, d.ctl);
         }
         g_launches += srv->mixed ? 2 : 1;
-        // no synchronisation: the pinned h_ctl / h_slots entries are next written by
-        // the D2H copy that follows the next batch on the same stream
-        AMIE_CUDA(cudaGetLastError());
-        return AMIE_OK;
-    }
-
-    // Continue a mixed slot's inner run from its replaced residual with the
-    // search direction kept (reliable update); `ratio` = new / old residual norm.
-    static amie_status resume_inner(amie_server *srv, int slot, amie_server::Req *r, double ratio)
-    {
-        cudaStream_t st = srv->ctx->stream;
-        amie_topo *t = r->topo;
-        const SlotDesc &d = srv->h_slots[slot];
-        const int nc = d.c1 - d.c0;
-        const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
-        const double need = kMixedLastTarget * srv->cfg.rtol * r->bnorm / r->rnorm;
-        const double inner = std::min(0.5, std::max(kInnerReduction, need));
-        k_scale_to_f32<<<nc, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / r->rnorm, t->r32.p, t->d32.p);
-        k_pcg_resume<float><<<nc, kVecThreads, 0, st>>>(d.v32, t->n, d.parts, d.ctl, ratio, inner * inner,
-                                                        std::max<int64_t>(1, maxit - r->iterations));
-        g_launches += 2;
-        srv->h_ctl[slot].done = 0;   // the device block now says so too; refreshed after the next batch
+        // no synchronisation: the slot's pinned h_ctl / h_slots / h_run entries are
+        // written again only when it is retired (which synchronises the stream)
         AMIE_CUDA(cudaGetLastError());
         return AMIE_OK;
     }
@@ -575,6 +772,8 @@ struct ServerOps {
         const int c0 = alloc_ctas(srv, count);
         if (c0 < 0) return AMIE_NOT_READY;
         for (int c = c0; c < c0 + count; c++) srv->h_cta_slot[c] = (int16_t)slot;
+        if (srv->short_slot_at > 0 && ++srv->n_joined == srv->short_slot_at && count > 1)
+            srv->h_cta_slot[c0 + count - 1] = -1;   // test hook: one CTA of the slot is not launched
         srv->slot_req[slot] = r;
         r->slot = slot;
         {
@@ -590,6 +789,15 @@ struct ServerOps {
             AMIE_CUDA(cudaStreamSynchronize(st));
             return retire(srv, r, AMIE_OK);
         }
+        SlotRun &run = srv->h_run[slot];
+        run = SlotRun{};
+        run.bnorm = r->bnorm;
+        run.target = srv->cfg.rtol * r->bnorm;
+        run.rnorm = r->rnorm;
+        run.maxit = std::max<int64_t>(1000, (int64_t)r->topo->n);
+        run.status = AMIE_NOT_READY;
+        run.mode = kRunIterating;
+        AMIE_CUDA(cudaMemcpyAsync(srv->d_run.p + slot, srv->h_run + slot, sizeof(SlotRun), cudaMemcpyHostToDevice, st));
         return start_inner(srv, slot, r);
     }
 
@@ -628,47 +836,32 @@ struct ServerOps {
         return AMIE_OK;
     }
 
-    // Slots whose inner runs finished in the last batch: FP64 residual
-    // replacement for all of them (launched back to back, one synchronisation),
-    // then retire, resume or restart each.
-    static amie_status advance_all(amie_server *srv, const std::vector<int> &slots)
+    // Kernels that end every batch: the FP64 residual replacement and the
+    // decision for the slots whose inner run stopped (device-side refinement).
+    static void launch_refine(amie_server *srv, cudaStream_t st)
     {
-        cudaStream_t st = srv->ctx->stream;
-        const int cap = kNormParts;
-        for (size_t k = 0; k < slots.size(); k++) {
-            const int slot = slots[k];
-            amie_server::Req *r = srv->slot_req[slot];
-            amie_topo *t = r->topo;
-            SolverState *s = state_of(t);
-            r->iterations += srv->h_ctl[slot].iterations;
-            if (srv->mixed) {
-                k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, r->rnorm, t->x.p);
-                AMIE_LAUNCHED();
-                r->refinements++;
-            }
-            // r = b - A x and its partial norms, on few CTAs (requests are small)
-            const int g = (int)std::min<uint64_t>((uint64_t)cap, std::max<uint64_t>(1, (t->n_rows + 255) / 256));
-            double *part = s->parts.p + 3 * s->stride;
-            launch_spmv<double>(t, g, bsr64(t), t->x.p, t->rhs.p, t->r.p, part, st);
-            AMIE_CUDA(cudaMemcpyAsync(srv->h_norm + (size_t)k * cap, part, g * sizeof(double), cudaMemcpyDeviceToHost, st));
-            srv->h_norm_n[k] = g;
-        }
-        AMIE_CUDA(cudaStreamSynchronize(st));
-        for (size_t k = 0; k < slots.size(); k++) {
-            const int slot = slots[k];
-            amie_server::Req *r = srv->slot_req[slot];
-            amie_topo *t = r->topo;
-            double rr = 0.0;
-            for (int i = 0; i < srv->h_norm_n[k]; i++) rr += srv->h_norm[(size_t)k * cap + i];
-            const double scale = r->rnorm;
-            r->rnorm = std::sqrt(rr);
-            const int64_t maxit = std::max<int64_t>(1000, (int64_t)t->n);
-            if (!(rr == rr)) AMIE_TRY(retire(srv, r, AMIE_NAN));
-            else if (r->rnorm <= srv->cfg.rtol * r->bnorm) AMIE_TRY(retire(srv, r, AMIE_OK));
-            else if (r->iterations >= maxit || r->refinements > 200) AMIE_TRY(retire(srv, r, AMIE_NOT_CONVERGED));
-            // keep the direction while replacements show progress (see solve_pcg)
-            else if (srv->mixed && r->rnorm <= 0.5 * scale) AMIE_TRY(resume_inner(srv, slot, r, r->rnorm / scale));
-            else AMIE_TRY(start_inner(srv, slot, r));
+        const SlotDesc *sl = srv->d_slots.p;
+        const int16_t *cs = srv->d_cta_slot.p;
+        const int g = srv->grid;
+        if (srv->mixed) kb_accumulate<<<g, kVecThreads, 0, st>>>(sl, cs);
+        kb_residual<<<g, kVecThreads, 0, st>>>(sl, cs);
+        kb_restart<<<g, kVecThreads, 0, st>>>(sl, cs, kInnerReduction, kMixedLastTarget);
+    }
+
+    static int refine_kernels(const amie_server *srv) { return srv->mixed ? 3 : 2; }
+
+    // Requests whose solve the last batch ended (final SlotRun status): retired.
+    static amie_status collect(amie_server *srv)
+    {
+        for (size_t i = 0; i < srv->slot_req.size(); i++) {
+            amie_server::Req *r = srv->slot_req[i];
+            if (!r) continue;
+            const SlotRun &run = srv->h_run[i];
+            if (run.status == AMIE_NOT_READY) continue;
+            r->iterations = run.iterations;
+            r->refinements = run.refinements;
+            r->rnorm = run.rnorm;
+            AMIE_TRY(retire(srv, r, (amie_status)run.status));
         }
         return AMIE_OK;
     }
@@ -692,6 +885,7 @@ struct ServerOps {
                 launch_k(true, kb_direction<double>, g, 0, st, sl, cs);
             }
         }
+        launch_refine(srv, st);
         AMIE_CUDA(cudaStreamEndCapture(st, &graph));
         cudaError_t e = cudaGraphInstantiate(&srv->graph, graph, 0);
         cudaGraphDestroy(graph);
@@ -788,7 +982,9 @@ struct ServerOps {
                     int iters = srv->cfg.iters_per_launch;
                     uint32_t *bar = srv->d_bar.p;
                     int32_t *err = srv->d_err.p;
-                    void *args[] = {(void *)&sl, (void *)&cs, (void *)&iters, (void *)&bar, (void *)&err};
+                    uint32_t polls = srv->polls;
+                    void *args[] = {(void *)&sl, (void *)&cs, (void *)&iters, (void *)&bar, (void *)&err,
+                                    (void *)&polls};
                     const cudaError_t le = cudaLaunchCooperativeKernel((const void *)kb_persistent<float>,
                                                                        dim3(srv->grid), dim3(kVecThreads), args, 0, st);
                     if (le != cudaSuccess) {   // nothing ran: report and stop rather than wait on stale blocks
@@ -805,11 +1001,13 @@ struct ServerOps {
                     }
                     g_launches += 1;
                     cudaMemcpyAsync(srv->h_err, srv->d_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+                    launch_refine(srv, st);
                 } else {
                     cudaGraphLaunch(srv->graph, st);
                     g_launches += (srv->mixed ? 2 : 3) * srv->cfg.iters_per_launch;
                 }
-                cudaMemcpyAsync(srv->h_ctl, srv->d_ctl.p, srv->slot_req.size() * sizeof(PcgCtl), cudaMemcpyDeviceToHost,
+                g_launches += refine_kernels(srv);
+                cudaMemcpyAsync(srv->h_run, srv->d_run.p, srv->slot_req.size() * sizeof(SlotRun), cudaMemcpyDeviceToHost,
                                 st);
                 cudaEventRecord(srv->ctx->ev1, st);
             }
@@ -833,27 +1031,23 @@ struct ServerOps {
             if (active) {
                 cudaEventSynchronize(srv->ctx->ev1);
                 t_waited = now_s();
-                if (srv->persistent && *srv->h_err) {   // a slot barrier timed out: stop serving
-                    srv->error = "persistent batch: slot barrier timed out";
-                    std::lock_guard<std::mutex> lk(srv->mu);
-                    for (auto &kv : srv->all)
-                        if (kv.second->status == AMIE_NOT_READY) {
-                            kv.second->status = AMIE_TIMEOUT;
-                            kv.second->t_done = now_s();
-                        }
-                    srv->stop_flag = true;
-                    srv->cv.notify_all();
-                    break;
+                if (srv->persistent && *srv->h_err) {
+                    // a slot barrier gave up and the launch ended: the batch's slots are in
+                    // an unknown state, so their requests end with AMIE_TIMEOUT; the flag is
+                    // cleared and the server goes on with the next requests
+                    srv->n_timeouts++;
+                    for (size_t i = 0; i < srv->slot_req.size(); i++)
+                        if (srv->slot_req[i]) retire(srv, srv->slot_req[i], AMIE_TIMEOUT);
+                    *srv->h_err = 0;
+                    cudaMemsetAsync(srv->d_err.p, 0, sizeof(int32_t), srv->ctx->stream);
+                    cudaStreamSynchronize(srv->ctx->stream);
                 }
-                std::vector<int> finished;
                 for (size_t i = 0; i < srv->slot_req.size(); i++) {
                     amie_server::Req *r = srv->slot_req[i];
-                    if (!r) continue;
-                    if (r->cancelled) { retire(srv, r, AMIE_CANCELLED); continue; }
-                    if (srv->h_ctl[i].done) finished.push_back((int)i);
+                    if (r && r->cancelled) retire(srv, r, AMIE_CANCELLED);
                 }
                 tv = now_s();
-                if (!finished.empty()) advance_all(srv, finished);
+                collect(srv);
                 t_adv = now_s() - tv;
             }
             const double tj = now_s();
@@ -958,6 +1152,8 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
             const int v = std::atoi(e);
             if (v >= 32 && v <= (1 << 20)) srv->rows_per_cta = v;
         }
+        srv->polls = c.barrier_polls ? c.barrier_polls : kBarrierPolls;
+        if (const char *e = std::getenv("AMIE_SERVER_SHORT_SLOT")) srv->short_slot_at = std::max(0, std::atoi(e));
     }
     amie_config ac{ctx->device, 0, 0};
     amie_status rc = amie_ctx_create(&ac, &srv->adm);
@@ -971,25 +1167,27 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
         return s;
     };
     srv->slot_req.assign(c.max_slots, nullptr);
-    srv->h_norm_n.assign(c.max_slots, 0);
     if ((rc = srv->d_slots.alloc(ctx, c.max_slots)) || (rc = srv->d_ctl.alloc(ctx, c.max_slots)) ||
+        (rc = srv->d_run.alloc(ctx, c.max_slots)) ||
         (rc = srv->d_bar.alloc(ctx, c.max_slots)) || (rc = srv->d_err.alloc(ctx, 1)) ||
         (rc = srv->d_cta_slot.alloc(ctx, srv->grid)) || (rc = srv->d_parts.alloc(ctx, 4 * (size_t)srv->grid)))
         return fail(rc);
     if (cudaMallocHost((void **)&srv->h_slots, c.max_slots * sizeof(SlotDesc)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_ctl, c.max_slots * sizeof(PcgCtl)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_err, sizeof(int32_t)) != cudaSuccess ||
-        cudaMallocHost((void **)&srv->h_norm, (size_t)c.max_slots * kNormParts * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost((void **)&srv->h_run, c.max_slots * sizeof(SlotRun)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_cta_slot, srv->grid * sizeof(int16_t)) != cudaSuccess)
         return fail(AMIE_OOM);
     std::memset(srv->h_slots, 0, c.max_slots * sizeof(SlotDesc));
     std::memset(srv->h_ctl, 0, c.max_slots * sizeof(PcgCtl));
+    std::memset(srv->h_run, 0, c.max_slots * sizeof(SlotRun));
     *srv->h_err = 0;
     cudaMemsetAsync(srv->d_err.p, 0, sizeof(int32_t), ctx->stream);
     for (int i = 0; i < srv->grid; i++) srv->h_cta_slot[i] = -1;
     cudaStream_t st = ctx->stream;
     cudaMemcpyAsync(srv->d_slots.p, srv->h_slots, c.max_slots * sizeof(SlotDesc), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(srv->d_ctl.p, srv->h_ctl, c.max_slots * sizeof(PcgCtl), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(srv->d_run.p, srv->h_run, c.max_slots * sizeof(SlotRun), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(srv->d_cta_slot.p, srv->h_cta_slot, srv->grid * sizeof(int16_t), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(srv->d_parts.p, 0, 4 * (size_t)srv->grid * 8, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return fail(AMIE_CUDA_ERROR);
@@ -1142,10 +1340,11 @@ extern "C" amie_status amie_server_stop(amie_server *srv)
     if (srv->h_slots) cudaFreeHost(srv->h_slots);
     if (srv->h_ctl) cudaFreeHost(srv->h_ctl);
     if (srv->h_err) cudaFreeHost(srv->h_err);
-    if (srv->h_norm) cudaFreeHost(srv->h_norm);
+    if (srv->h_run) cudaFreeHost(srv->h_run);
     if (srv->h_cta_slot) cudaFreeHost(srv->h_cta_slot);
     srv->d_slots.release();
     srv->d_ctl.release();
+    srv->d_run.release();
     srv->d_bar.release();
     srv->d_err.release();
     srv->d_cta_slot.release();

@@ -80,8 +80,13 @@ struct SolverState {
     int graph_iters = 0;
     DevArray<double> x_saved;        // FP64 solve: the first stage's iterate while the second runs
     // FP32 inner runs of the mixed solver as single-reduction (Chronopoulos-Gear)
-    // PCG, one kernel per iteration (AMIE_CGCG=0: the two-kernel standard PCG)
-    bool cgcg = true;
+    // PCG, one kernel per iteration; opt-in (AMIE_CGCG=1).  Measured against the
+    // two-kernel standard PCG (mixed, rtol 1e-10): 150 k-DOF P1 11.7 vs 13.5 us per
+    // iteration but 2,016 vs 1,584 iterations and a node error of 1.3e-8 vs 3.6e-9;
+    // 64^3-voxel tetrahedra 47.0 vs 42.8 us per iteration; 1.2 M-DOF P2 (4,000
+    // inclusions, a Heaviside crack) did not converge: the recursively updated
+    // s = A p and the alpha recurrence drift in FP32 over its ~18,000 iterations
+    bool cgcg = false;
     int grid_cgcg = 0;
     int cg_cur = 0;                  // buffer of r, w holding the current FP32 residual
     DevArray<float> r32b, w32[2], s32[2], slice3;
@@ -622,8 +627,10 @@ amie_status run_cgcg(amie_topo *t, SolverState *s, double scale, double tol2, in
     c.pq = scale;
     if (scale != 0.0) {
         c.rz = c.rz * scale * scale;
+        c.rz_prev = c.rz_prev * scale * scale;
     } else {
         c.rz = 0.0;
+        c.rz_prev = 0.0;
         c.alpha = 0.0;
     }
     *s->h_ctl = c;
@@ -760,6 +767,9 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
     st_out->iterations = total;
     st_out->relres = std::sqrt(rr) / bnorm;
     st_out->status = result;
+    if (result != AMIE_OK)
+        set_error("%s PCG stopped at relative residual %g (rtol %g) after %lld iterations, %d refinements",
+                  mixed ? "mixed" : "FP64", st_out->relres, rtol, (long long)total, (int)st_out->refinements);
     return AMIE_OK;
 }
 
@@ -910,16 +920,28 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     AMIE_CUDA(cudaMemsetAsync(vz, 0, t->n * w, st));
     AMIE_CUDA(cudaMemsetAsync(vp, 0, t->n * w, st));
     AMIE_CUDA(cudaMemsetAsync(vp2, 0, t->n * w, st));
-    // the SpMV kernel of the solver graph: with the direction folded in, beta = 0.5, first buffer current
+    // the SpMV kernel of the solver graph: with the direction folded in, beta = 0.5, first buffer current;
+    // for the single-reduction iteration (the mixed solver's FP32 kernel when it is on) every
+    // vector it touches zeroed and a stop that never triggers
+    const bool cg = precision == 32 && use_cgcg(t, s);
     PcgCtl c{};
     c.beta = 0.5;
+    if (cg) {
+        const CgcgVecs<float> v = cgcg_vecs(t, s);
+        for (float *q : {v.x, v.p, v.r[0], v.r[1], v.w[0], v.w[1], v.s[0], v.s[1]})
+            AMIE_CUDA(cudaMemsetAsync(q, 0, t->n * 4, st));
+        c.tol2 = -1.0;
+        c.maxit = INT64_MAX;
+    }
     *s->h_ctl = c;
     AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
     PcgParts parts = parts_of(s);
     const int pi = precision == 64 ? 1 : 0;
     for (int i = 0; i <= reps; i++) {   // launch 0 is a warm-up
         if (i == 1) AMIE_CUDA(cudaEventRecord(t->ctx->ev0, st));
-        if (precision == 32 && fold<float>(s)) {
+        if (cg) {
+            launch_cgcg(t, s, false, false, st);
+        } else if (precision == 32 && fold<float>(s)) {
             launch_spmv_dir<float>(t, s->grid_dir[pi], vecs_of<float>(t), parts.pq, s->ctl.p, false, st, false,
                                    s->matrix_hint);
         } else {

@@ -1601,8 +1601,12 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_sell_cgcg(SellView<T> A, Cgc
         ctl->rr = br;
         ctl->pq = bd;
         if (start) {
-            // a kept direction continues (gamma_old rescaled by the host), else alpha = gamma / delta
-            const double beta = (scale != 0.0 && gamma_old != 0.0) ? bg / gamma_old : 0.0;
+            // A kept direction continues, else alpha = gamma / delta.  The stopped run's
+            // last iteration moved along p_i and left gamma_(i+1) in rz and gamma_i in
+            // rz_prev (both rescaled by the host); the new residual stands in for
+            // r_(i+1), so beta = gamma_new / gamma_i.
+            const double gamma_i = ctl->rz_prev;
+            const double beta = (scale != 0.0 && gamma_i != 0.0) ? bg / gamma_i : 0.0;
             const double den = beta != 0.0 && alpha_old != 0.0 ? bd - beta * bg / alpha_old : bd;
             ctl->beta = beta;
             ctl->alpha = den != 0.0 ? bg / den : 0.0;

@@ -429,36 +429,133 @@ def inclusion_square(N, L=0.04, order=1, n_inclusions=300, E_matrix=30e9, E_inc=
     return m, bcs, meta
 
 
-def homogenisation_request(target_dof, fraction, seed, L=0.04, strain=1e-4, E_matrix=30e9, E_inc=60e9):
-    """Config-4 request: config-0 style microstructure at a given size and inclusion
-    area fraction, with the macro strain eps_yy imposed on the whole boundary
-    (u_x = 0, u_y = strain * y)."""
+def _jinv_closed(X, Y):
+    """Inverse Jacobians (n,2,2) of P1 triangles, as _tri_jinv, in closed form."""
+    a = X[:, 2] - X[:, 1]
+    b = Y[:, 2] - Y[:, 1]
+    c = X[:, 0] - X[:, 1]
+    d = Y[:, 0] - Y[:, 1]
+    det = a * d - b * c
+    inv = np.empty((len(X), 2, 2))
+    inv[:, 0, 0] = d / det
+    inv[:, 0, 1] = -b / det
+    inv[:, 1, 0] = -c / det
+    inv[:, 1, 1] = a / det
+    return inv
+
+
+def _place_inclusions_batched(rng, radii, L, min_dist=1e-5, tries=200):
+    """Random sequential addition of non-overlapping circles in [0, L]^2, largest
+    first, up to `tries` candidate positions each (as place_inclusions), the
+    candidates drawn and tested in growing batches: the first candidate clear
+    of every placed circle wins."""
+    radii = np.sort(radii)[::-1]
+    cx = np.zeros(len(radii))
+    cy = np.zeros(len(radii))
+    cr = np.zeros(len(radii))
+    k = 0
+    for r in radii:
+        left = tries
+        for batch in (4, 16, 64):
+            nb = min(batch, left)
+            left -= nb
+            cand = rng.uniform(r, L - r, (nb, 2))
+            if k == 0:
+                j = 0
+            else:
+                dx = cand[:, :1] - cx[None, :k]
+                dy = cand[:, 1:] - cy[None, :k]
+                ok = np.flatnonzero(((dx * dx + dy * dy) > (cr[None, :k] + r + min_dist) ** 2).all(1))
+                if ok.size == 0:
+                    if left == 0:
+                        break
+                    continue
+                j = ok[0]
+            cx[k], cy[k], cr[k] = cand[j, 0], cand[j, 1], r
+            k += 1
+            break
+    return cx[:k], cy[:k], cr[:k]
+
+
+def _in_circles_structured(gx, gy, N, h, cx, cy, cr):
+    """Inclusion mask of the 2 N^2 triangles of structured_triangles(N, order=1)
+    from their centroids: each circle tests the triangles of the grid cells its
+    bounding box (plus one cell) covers."""
+    if len(cx) == 0:
+        return np.zeros(len(gx), bool)
+    i0 = np.clip(np.floor((cx - cr) / h).astype(np.int64) - 1, 0, N - 1)
+    i1 = np.clip(np.floor((cx + cr) / h).astype(np.int64) + 1, 0, N - 1)
+    j0 = np.clip(np.floor((cy - cr) / h).astype(np.int64) - 1, 0, N - 1)
+    j1 = np.clip(np.floor((cy + cr) / h).astype(np.int64) + 1, 0, N - 1)
+    ni = i1 - i0 + 1
+    cnt = ni * (j1 - j0 + 1)
+    circ = np.repeat(np.arange(len(cx)), cnt)
+    off = np.arange(int(cnt.sum())) - np.repeat(np.cumsum(cnt) - cnt, cnt)
+    cell = (j0[circ] + off // ni[circ]) * N + i0[circ] + off % ni[circ]
+    inside = np.zeros(len(gx), bool)
+    for half in (0, N * N):   # the two triangles of each cell
+        e = cell + half
+        hit = (gx[e] - cx[circ]) ** 2 + (gy[e] - cy[circ]) ** 2 < cr[circ] ** 2
+        inside[e[hit]] = True
+    return inside
+
+
+def homogenisation_request(target_dof, fraction, seed, L=0.04, strain=1e-4, E_matrix=30e9, E_inc=60e9, nu=0.2,
+                           rmin=0.3e-3, rmax=1.5e-3, jitter=0.15):
+    """Config-4 request: a config-0 style microstructure (P1 triangles on a
+    jittered N x N grid, non-overlapping inclusions with radii U[rmin, rmax]
+    drawn until the area fraction is reached) of about `target_dof` DOF, with
+    the macro strain eps_yy imposed on the whole boundary (u_x = 0,
+    u_y = strain * y).  Generated in a few milliseconds (batched placement and
+    inclusion test, closed-form Jacobians), so that every request of a stream
+    can carry its own microstructure."""
+    rng = np.random.default_rng(seed)
     N = max(4, int(round(np.sqrt(target_dof / 2.0))) - 1)
-    m, _, meta = inclusion_square(N, L=L, order=1, E_matrix=E_matrix, E_inc=E_inc, rmin=0.3e-3, rmax=1.5e-3,
-                                  seed=seed, fraction=fraction)
-    M = N + 1
+    x, y, conn, vx, vy, M = structured_triangles(N, L, 1, jitter, rng)
+    h = L / N
+    radii = []
+    area = 0.0
+    while area < fraction * L * L and len(radii) < 100000:
+        r = rng.uniform(rmin, rmax)
+        radii.append(r)
+        area += np.pi * r * r
+    cx, cy, cr = _place_inclusions_batched(rng, np.array(radii), L)
+    mat = _in_circles_structured(vx.mean(1), vy.mean(1), N, h, cx, cy, cr).astype(np.uint32)
+    E_count = len(conn)
+    m = am.MeshData(dim=2, stride=2, kind=np.full(E_count, am.TRI3, np.uint8),
+                    dof_ptr=(np.arange(E_count + 1) * 3).astype(np.uint32), dof_ids=conn.ravel(),
+                    gp_ptr=np.zeros(E_count + 1, np.uint32), gp=np.zeros(0), jinv=_jinv_closed(vx, vy).reshape(-1),
+                    mat=mat, cmat_table=np.stack([plane_stress(E_matrix, nu), plane_stress(E_inc, nu)]).reshape(-1),
+                    ndofmax=len(x))
     I, J = np.meshgrid(np.arange(M), np.arange(M), indexing="xy")
     I, J = I.ravel(), J.ravel()
     bnd = np.nonzero((I == 0) | (J == 0) | (I == M - 1) | (J == M - 1))[0]
-    y = J[bnd] * (L / N)
     ids = np.concatenate([bnd * 2, bnd * 2 + 1]).astype(np.uint32)
-    vals = np.concatenate([np.zeros(len(bnd)), strain * y])
+    vals = np.concatenate([np.zeros(len(bnd)), strain * J[bnd] * h])
     order = np.argsort(ids)
+    meta = dict(n_nodes=len(x), n_elem=E_count, n_inclusions=len(cr), n_dof=2 * len(x),
+                fraction=float(np.pi * (cr ** 2).sum() / (L * L)))
     return m, (ids[order], vals[order], np.zeros(len(ids), np.uint8)), meta
 
 
-def serving_mix(n_requests, rate, dof_min=2000, dof_max=200000, seed=7, pool=64):
-    """Config-4 arrival stream: Poisson arrivals at `rate` req/s, log-uniform sizes,
-    inclusion fraction U[0.2, 0.6].  A pool of `pool` distinct microstructures is
-    generated and each request draws one (numpy generation of thousands of
-    meshes would dominate the run); sizes and fractions follow the stated laws."""
+def serving_mix(n_requests, rate, dof_min=2000, dof_max=200000, seed=7):
+    """Config-4 arrival stream: Poisson arrivals at `rate` req/s, each request
+    its own microstructure with log-uniform size in [dof_min, dof_max] and
+    inclusion fraction U[0.2, 0.6].  Returns (specs, arrivals): specs[k] =
+    (target_dof, fraction, seed) for serving_request; the meshes are built
+    on demand (all of them at once would take gigabytes)."""
     rng = np.random.default_rng(seed)
-    sizes = np.exp(rng.uniform(np.log(dof_min), np.log(dof_max), pool))
-    fracs = rng.uniform(0.2, 0.6, pool)
-    meshes = [homogenisation_request(int(s), float(f), seed * 1000 + i) for i, (s, f) in enumerate(zip(sizes, fracs))]
+    sizes = np.exp(rng.uniform(np.log(dof_min), np.log(dof_max), n_requests))
+    fracs = rng.uniform(0.2, 0.6, n_requests)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
-    which = rng.integers(0, pool, n_requests)
-    return meshes, arrivals, which
+    specs = [(int(sz), float(f), seed * 100000 + k) for k, (sz, f) in enumerate(zip(sizes, fracs))]
+    return specs, arrivals
+
+
+def serving_request(spec):
+    """The request of a serving_mix spec: (mesh, (ids, values, kinds))."""
+    m, bcs, _ = homogenisation_request(*spec)
+    return m, bcs
 
 
 def notched_beam(nx=706, ny=176, Lx=0.4, Ly=0.1, notch_w=0.02, notch_h=0.002, E=35e9, nu=0.2, seed=3,
