@@ -1052,14 +1052,19 @@ namespace amie {
 void release_solver_state(const amie_topo *t);
 }
 
+void release_topology(amie_topo *t)
+{
+    release_solver_state(t);
+    release_damage(t);
+    delete t;
+}
+
 extern "C" amie_status amie_topology_destroy(amie_topo *t)
 {
     if (!t) return AMIE_OK;
     cudaSetDevice(t->ctx->device);
     cudaStreamSynchronize(t->ctx->stream);
-    release_solver_state(t);
-    release_damage(t);
-    delete t;
+    release_topology(t);
     return AMIE_OK;
 }
 

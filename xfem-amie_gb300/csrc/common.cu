@@ -3,6 +3,8 @@
 
 #include <cstdarg>
 #include <mutex>
+#include <unordered_map>
+#include <vector>
 
 namespace amie {
 
@@ -28,7 +30,7 @@ amie_status dev_alloc(Ctx *ctx, void **p, size_t bytes)
                   (unsigned long long)bytes, (unsigned long long)ctx->budget);
         return AMIE_OOM;
     }
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = ctx->pool ? cudaMallocFromPoolAsync(p, bytes, ctx->pool, ctx->stream) : cudaMalloc(p, bytes);
     if (e != cudaSuccess) {
         set_error("cudaMalloc(%llu): %s", (unsigned long long)bytes, cudaGetErrorString(e));
         cudaGetLastError();
@@ -39,11 +41,45 @@ amie_status dev_alloc(Ctx *ctx, void **p, size_t bytes)
     return AMIE_OK;
 }
 
+static thread_local cudaStream_t t_free_stream = nullptr;
+
+void set_free_stream(cudaStream_t st) { t_free_stream = st; }
+
 void dev_free(Ctx *ctx, void *p, size_t bytes)
 {
     if (!p) return;
-    cudaFree(p);
+    if (ctx && ctx->pool) cudaFreeAsync(p, t_free_stream ? t_free_stream : ctx->stream);
+    else cudaFree(p);
     if (ctx) ctx->allocated -= bytes;
+}
+
+static std::mutex g_pinned_mu;
+static std::unordered_map<size_t, std::vector<void *>> g_pinned_free;
+
+void *pinned_get(size_t bytes)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        auto &v = g_pinned_free[bytes];
+        if (!v.empty()) {
+            void *p = v.back();
+            v.pop_back();
+            return p;
+        }
+    }
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void pinned_put(void *p, size_t bytes)
+{
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    g_pinned_free[bytes].push_back(p);
 }
 
 }  // namespace amie

@@ -50,10 +50,18 @@ extern std::atomic<uint64_t> g_launches;
 
 #define AMIE_LAUNCHED() (::amie::g_launches.fetch_add(1, std::memory_order_relaxed))
 
-// Device allocation tracked against the context's HBM budget.
+// Device allocation tracked against the context's HBM budget.  A context with
+// a memory pool allocates stream-ordered on its stream and frees on the
+// calling thread's free stream (set_free_stream) or its own: no implicit
+// device synchronisation, which matters where solves run beside admissions.
 struct Ctx;
 amie_status dev_alloc(Ctx *ctx, void **p, size_t bytes);
 void dev_free(Ctx *ctx, void *p, size_t bytes);
+void set_free_stream(cudaStream_t st);   // this thread's frees of pool memory follow st (nullptr: the context's)
+
+// Small pinned host blocks, recycled instead of freed (cudaFreeHost waits for the device).
+void *pinned_get(size_t bytes);
+void pinned_put(void *p, size_t bytes);
 
 template <typename T>
 struct DevArray {
@@ -90,6 +98,7 @@ struct Ctx {
     int num_sms = kSMs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double *h_scalars = nullptr;  // pinned scratch for solver control reads
+    cudaMemPool_t pool = nullptr; // stream-ordered allocations (the server's admission contexts)
 };
 
 // Device-side view of the element data used by the quadrature kernels.
@@ -168,6 +177,7 @@ namespace amie {
 struct DamageState;
 }
 void release_damage(amie_topo *t);   // damage.cu
+void release_topology(amie_topo *t);   // assemble.cu: frees everything, no synchronisation
 
 // Opaque handles of the C-ABI.
 struct amie_ctx : public amie::Ctx {};

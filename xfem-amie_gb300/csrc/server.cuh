@@ -41,7 +41,7 @@ struct SlotRun {
     int32_t refinements;  // residual replacements (mixed)
     int32_t status;       // AMIE_NOT_READY while the solve runs, then its result
     int32_t mode;         // kRunIterating, or what kb_restart does next
-    int32_t pad_;
+    uint32_t gen;         // join number of the request (the host ignores copies of an earlier one)
 };
 constexpr int32_t kRunIterating = 0;   // the inner run iterates (or stopped and awaits kb_residual)
 constexpr int32_t kRunResume = 1;      // continue the inner run from the replaced residual, direction kept
@@ -528,7 +528,8 @@ __global__ void __launch_bounds__(kVecThreads) kb_restart(const SlotDesc *slots,
 
 struct amie_server {
     amie_ctx *ctx = nullptr;        // solve stream
-    amie_ctx *adm = nullptr;        // admission stream
+    std::vector<amie_ctx *> adms;   // one context (stream) per admission thread
+    cudaStream_t xfer = nullptr;    // result copies of retired solves (beside the batches)
     amie_server_config cfg{};
     bool mixed = true;
     int grid = 0, group = 8;
@@ -558,6 +559,7 @@ struct amie_server {
         double t_submit = 0, t_admit = 0, t_done = 0;
         amie_topo *topo = nullptr;
         int slot = -1;
+        uint32_t gen = 0;   // join number
         double bnorm = 0, rnorm = 0;   // rnorm: the true residual the current inner run was scaled by
         int64_t iterations = 0;
         int refinements = 0;
@@ -573,8 +575,10 @@ struct amie_server {
     std::map<uint64_t, Req *> all;
     uint64_t next_ticket = 1;
     bool running = false, stop_flag = false;
-    std::thread worker;     // the batch loop
-    std::thread admitter;   // admissions, on the admission context, overlapping the batch
+    std::thread worker;                   // the batch loop
+    std::vector<std::thread> admitters;   // admissions, each on its own context, overlapping the batch
+    cudaMemPool_t pool = nullptr;         // the admission contexts' stream-ordered allocations
+    uint32_t n_gen = 0;                   // joins so far
     std::deque<Req *> ready;                     // admitted, waiting to join (under mu)
     int admitting = 0, n_active = 0, n_waiting = 0;   // (under mu) inside admit(), in slots, admitted but not joined
 
@@ -587,7 +591,9 @@ struct amie_server {
     amie::SlotDesc *h_slots = nullptr;           // pinned
     amie::PcgCtl *h_ctl = nullptr;               // pinned: a joining slot's first control block
     amie::DevArray<amie::SlotRun> d_run;         // per slot: the solve's state (device-side refinement)
-    amie::SlotRun *h_run = nullptr;              // pinned
+    amie::SlotRun *h_run = nullptr;              // pinned: a joining slot's first state
+    amie::SlotRun *h_ring = nullptr;             // pinned, 2 x slots: d_run after each of two batches in flight
+    cudaEvent_t ring_ev[2] = {nullptr, nullptr};
     int16_t *h_cta_slot = nullptr;               // pinned
     cudaGraphExec_t graph = nullptr;
     std::string error;
@@ -647,10 +653,10 @@ struct ServerOps {
 
     // Upload + pattern + element matrices + gather + elimination on the admission stream,
     // then the initial FP64 residual.
-    static amie_status admit(amie_server *srv, amie_server::Req *r)
+    static amie_status admit(amie_server *srv, amie_server::Req *r, amie_ctx *adm)
     {
         amie_topo *t = nullptr;
-        AMIE_TRY(amie_topology_build(srv->adm, &r->mesh, &t));
+        AMIE_TRY(amie_topology_build(adm, &r->mesh, &t));
         r->topo = t;
         if (t->s != 2) {
             set_error("the server batches 2D meshes only");
@@ -665,7 +671,7 @@ struct ServerOps {
         if (srv->mixed) AMIE_TRY(finalize_matrix_async(t, true));
         AMIE_TRY(ensure_sell(t, !srv->mixed, srv->mixed));
         AMIE_TRY(ensure_sell_partition(t, ctas_for(srv, t->n_rows)));   // the slot's CTA count
-        cudaStream_t st = srv->adm->stream;
+        cudaStream_t st = adm->stream;
         if (!r->x0.empty() && r->x0.size() == t->n)
             AMIE_CUDA(cudaMemcpyAsync(t->x.p, r->x0.data(), t->n * 8, cudaMemcpyHostToDevice, st));
         else
@@ -791,6 +797,8 @@ struct ServerOps {
         }
         SlotRun &run = srv->h_run[slot];
         run = SlotRun{};
+        r->gen = ++srv->n_gen;
+        run.gen = r->gen;
         run.bnorm = r->bnorm;
         run.target = srv->cfg.rtol * r->bnorm;
         run.rnorm = r->rnorm;
@@ -801,30 +809,38 @@ struct ServerOps {
         return start_inner(srv, slot, r);
     }
 
+    // Ends a request.  Its result is copied on the transfer stream (the solve
+    // stream may hold a batch in flight, which skips the finished slot); the
+    // slot's descriptor and CTAs are released by copies queued on the solve
+    // stream (applied before the next batch), and so is the topology's memory
+    // (stream-ordered frees into the server's pool, after that batch).
     static amie_status retire(amie_server *srv, amie_server::Req *r, amie_status result)
     {
         cudaStream_t st = srv->ctx->stream;
         amie_topo *t = r->topo;
         if (t && result != AMIE_CANCELLED) {
             r->x.resize(t->n);
-            AMIE_CUDA(cudaMemcpyAsync(r->x.data(), t->x.p, t->n * 8, cudaMemcpyDeviceToHost, st));
-            AMIE_CUDA(cudaStreamSynchronize(st));
+            AMIE_CUDA(cudaMemcpyAsync(r->x.data(), t->x.p, t->n * 8, cudaMemcpyDeviceToHost, srv->xfer));
+            AMIE_CUDA(cudaStreamSynchronize(srv->xfer));
         }
         if (r->slot >= 0) {
             const int slot = r->slot;
             for (int c = 0; c < srv->grid; c++)
                 if (srv->h_cta_slot[c] == slot) srv->h_cta_slot[c] = -1;
             srv->h_slots[slot].active = 0;
+            // the pinned sources are rewritten only by later joins and retirements
+            // of the loop thread, whose copies follow these on the same stream
             AMIE_CUDA(cudaMemcpyAsync(srv->d_slots.p + slot, srv->h_slots + slot, sizeof(SlotDesc), cudaMemcpyHostToDevice, st));
             AMIE_CUDA(cudaMemcpyAsync(srv->d_cta_slot.p, srv->h_cta_slot, srv->grid * sizeof(int16_t), cudaMemcpyHostToDevice, st));
-            AMIE_CUDA(cudaStreamSynchronize(st));
             srv->slot_req[slot] = nullptr;
             r->slot = -1;
             std::lock_guard<std::mutex> lk(srv->mu);
             srv->n_active--;
         }
         if (t) {
-            amie_topology_destroy(t);
+            set_free_stream(st);
+            release_topology(t);
+            set_free_stream(nullptr);
             r->topo = nullptr;
         }
         srv->in_use -= r->footprint;
@@ -850,14 +866,15 @@ struct ServerOps {
 
     static int refine_kernels(const amie_server *srv) { return srv->mixed ? 3 : 2; }
 
-    // Requests whose solve the last batch ended (final SlotRun status): retired.
-    static amie_status collect(amie_server *srv)
+    // Requests whose solve a batch ended (final SlotRun status in the batch's
+    // copy `runs`, of the request's own join): retired.
+    static amie_status collect(amie_server *srv, const SlotRun *runs)
     {
         for (size_t i = 0; i < srv->slot_req.size(); i++) {
             amie_server::Req *r = srv->slot_req[i];
             if (!r) continue;
-            const SlotRun &run = srv->h_run[i];
-            if (run.status == AMIE_NOT_READY) continue;
+            const SlotRun &run = runs[i];
+            if (run.gen != r->gen || run.status == AMIE_NOT_READY) continue;
             r->iterations = run.iterations;
             r->refinements = run.refinements;
             r->rnorm = run.rnorm;
@@ -906,7 +923,7 @@ struct ServerOps {
     // Admission thread: takes pending requests while slots allow and admits
     // them (topology, assembly, elimination, SELL copy, first residual) on the
     // admission context, overlapping the batch loop; hands them over in `ready`.
-    static void admit_loop(amie_server *srv)
+    static void admit_loop(amie_server *srv, amie_ctx *adm)
     {
         cudaSetDevice(srv->ctx->device);
         while (true) {
@@ -945,7 +962,7 @@ struct ServerOps {
             }
             const double ta = now_s();
             r->t_admit = ta;
-            const amie_status st = admit(srv, r);
+            const amie_status st = admit(srv, r, adm);
             if (st != AMIE_OK && r->topo) {
                 amie_topology_destroy(r->topo);
                 r->topo = nullptr;
@@ -965,56 +982,71 @@ struct ServerOps {
         }
     }
 
+    // One batch on the solve stream (graph, or cooperative launch + refinement),
+    // then the copy of every slot's SlotRun into ring buffer `k` and its event.
+    static bool launch_batch(amie_server *srv, int k)
+    {
+        cudaStream_t st = srv->ctx->stream;
+        if (srv->persistent) {
+            cudaMemsetAsync(srv->d_bar.p, 0, srv->slot_req.size() * sizeof(uint32_t), st);
+            const SlotDesc *sl = srv->d_slots.p;
+            const int16_t *cs = srv->d_cta_slot.p;
+            int iters = srv->cfg.iters_per_launch;
+            uint32_t *bar = srv->d_bar.p;
+            int32_t *err = srv->d_err.p;
+            uint32_t polls = srv->polls;
+            void *args[] = {(void *)&sl, (void *)&cs, (void *)&iters, (void *)&bar, (void *)&err, (void *)&polls};
+            const cudaError_t le = cudaLaunchCooperativeKernel((const void *)kb_persistent<float>, dim3(srv->grid),
+                                                               dim3(kVecThreads), args, 0, st);
+            if (le != cudaSuccess) {   // nothing ran: report and stop rather than wait on stale blocks
+                srv->error = std::string("cooperative launch: ") + cudaGetErrorString(le);
+                std::lock_guard<std::mutex> lk(srv->mu);
+                for (auto &kv : srv->all)
+                    if (kv.second->status == AMIE_NOT_READY) {
+                        kv.second->status = AMIE_CUDA_ERROR;
+                        kv.second->t_done = now_s();
+                    }
+                srv->stop_flag = true;
+                srv->cv.notify_all();
+                return false;
+            }
+            g_launches += 1;
+            cudaMemcpyAsync(srv->h_err, srv->d_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+            launch_refine(srv, st);
+        } else {
+            cudaGraphLaunch(srv->graph, st);
+            g_launches += (srv->mixed ? 2 : 3) * srv->cfg.iters_per_launch;
+        }
+        g_launches += refine_kernels(srv);
+        const size_t ns = srv->slot_req.size();
+        cudaMemcpyAsync(srv->h_ring + (size_t)k * ns, srv->d_run.p, ns * sizeof(SlotRun), cudaMemcpyDeviceToHost, st);
+        cudaEventRecord(srv->ring_ev[k], st);
+        return true;
+    }
+
+    // The batch loop.  Two batches stay in flight (one with the persistent
+    // kernel): while batch k + 1 runs, the host reads batch k's SlotRun copy,
+    // retires the solves it finished (those slots do no work in batch k + 1)
+    // and joins admitted requests, whose start kernels and table updates queue
+    // behind batch k + 1.
     static void loop(amie_server *srv)
     {
         cudaSetDevice(srv->ctx->device);
         std::vector<amie_server::Req *> admitted;   // handed over, not yet joined
+        const int depth = srv->persistent ? 1 : 2;
+        int64_t launched = 0, done = 0;             // batches launched / processed
         while (true) {
             const double t_round = now_s();
-            // 1. batch iterations in flight on the solve stream
-            const bool active = any_active(srv);
-            if (active) {
-                cudaStream_t st = srv->ctx->stream;
-                if (srv->persistent) {
-                    cudaMemsetAsync(srv->d_bar.p, 0, srv->slot_req.size() * sizeof(uint32_t), st);
-                    const SlotDesc *sl = srv->d_slots.p;
-                    const int16_t *cs = srv->d_cta_slot.p;
-                    int iters = srv->cfg.iters_per_launch;
-                    uint32_t *bar = srv->d_bar.p;
-                    int32_t *err = srv->d_err.p;
-                    uint32_t polls = srv->polls;
-                    void *args[] = {(void *)&sl, (void *)&cs, (void *)&iters, (void *)&bar, (void *)&err,
-                                    (void *)&polls};
-                    const cudaError_t le = cudaLaunchCooperativeKernel((const void *)kb_persistent<float>,
-                                                                       dim3(srv->grid), dim3(kVecThreads), args, 0, st);
-                    if (le != cudaSuccess) {   // nothing ran: report and stop rather than wait on stale blocks
-                        srv->error = std::string("cooperative launch: ") + cudaGetErrorString(le);
-                        std::lock_guard<std::mutex> lk(srv->mu);
-                        for (auto &kv : srv->all)
-                            if (kv.second->status == AMIE_NOT_READY) {
-                                kv.second->status = AMIE_CUDA_ERROR;
-                                kv.second->t_done = now_s();
-                            }
-                        srv->stop_flag = true;
-                        srv->cv.notify_all();
-                        break;
-                    }
-                    g_launches += 1;
-                    cudaMemcpyAsync(srv->h_err, srv->d_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
-                    launch_refine(srv, st);
-                } else {
-                    cudaGraphLaunch(srv->graph, st);
-                    g_launches += (srv->mixed ? 2 : 3) * srv->cfg.iters_per_launch;
-                }
-                g_launches += refine_kernels(srv);
-                cudaMemcpyAsync(srv->h_run, srv->d_run.p, srv->slot_req.size() * sizeof(SlotRun), cudaMemcpyDeviceToHost,
-                                st);
-                cudaEventRecord(srv->ctx->ev1, st);
+            // 1. keep `depth` batches in flight while any slot is active
+            if (any_active(srv) && launched - done < depth) {
+                if (!launch_batch(srv, (int)(launched & 1))) break;
+                launched++;
+                if (launched - done < depth) continue;   // fill the pipeline first
             }
-            // 2. requests the admission thread has finished
+            // 2. requests the admission threads have finished
             {
                 std::unique_lock<std::mutex> lk(srv->mu);
-                if (!active && srv->ready.empty() && admitted.empty()) {
+                if (launched == done && srv->ready.empty() && admitted.empty()) {
                     if (srv->stop_flag && srv->pending.empty() && srv->admitting == 0) break;
                     srv->cv.wait_for(lk, std::chrono::milliseconds(2));
                     continue;
@@ -1026,10 +1058,12 @@ struct ServerOps {
                 srv->n_waiting = (int)admitted.size();
             }
             const double tw = now_s();
-            // 3. batch results
-            double t_waited = tw, tv = tw, t_adv = 0.0;
-            if (active) {
-                cudaEventSynchronize(srv->ctx->ev1);
+            // 3. results of the oldest batch in flight
+            double t_waited = tw, t_adv = 0.0;
+            if (launched > done) {
+                const int k = (int)(done & 1);
+                cudaEventSynchronize(srv->ring_ev[k]);
+                done++;
                 t_waited = now_s();
                 if (srv->persistent && *srv->h_err) {
                     // a slot barrier gave up and the launch ended: the batch's slots are in
@@ -1040,15 +1074,13 @@ struct ServerOps {
                         if (srv->slot_req[i]) retire(srv, srv->slot_req[i], AMIE_TIMEOUT);
                     *srv->h_err = 0;
                     cudaMemsetAsync(srv->d_err.p, 0, sizeof(int32_t), srv->ctx->stream);
-                    cudaStreamSynchronize(srv->ctx->stream);
                 }
                 for (size_t i = 0; i < srv->slot_req.size(); i++) {
                     amie_server::Req *r = srv->slot_req[i];
                     if (r && r->cancelled) retire(srv, r, AMIE_CANCELLED);
                 }
-                tv = now_s();
-                collect(srv);
-                t_adv = now_s() - tv;
+                collect(srv, srv->h_ring + (size_t)k * srv->slot_req.size());
+                t_adv = now_s() - t_waited;
             }
             const double tj = now_s();
             // 4. join admitted requests
@@ -1071,7 +1103,7 @@ struct ServerOps {
                 srv->stats.advance_s += t_adv;
                 srv->stats.join_s += te - tj;
                 srv->stats.loop_s += te - t_round;
-                if (active) srv->stats.batches++;
+                if (t_waited > tw) srv->stats.batches++;
                 srv->cv.notify_all();
             }
             cudaError_t e = cudaGetLastError();
@@ -1084,6 +1116,8 @@ struct ServerOps {
                 break;
             }
         }
+        // nothing of this thread's may remain in flight when it ends
+        cudaStreamSynchronize(srv->ctx->stream);
     }
 };
 
@@ -1155,17 +1189,53 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
         srv->polls = c.barrier_polls ? c.barrier_polls : kBarrierPolls;
         if (const char *e = std::getenv("AMIE_SERVER_SHORT_SLOT")) srv->short_slot_at = std::max(0, std::atoi(e));
     }
+    // admission threads (AMIE_SERVER_ADMITTERS, 1-8, default 2), each on its own context
+    // (4,096-request mix at 200/s: 1.5 ms of admission per request; one thread and
+    // three gave the same latencies)
+    int n_adm = 2;
+    if (const char *e = std::getenv("AMIE_SERVER_ADMITTERS")) n_adm = std::max(1, std::min(8, std::atoi(e)));
     amie_config ac{ctx->device, 0, 0};
-    amie_status rc = amie_ctx_create(&ac, &srv->adm);
-    if (rc != AMIE_OK) {
-        delete srv;
-        return rc;
-    }
+    amie_status rc = AMIE_OK;
     auto fail = [&](amie_status s) {
-        amie_ctx_destroy(srv->adm);
+        for (amie_ctx *a : srv->adms) amie_ctx_destroy(a);
+        if (srv->pool) cudaMemPoolDestroy(srv->pool);
+        if (srv->xfer) cudaStreamDestroy(srv->xfer);
+        for (cudaEvent_t e : srv->ring_ev)
+            if (e) cudaEventDestroy(e);
+        if (srv->h_slots) cudaFreeHost(srv->h_slots);
+        if (srv->h_ctl) cudaFreeHost(srv->h_ctl);
+        if (srv->h_err) cudaFreeHost(srv->h_err);
+        if (srv->h_run) cudaFreeHost(srv->h_run);
+        if (srv->h_ring) cudaFreeHost(srv->h_ring);
+        if (srv->h_cta_slot) cudaFreeHost(srv->h_cta_slot);
         delete srv;
         return s;
     };
+    {
+        // requests' memory comes from a pool of the server's: allocated stream-ordered
+        // on an admission stream, freed stream-ordered on the solve stream at retirement
+        // (cudaFree would wait for the batch in flight); kept cached, and a free is
+        // reused only once it has completed (no cross-stream dependencies inserted)
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = ctx->device;
+        if (cudaMemPoolCreate(&srv->pool, &props) != cudaSuccess) return fail(AMIE_CUDA_ERROR);
+        uint64_t keep = UINT64_MAX;
+        int no = 0;
+        cudaMemPoolSetAttribute(srv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        cudaMemPoolSetAttribute(srv->pool, cudaMemPoolReuseAllowInternalDependencies, &no);
+    }
+    for (int i = 0; i < n_adm; i++) {
+        amie_ctx *a = nullptr;
+        if ((rc = amie_ctx_create(&ac, &a)) != AMIE_OK) return fail(rc);
+        a->pool = srv->pool;
+        srv->adms.push_back(a);
+    }
+    if (cudaStreamCreateWithFlags(&srv->xfer, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&srv->ring_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&srv->ring_ev[1], cudaEventDisableTiming) != cudaSuccess)
+        return fail(AMIE_CUDA_ERROR);
     srv->slot_req.assign(c.max_slots, nullptr);
     if ((rc = srv->d_slots.alloc(ctx, c.max_slots)) || (rc = srv->d_ctl.alloc(ctx, c.max_slots)) ||
         (rc = srv->d_run.alloc(ctx, c.max_slots)) ||
@@ -1176,6 +1246,7 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
         cudaMallocHost((void **)&srv->h_ctl, c.max_slots * sizeof(PcgCtl)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_err, sizeof(int32_t)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_run, c.max_slots * sizeof(SlotRun)) != cudaSuccess ||
+        cudaMallocHost((void **)&srv->h_ring, 2 * (size_t)c.max_slots * sizeof(SlotRun)) != cudaSuccess ||
         cudaMallocHost((void **)&srv->h_cta_slot, srv->grid * sizeof(int16_t)) != cudaSuccess)
         return fail(AMIE_OOM);
     std::memset(srv->h_slots, 0, c.max_slots * sizeof(SlotDesc));
@@ -1194,7 +1265,7 @@ extern "C" amie_status amie_server_start(amie_ctx *ctx, const amie_server_config
     if ((rc = ServerOps::capture(srv)) != AMIE_OK) return fail(rc);
     srv->running = true;
     srv->worker = std::thread(ServerOps::loop, srv);
-    srv->admitter = std::thread(ServerOps::admit_loop, srv);
+    for (amie_ctx *a : srv->adms) srv->admitters.emplace_back(ServerOps::admit_loop, srv, a);
     *out = srv;
     return AMIE_OK;
 }
@@ -1328,20 +1399,29 @@ extern "C" amie_status amie_server_stop(amie_server *srv)
             if (r) r->cancelled = true;
         srv->cv.notify_all();
     }
-    if (srv->admitter.joinable()) srv->admitter.join();
+    for (std::thread &a : srv->admitters)
+        if (a.joinable()) a.join();
     if (srv->worker.joinable()) srv->worker.join();
     cudaSetDevice(srv->ctx->device);
     cudaStreamSynchronize(srv->ctx->stream);
+    for (amie_ctx *a : srv->adms) cudaStreamSynchronize(a->stream);
+    amie::set_free_stream(srv->ctx->stream);
     for (auto &kv : srv->all) {
-        if (kv.second->topo) amie_topology_destroy(kv.second->topo);
+        if (kv.second->topo) release_topology(kv.second->topo);
         delete kv.second;
     }
+    amie::set_free_stream(nullptr);
+    cudaStreamSynchronize(srv->ctx->stream);
     if (srv->graph) cudaGraphExecDestroy(srv->graph);
     if (srv->h_slots) cudaFreeHost(srv->h_slots);
     if (srv->h_ctl) cudaFreeHost(srv->h_ctl);
     if (srv->h_err) cudaFreeHost(srv->h_err);
     if (srv->h_run) cudaFreeHost(srv->h_run);
+    if (srv->h_ring) cudaFreeHost(srv->h_ring);
     if (srv->h_cta_slot) cudaFreeHost(srv->h_cta_slot);
+    if (srv->xfer) cudaStreamDestroy(srv->xfer);
+    for (cudaEvent_t e : srv->ring_ev)
+        if (e) cudaEventDestroy(e);
     srv->d_slots.release();
     srv->d_ctl.release();
     srv->d_run.release();
@@ -1349,7 +1429,8 @@ extern "C" amie_status amie_server_stop(amie_server *srv)
     srv->d_err.release();
     srv->d_cta_slot.release();
     srv->d_parts.release();
-    amie_ctx_destroy(srv->adm);
+    for (amie_ctx *a : srv->adms) amie_ctx_destroy(a);
+    if (srv->pool) cudaMemPoolDestroy(srv->pool);
     delete srv;
     return AMIE_OK;
 }

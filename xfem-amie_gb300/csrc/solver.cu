@@ -96,8 +96,8 @@ struct SolverState {
         if (graph64) cudaGraphExecDestroy(graph64);
         if (graph32) cudaGraphExecDestroy(graph32);
         if (graph_cg) cudaGraphExecDestroy(graph_cg);
-        if (h_ctl) cudaFreeHost(h_ctl);
-        if (h_ring) cudaFreeHost(h_ring);
+        pinned_put(h_ctl, sizeof(PcgCtl));
+        pinned_put(h_ring, 2 * sizeof(PcgCtl));
         for (cudaEvent_t e : ring_ev)
             if (e) cudaEventDestroy(e);
     }
@@ -327,8 +327,12 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         if (const char *e = std::getenv("AMIE_FOLD_DIR")) s->fold_dir = std::atoi(e) != 0;
         AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->stride));
         AMIE_TRY(s->ctl.alloc(t->ctx, 1));
-        AMIE_CUDA(cudaMallocHost((void **)&s->h_ctl, sizeof(PcgCtl)));
-        AMIE_CUDA(cudaMallocHost((void **)&s->h_ring, 2 * sizeof(PcgCtl)));
+        s->h_ctl = (PcgCtl *)pinned_get(sizeof(PcgCtl));
+        s->h_ring = (PcgCtl *)pinned_get(2 * sizeof(PcgCtl));
+        if (!s->h_ctl || !s->h_ring) {
+            set_error("pinned host allocation failed");
+            return AMIE_OOM;
+        }
         for (cudaEvent_t &e : s->ring_ev) AMIE_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         const uint64_t n = t->n;
         AMIE_TRY(t->r.alloc(t->ctx, n));
