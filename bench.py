@@ -77,6 +77,8 @@ def parse_args():
     ap.add_argument("--launch-list", action="store_true", help="run exactly one step without warm-up (for an ncu "
                                                                "launch list), print its timing, exit")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--damage-only", action="store_true", help="run only the config-3 damage loop (--damage-steps) "
+                                                               "and print its statistics")
     ap.add_argument("--damage-steps", type=int, default=30, help="config-3 damage-loop load steps of 1 um "
                                                                  "deflection each (0 = skip)")
     return ap.parse_args()
@@ -122,17 +124,26 @@ def cgcg_on() -> bool:
     return os.environ.get("AMIE_CGCG", "0") not in ("", "0")
 
 
-def spmv_bytes(nnzb: int, n_rows: int, s: int, w: int, fold: bool = False, cgcg: bool = False) -> int:
+def spmv_bytes(nnzb: int, n_rows: int, s: int, w: int, fold: bool = False, cgcg=False) -> int:
     """Algorithmic bytes of one block SpMV: blocks + column indices + row pointers + x read + y write;
     with the direction update folded in, z and p_old are read and q and p_new written (4 vectors);
-    one single-reduction PCG iteration reads r, w, s_old, D^-1, p, x and writes p, s, x, r_new,
-    w_new (11 vectors)."""
-    vecs = 11 if cgcg else (4 if fold else 2)
+    one single-reduction PCG iteration (cgcg True) reads r, w, s_old, D^-1, p, x and writes p, s, x,
+    r_new, w_new (11 vectors); one iteration of the one-kernel PCG (cgcg "fused") reads r, q, x,
+    D^-1, p_old and the interleaved z, w (7) and writes r, x, q, p_new, z, w (6): 13 vectors."""
+    vecs = 13 if cgcg == "fused" else (11 if cgcg else (4 if fold else 2))
     return nnzb * (s * s * w + 4) + 4 * (n_rows + 1) + vecs * n_rows * s * w
+
+
+def fused_on() -> bool:
+    """Whether the mixed solver's FP32 runs are one kernel per iteration of standard PCG
+    (opt-in, AMIE_FUSED=1; the default is the two-kernel graph)."""
+    return os.environ.get("AMIE_FUSED", "0") not in ("", "0")
 
 
 def spmv_kernel_key(w: int):
     """(kernel name, traffic key suffix, cgcg, fold) of the dominant kernel of a solve in w-byte floats."""
+    if w == 4 and fused_on():
+        return "k_sell_fused", "sell_fused", "fused", False
     if w == 4 and cgcg_on():
         return "k_sell_cgcg", "sell_cgcg", True, False
     if w == 4 and fold_dir():
@@ -356,6 +367,10 @@ def run_ours(args, world, rank, local, dist):
     solver = G.SOLVER_PCG_MIXED if args.solver == "mixed" else G.SOLVER_PCG_FP64
     if args.serve_only:
         print(json.dumps({"serving": run_serving(ctx, args.serve, args.serve_rate, solver, iters=args.serve_iters)}))
+        ctx.close()
+        return 0
+    if args.damage_only:
+        print(json.dumps({"damage_loop": run_damage_loop(ctx, solver, args.damage_steps, 1e-6 * args.damage_steps)}))
         ctx.close()
         return 0
     m, bcs, meta, name = make_workload(args.config, args.size)

@@ -96,3 +96,28 @@ def test_single_reduction_pcg_solves(gpu_ctx, monkeypatch, name):
         assert np.abs(x1[s] - xo[s]).max() <= 1e-8 * np.abs(xo[s]).max()
     finally:
         t.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_one_kernel_pcg_solves(gpu_ctx, monkeypatch, name):
+    """The opt-in one-kernel FP32 PCG (AMIE_FUSED=1, k_sell_fused: the previous
+    iteration's update and the direction formed inside the SpMV, r.z of the
+    next step from the expansion of r - alpha q) reaches the oracle's solution
+    and repeats bit for bit."""
+    import amie_gpu
+    monkeypatch.setenv("AMIE_FUSED", "1")
+    d = load_golden(name)
+    m = am.from_golden(d, "tabulated")
+    t = amie_gpu.Topology(gpu_ctx, m)
+    try:
+        t.assemble()
+        t.apply_dirichlet(*am.golden_bcs(d))
+        x1, st1 = t.solve(amie_gpu.SOLVER_PCG_MIXED, rtol=1e-10)
+        x2, st2 = t.solve(amie_gpu.SOLVER_PCG_MIXED, rtol=1e-10)
+        assert st1["relres"] <= 1e-10 and relres(d, m, x1) <= 2e-10
+        assert np.array_equal(x1, x2) and st1["iterations"] == st2["iterations"]
+        xo, _, _, _ = O.pcg(m.stride, d["row_size"], d["column_index"], d["array"], d["rhs"], rtol=1e-13)
+        s = node_dofs(m)
+        assert np.abs(x1[s] - xo[s]).max() <= 1e-8 * np.abs(xo[s]).max()
+    finally:
+        t.close()

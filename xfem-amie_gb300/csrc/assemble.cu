@@ -453,9 +453,24 @@ __global__ void k_gather(uint64_t nnzb, const uint64_t *map_ptr, const uint32_t 
     const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nnzb) return;
     double a[S * S], c[S * S];
+    const uint64_t k0 = map_ptr[b], k1 = map_ptr[b + 1];
+    // the first contribution enters as sc*K: from a = c = 0 the update gives
+    // y = sc*K, t = y, c = (y - 0) - y = 0 exactly, so nothing else is computed
+    // for it (most blocks have one or two contributions; FP64 issue bounds this kernel)
+    if (k0 < k1) {
+        const uint32_t blk = map[k0];
+        const double sc = scale ? scale[blk_elem[blk]] : 1.0;
+        const double *src = ke + (uint64_t)blk * S * S;
 #pragma unroll
-    for (int q = 0; q < S * S; q++) { a[q] = 0.0; c[q] = 0.0; }
-    for (uint64_t k = map_ptr[b]; k < map_ptr[b + 1]; k++) {
+        for (int q = 0; q < S * S; q++) {
+            a[q] = sc * src[q];
+            c[q] = 0.0;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < S * S; q++) { a[q] = 0.0; c[q] = 0.0; }
+    }
+    for (uint64_t k = k0 + 1; k < k1; k++) {
         const uint32_t blk = map[k];
         const double sc = scale ? scale[blk_elem[blk]] : 1.0;
         const double *src = ke + (uint64_t)blk * S * S;
@@ -516,13 +531,17 @@ __global__ void k_mark_fixed(uint32_t n_bc, const uint32_t *ids, const double *v
 }
 
 // SET_FORCE_* multipliers, added in multiplier order after elimination
-// (solvers/assembly.cpp:277-283).
-__global__ void k_add_forces(uint32_t n_bc, const uint32_t *ids, const double *vals, const uint8_t *kinds,
-                             double *rhs)
+// (solvers/assembly.cpp:277-283): the force multipliers only, one thread each
+// when no DOF has two of them (no order to keep), else one thread in order.
+__global__ void k_add_forces(uint32_t n_force, const uint32_t *ids, const double *vals, int unique, double *rhs)
 {
-    if (blockIdx.x != 0 || threadIdx.x != 0 || !kinds) return;
-    for (uint32_t i = 0; i < n_bc; i++)
-        if (kinds[i] == AMIE_BC_FORCE) rhs[ids[i]] += vals[i];
+    if (unique) {
+        const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < n_force) rhs[ids[i]] += vals[i];
+        return;
+    }
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (uint32_t i = 0; i < n_force; i++) rhs[ids[i]] += vals[i];
 }
 
 // InverseDiagonal: 1/A_ii if |A_ii| > 1e-12 else 0 (sparse/sparse_matrix.cpp:216-231),
@@ -1238,8 +1257,10 @@ amie_status dirichlet_async(amie_topo *t, uint32_t n_bc, const uint32_t *ids_dev
         k_dirichlet<3><<<blocks_for(t->n_rows, 128), 128, 0, st>>>(t->n_rows, t->row_ptr.p, t->col.p, t->val.p,
                                                                  t->fixed.p, t->fixval.p, t->rhs.p);
     AMIE_LAUNCHED();
-    if (n_bc && kinds_dev) {
-        k_add_forces<<<1, 32, 0, st>>>(n_bc, ids_dev, vals_dev, kinds_dev, t->rhs.p);
+    if (t->n_force) {
+        const uint32_t nf = t->n_force;
+        k_add_forces<<<t->force_unique ? blocks_for(nf, 256) : 1, t->force_unique ? 256 : 32, 0, st>>>(
+            nf, t->force_ids.p, t->force_vals.p, t->force_unique ? 1 : 0, t->rhs.p);
         AMIE_LAUNCHED();
     }
     AMIE_CUDA(cudaGetLastError());
@@ -1396,6 +1417,24 @@ extern "C" amie_status amie_apply_dirichlet(amie_topo *t, uint32_t n_bc, const u
     AMIE_TRY(upload(t->ctx, t->bc_vals, values, n_bc));
     t->has_bc_kinds = kinds != nullptr;
     if (kinds) AMIE_TRY(upload(t->ctx, t->bc_kinds, kinds, n_bc));
+    {
+        // the force multipliers in multiplier order, and whether a DOF has two
+        std::vector<uint32_t> fid;
+        std::vector<double> fval;
+        for (uint32_t i = 0; kinds && i < n_bc; i++)
+            if (kinds[i] == AMIE_BC_FORCE) {
+                fid.push_back(ids[i]);
+                fval.push_back(values[i]);
+            }
+        std::vector<uint32_t> sorted(fid);
+        std::sort(sorted.begin(), sorted.end());
+        t->force_unique = std::adjacent_find(sorted.begin(), sorted.end()) == sorted.end();
+        t->n_force = (uint32_t)fid.size();
+        if (t->n_force) {
+            AMIE_TRY(upload(t->ctx, t->force_ids, fid.data(), fid.size()));
+            AMIE_TRY(upload(t->ctx, t->force_vals, fval.data(), fval.size()));
+        }
+    }
     t->has_rhs0 = rhs0 != nullptr;
     if (rhs0) AMIE_TRY(upload(t->ctx, t->rhs0, rhs0, t->n));
     else AMIE_CUDA(cudaMemsetAsync(t->rhs.p, 0, t->n * 8, st));

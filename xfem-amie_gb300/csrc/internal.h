@@ -257,6 +257,10 @@ struct amie_topo {
     amie::DevArray<uint8_t> bc_kinds;
     uint32_t n_bc = 0;
     bool bc_set = false, has_rhs0 = false, has_bc_kinds = false;
+    amie::DevArray<uint32_t> force_ids;   // the SET_FORCE multipliers among them, in order
+    amie::DevArray<double> force_vals;
+    uint32_t n_force = 0;
+    bool force_unique = true;             // no DOF has two force multipliers
     amie::DevArray<double> scal;   // solver scalars
     amie::DevArray<int32_t> flags; // solver control flags
 

@@ -38,6 +38,19 @@ const void *sell_dir_kernel(int s, int hint)
     return (const void *)k_sell_dir<3, T, 0>;
 }
 
+// k_sell_fused instance for the stride and the matrix-stream hint
+const void *sell_fused_kernel(int s, int hint)
+{
+    if (s == 2) {
+        if (hint == 1) return (const void *)k_sell_fused<2, float, 1>;
+        if (hint == 2) return (const void *)k_sell_fused<2, float, 2>;
+        return (const void *)k_sell_fused<2, float, 0>;
+    }
+    if (hint == 1) return (const void *)k_sell_fused<3, float, 1>;
+    if (hint == 2) return (const void *)k_sell_fused<3, float, 2>;
+    return (const void *)k_sell_fused<3, float, 0>;
+}
+
 template <bool START>
 const void *sell_cgcg_kernel(int s, int hint)
 {
@@ -91,11 +104,27 @@ struct SolverState {
     int cg_cur = 0;                  // buffer of r, w holding the current FP32 residual
     DevArray<float> r32b, w32[2], s32[2], slice3;
     cudaGraphExec_t graph_cg = nullptr;
+    // FP32 inner runs of the mixed solver as one kernel per iteration of standard
+    // PCG (k_sell_fused); opt-in (AMIE_FUSED=1).  Same iterations and accuracy as
+    // the two-kernel graph (1.2 M-DOF P2: 18,556 vs 18,619, node error 4.2e-9 vs
+    // 3.4e-9), but slower: 48.3 vs 37.0 us per iteration there (51.0 us for the
+    // kernel alone against 28.7 us for k_sell_dir), 51.1 vs 42.8 on the 64^3-voxel
+    // tetrahedra.  The update's vectors move into the bandwidth-bound SpMV (the
+    // warp's rows are SELL-permuted, so their r, q, x, D^-1 accesses scatter), its
+    // gathers read 24 instead of 16 bytes per block column, and 80 registers
+    // leave 3 CTAs per SM; that costs more than the update kernel it saves.
+    bool fused = false;
+    int grid_fused = 0;
+    int fused_cur = 0;               // direction / zw buffer of the latest run's last direction
+    DevArray<float> zw32[2];         // per node: z then w = D^-1 q (2 s floats), double-buffered
+    DevArray<double> slice5;
+    cudaGraphExec_t graph_fused = nullptr;
     ~SolverState()
     {
         if (graph64) cudaGraphExecDestroy(graph64);
         if (graph32) cudaGraphExecDestroy(graph32);
         if (graph_cg) cudaGraphExecDestroy(graph_cg);
+        if (graph_fused) cudaGraphExecDestroy(graph_fused);
         pinned_put(h_ctl, sizeof(PcgCtl));
         pinned_put(h_ring, 2 * sizeof(PcgCtl));
         for (cudaEvent_t e : ring_ev)
@@ -311,6 +340,8 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         s->grid_cgcg = std::min(resident(sell_cgcg_kernel<false>(t->s, s->matrix_hint), 0),
                                 resident(sell_cgcg_kernel<true>(t->s, s->matrix_hint), 0));
         if (const char *e = std::getenv("AMIE_CGCG")) s->cgcg = std::atoi(e) != 0;
+        s->grid_fused = resident(sell_fused_kernel(t->s, s->matrix_hint), 0);
+        if (const char *e = std::getenv("AMIE_FUSED")) s->fused = std::atoi(e) != 0;
         AMIE_CUDA(cudaGetLastError());
         AMIE_TRY(ensure_sell_partition(t, s->grid_cgcg));
         AMIE_TRY(ensure_sell_partition(t, s->grid));
@@ -320,12 +351,13 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         AMIE_TRY(ensure_sell_partition(t, s->grid_dir[1]));
         s->stride = std::max(std::max(std::max(s->grid, std::max(s->grid_vec[0], s->grid_vec[1])),
                                       std::max(s->grid_sell[0], s->grid_sell[1])),
-                             std::max(std::max(s->grid_dir[0], s->grid_dir[1]), s->grid_cgcg));
+                             std::max(std::max(s->grid_dir[0], s->grid_dir[1]),
+                                      std::max(s->grid_cgcg, s->grid_fused)));
         // tuning overrides for measurements: AMIE_PDL=0 launches the PCG graph kernels plainly,
         // AMIE_FOLD_DIR=0 keeps the separate direction kernel (three kernels per iteration)
         if (const char *e = std::getenv("AMIE_PDL")) s->pdl = std::atoi(e) != 0;
         if (const char *e = std::getenv("AMIE_FOLD_DIR")) s->fold_dir = std::atoi(e) != 0;
-        AMIE_TRY(s->parts.alloc(t->ctx, 4 * (size_t)s->stride));
+        AMIE_TRY(s->parts.alloc(t->ctx, 5 * (size_t)s->stride));   // pq | rz | rr | spare (+ the fused kernel's fifth)
         AMIE_TRY(s->ctl.alloc(t->ctx, 1));
         s->h_ctl = (PcgCtl *)pinned_get(sizeof(PcgCtl));
         s->h_ring = (PcgCtl *)pinned_get(2 * sizeof(PcgCtl));
@@ -462,6 +494,71 @@ bool use_cgcg(amie_topo *t, SolverState *s)
     return s->cgcg && s->r32b.p && t->sell32_ok && t->sell_cta_first.count(s->grid_cgcg);
 }
 
+FusedVecs<float> fused_vecs(amie_topo *t, SolverState *s)
+{
+    FusedVecs<float> v;
+    v.dinv = t->invdiag32.p;
+    v.x = t->d32.p;
+    v.r = t->r32.p;
+    v.q = t->q32.p;
+    v.p[0] = t->p32.p;
+    v.p[1] = t->p32_alt.p;
+    v.zw[0] = s->zw32[0].p;
+    v.zw[1] = s->zw32[1].p;
+    v.slice5 = s->slice5.p;
+    return v;
+}
+
+// Buffers and CTA table of the one-kernel PCG (single solves only: the server's
+// requests do not need them); false if it is off or the FP32 SELL copy is missing.
+amie_status ensure_fused(amie_topo *t, SolverState *s, bool *on)
+{
+    *on = false;
+    if (!s->fused || !t->sell32_ok || !t->r32.p) return AMIE_OK;
+    if (!s->zw32[0].p) {
+        const uint64_t n = t->n;
+        for (int k = 0; k < 2; k++) {
+            AMIE_TRY(s->zw32[k].alloc(t->ctx, 2 * n));
+            AMIE_CUDA(cudaMemsetAsync(s->zw32[k].p, 0, 2 * n * 4, t->ctx->stream));
+        }
+        AMIE_TRY(s->slice5.alloc(t->ctx, 5 * (size_t)std::max<uint32_t>(t->n_slices, 1)));
+        AMIE_TRY(ensure_sell_partition(t, s->grid_fused));
+    }
+    *on = t->sell_cta_first.count(s->grid_fused) != 0;
+    return AMIE_OK;
+}
+
+// One launch of k_sell_fused.
+void launch_fused(amie_topo *t, SolverState *s, bool pdl, cudaStream_t st)
+{
+    SellView<float> sv = sell_of<float>(t);
+    sv.prefetch_bytes = s->prefetch_bytes;
+    sv.cta_first = t->sell_cta_first.find(s->grid_fused)->second.p;
+    auto kern = (void (*)(SellView<float>, FusedVecs<float>, double *, PcgCtl *))sell_fused_kernel(t->s, s->matrix_hint);
+    launch_k(pdl, kern, s->grid_fused, 0, st, sv, fused_vecs(t, s), s->parts.p, s->ctl.p);
+    AMIE_LAUNCHED();
+}
+
+amie_status graph_fused(amie_topo *t, SolverState *s)
+{
+    if (s->graph_fused) return AMIE_OK;
+    cudaStream_t st = t->ctx->stream;
+    cudaGraph_t graph = nullptr;
+    AMIE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const uint64_t before = g_launches.load();
+    for (int it = 0; it < kGraphIters; it++) launch_fused(t, s, s->pdl && it > 0, st);
+    g_launches = before;   // captured, not launched: counted per graph launch
+    AMIE_CUDA(cudaStreamEndCapture(st, &graph));
+    cudaError_t e = cudaGraphInstantiate(&s->graph_fused, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        s->graph_fused = nullptr;
+        set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        return AMIE_CUDA_ERROR;
+    }
+    return AMIE_OK;
+}
+
 template <typename T>
 amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
 {
@@ -521,15 +618,21 @@ amie_status read_sum(amie_topo *t, const double *dev, int n, double *out)
 }
 
 // Launches the PCG graph until the control block reports done.
+// Graphs of the FP32 runs: two-kernel standard PCG, single-reduction, one-kernel PCG.
+enum class Graph { standard, cgcg, fused };
+
 template <typename T>
 amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iters, double *rr_out,
-                      bool cgcg = false)
+                      Graph kind = Graph::standard)
 {
     cudaStream_t st = t->ctx->stream;
     cudaGraphExec_t *g = sizeof(T) == 8 ? &s->graph64 : &s->graph32;
-    if (cgcg) {
+    if (kind == Graph::cgcg) {
         AMIE_TRY(graph_cgcg(t, s));
         g = &s->graph_cg;
+    } else if (kind == Graph::fused) {
+        AMIE_TRY(graph_fused(t, s));
+        g = &s->graph_fused;
     } else {
         AMIE_TRY(graph_for<T>(t, s, g));
     }
@@ -541,7 +644,7 @@ amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iter
     // check.  A launch queued after the stop finds `done` set and its kernels
     // return at once.  Each ring slot is read only after its event completed.
     const int pi = sizeof(T) == 8 ? 1 : 0;
-    const int per_iter = cgcg ? 1 : s->graph_kernels[pi];
+    const int per_iter = kind != Graph::standard ? 1 : s->graph_kernels[pi];
     auto launch = [&](int64_t k) -> amie_status {
         AMIE_CUDA(cudaGraphLaunch(*g, st));
         g_launches += per_iter * kGraphIters;
@@ -642,8 +745,36 @@ amie_status run_cgcg(amie_topo *t, SolverState *s, double scale, double tol2, in
     launch_cgcg(t, s, true, false, st);
     // the pinned copy is rewritten by drive_pcg only after this copy has completed
     AMIE_CUDA(cudaStreamSynchronize(st));
-    AMIE_TRY(drive_pcg<float>(t, s, maxit, iters, rr_out, true));
+    AMIE_TRY(drive_pcg<float>(t, s, maxit, iters, rr_out, Graph::cgcg));
     s->cg_cur = s->h_ctl->pcur;
+    return AMIE_OK;
+}
+
+// A one-kernel FP32 PCG run from the residual in r32: scale = the previous run's
+// residual scale over the new one to keep its last direction (reliable update),
+// 0 for a fresh start.
+amie_status run_fused(amie_topo *t, SolverState *s, double scale, double tol2, int64_t maxit, int64_t *iters,
+                      double *rr_out)
+{
+    cudaStream_t st = t->ctx->stream;
+    PcgCtl c = *s->h_ctl;   // the previous run's final state (rz of its last direction)
+    c.done = 0;
+    c.ticket = 0;
+    c.iterations = 0;
+    c.maxit = maxit;
+    c.tol2 = tol2;
+    c.pcur = s->fused_cur;
+    if (scale == 0.0) c.rz = 0.0;
+    *s->h_ctl = c;
+    AMIE_CUDA(cudaMemcpyAsync(s->ctl.p, s->h_ctl, sizeof(PcgCtl), cudaMemcpyHostToDevice, st));
+    const int gv = s->grid_vec[0];
+    if (t->s == 2) k_fused_prep<2, float><<<gv, kVecThreads, 0, st>>>(fused_vecs(t, s), t->n, scale, s->parts.p, s->ctl.p);
+    else k_fused_prep<3, float><<<gv, kVecThreads, 0, st>>>(fused_vecs(t, s), t->n, scale, s->parts.p, s->ctl.p);
+    AMIE_LAUNCHED();
+    // the pinned copy is rewritten by drive_pcg only after this copy has completed
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    AMIE_TRY(drive_pcg<float>(t, s, maxit, iters, rr_out, Graph::fused));
+    s->fused_cur = s->h_ctl->pcur;
     return AMIE_OK;
 }
 
@@ -723,7 +854,9 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
             // increment is added to x in FP64, r is replaced by the true FP64
             // residual and the FP32 run resumes with its search direction kept.
             const double norm = std::sqrt(rr);
-            const bool cg = use_cgcg(t, s);
+            bool fz = false;
+            AMIE_TRY(ensure_fused(t, s, &fz));
+            const bool cg = !fz && use_cgcg(t, s);
             float *r32 = cg && s->cg_cur ? s->r32b.p : t->r32.p;
             k_scale_to_f32<<<s->grid, kVecThreads, 0, st>>>(t->n, t->r.p, 1.0 / norm, r32, t->d32.p);
             AMIE_LAUNCHED();
@@ -734,7 +867,8 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
             // true residual that fell by less than half means the FP32 recursion has
             // drifted from it, and the run restarts from the new residual instead
             const bool fresh = prev_norm == 0.0 || norm > 0.5 * prev_norm;
-            if (cg) AMIE_TRY(run_cgcg(t, s, fresh ? 0.0 : prev_norm / norm, inner * inner, maxit - total, &it, &rr_in));
+            if (fz) AMIE_TRY(run_fused(t, s, fresh ? 0.0 : prev_norm / norm, inner * inner, maxit - total, &it, &rr_in));
+            else if (cg) AMIE_TRY(run_cgcg(t, s, fresh ? 0.0 : prev_norm / norm, inner * inner, maxit - total, &it, &rr_in));
             else if (fresh) AMIE_TRY(run_pcg<float>(t, s, inner * inner, maxit - total, &it, &rr_in));
             else AMIE_TRY(resume_pcg<float>(t, s, norm / prev_norm, inner * inner, maxit - total, &it, &rr_in));
             prev_norm = norm;
@@ -927,9 +1061,19 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     // the SpMV kernel of the solver graph: with the direction folded in, beta = 0.5, first buffer current;
     // for the single-reduction iteration (the mixed solver's FP32 kernel when it is on) every
     // vector it touches zeroed and a stop that never triggers
-    const bool cg = precision == 32 && use_cgcg(t, s);
+    bool fz = false;
+    if (precision == 32) AMIE_TRY(ensure_fused(t, s, &fz));
+    const bool cg = precision == 32 && !fz && use_cgcg(t, s);
     PcgCtl c{};
     c.beta = 0.5;
+    if (fz) {
+        // the one-kernel PCG iteration (the mixed solver's FP32 kernel when it is on)
+        const FusedVecs<float> v = fused_vecs(t, s);
+        for (float *q : {v.x, v.r, v.q, v.p[0], v.p[1]}) AMIE_CUDA(cudaMemsetAsync(q, 0, t->n * 4, st));
+        for (float *q : {v.zw[0], v.zw[1]}) AMIE_CUDA(cudaMemsetAsync(q, 0, 2 * t->n * 4, st));
+        c.tol2 = -1.0;
+        c.maxit = INT64_MAX;
+    }
     if (cg) {
         const CgcgVecs<float> v = cgcg_vecs(t, s);
         for (float *q : {v.x, v.p, v.r[0], v.r[1], v.w[0], v.w[1], v.s[0], v.s[1]})
@@ -943,7 +1087,9 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     const int pi = precision == 64 ? 1 : 0;
     for (int i = 0; i <= reps; i++) {   // launch 0 is a warm-up
         if (i == 1) AMIE_CUDA(cudaEventRecord(t->ctx->ev0, st));
-        if (cg) {
+        if (fz) {
+            launch_fused(t, s, false, st);
+        } else if (cg) {
             launch_cgcg(t, s, false, false, st);
         } else if (precision == 32 && fold<float>(s)) {
             launch_spmv_dir<float>(t, s->grid_dir[pi], vecs_of<float>(t), parts.pq, s->ctl.p, false, st, false,

@@ -58,7 +58,7 @@ struct PcgCtl {
     double alpha, beta, rz, rr, pq;
     double rz_prev;        // r.z of the iteration before the last one (kept for a resumed run)
     int32_t pcur;          // with two direction buffers: the one holding the latest p (0 = p, 1 = p2)
-    int32_t pad_;
+    int32_t first;         // one-kernel PCG: the next kernel starts a run (alpha = 0, not an iteration)
 };
 
 // Per-CTA partial sums.
@@ -1628,6 +1628,275 @@ __global__ void __launch_bounds__(kVecThreads, 2) k_sell_cgcg(SellView<T> A, Cgc
         }
         ctl->rz_prev = gamma_old;
         ctl->rz = bg;
+        ctl->ticket = 0;
+    }
+}
+
+
+// ------------------------------------------------------------------ one-kernel PCG iteration
+// Standard Jacobi-PCG (alpha = r.z / p.q with the explicit q = A p) in one
+// kernel per iteration, k_sell_fused.  Kernel k finishes iteration k-1 for
+// the warp's own rows (r_k = r_(k-1) - alpha q_(k-1), x += alpha p_(k-1)),
+// forms p_k = z_k + beta_k p_(k-1) for its own rows and for every column it
+// gathers, from the stored z_(k-1), w_(k-1) = D^-1 q_(k-1) and p_(k-1):
+// z_k = z_(k-1) - alpha w_(k-1), the same expression in every warp, so the
+// gathered and the stored p_k agree bit for bit.  It computes q_k = A p_k and
+// stores, interleaved per node, z_k = D^-1 r_k and w_k = D^-1 q_k for the next
+// kernel (z is re-formed from r every iteration, so it does not drift from
+// D^-1 r).  One ordered reduction gives p.q, q.z, q.w, r.z and r.r; the last
+// CTA sets alpha_k = r.z / p.q and, since beta_(k+1) is needed before the
+// kernel that could reduce r_(k+1).z_(k+1) runs, takes that dot from the
+// identity r_(k+1) = r_k - alpha_k q_k:
+//   r_(k+1).z_(k+1) = r_k.z_k - 2 alpha_k q_k.z_k + alpha_k^2 q_k.w_k,
+// with r_k.z_k the exact dot of this kernel (the expansion's rounding enters
+// one beta and does not accumulate).  p and zw are double-buffered (gathered
+// while being rewritten); r, q and x are touched by their own rows only.  The
+// first kernel of a run (ctl->first) runs with alpha = 0 on the state
+// k_fused_prep set up: zw = (D^-1 r, 0), q = 0, p = the kept direction scaled
+// (or 0), beta from the residual's r.z.
+template <typename T>
+struct FusedVecs {
+    const T *dinv;
+    T *x, *r, *q;   // own rows only
+    T *p[2];        // direction (gathered)
+    T *zw[2];       // per node: z (S entries), then w (S entries) (gathered)
+    double *slice5; // [5 * n_slices]: p.q, q.z, q.w, r.z, r.r partials of each slice
+};
+
+// S entries of a node's z and w (2S contiguous values of an interleaved buffer).
+template <int S, typename T>
+__device__ __forceinline__ void load_zw(const T *__restrict__ zw, uint32_t c, T z[S], T w[S])
+{
+    if constexpr (S == 2 && sizeof(T) == 4) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(zw) + c);
+        z[0] = a.x; z[1] = a.y; w[0] = a.z; w[1] = a.w;
+    } else {
+#pragma unroll
+        for (int q = 0; q < S; q++) {
+            z[q] = __ldg(zw + (uint64_t)c * 2 * S + q);
+            w[q] = __ldg(zw + (uint64_t)c * 2 * S + S + q);
+        }
+    }
+}
+
+// p_k of one entry from z_(k-1), w_(k-1), p_(k-1).
+template <typename T>
+__device__ __forceinline__ T fused_dir(T z, T w, T p, T al, T bt)
+{
+    return fma(bt, p, fma(-al, w, z));
+}
+
+template <int S, typename T, int HINT = kMatrixHint>
+__global__ void __launch_bounds__(kVecThreads) k_sell_fused(SellView<T> A, FusedVecs<T> v, double *part, PcgCtl *ctl)
+{
+    __shared__ double sh[5 * (kVecThreads >> 5)];
+    __shared__ int flag;
+    __shared__ uint32_t next_sl;
+    if (A.prefetch_bytes && threadIdx.x == 0) {
+        // the matrix does not change during a solve: stream the head of this CTA's
+        // slot range into L2 while the predecessor finishes (as k_sell_dir)
+        const uint32_t sb = __ldg(A.cta_first + blockIdx.x), se = __ldg(A.cta_first + blockIdx.x + 1);
+        const uint64_t g0 = __ldg(A.slice_ptr + sb), g1 = __ldg(A.slice_ptr + se);
+        const uint64_t vfull = (g1 - g0) * (S * S * sizeof(T)), cfull = (g1 - g0) * 4;
+        const uint64_t vcap = A.prefetch_bytes, ccap = A.prefetch_bytes / (S * S);
+        const uint64_t vb = (vfull < vcap ? vfull : vcap) & ~uint64_t(15);
+        const uint64_t cbytes = (cfull < ccap ? cfull : ccap) & ~uint64_t(15);
+        if (vb) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(A.val + g0 * (S * S)), "r"((uint32_t)vb) : "memory");
+        if (cbytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(A.col + g0), "r"((uint32_t)cbytes) : "memory");
+    }
+    pdl_wait();
+    pdl_release();
+    if (ctl->done) return;
+    constexpr int U = kSpmvUnroll;
+    constexpr uint32_t WPB = kVecThreads / 32;
+    const uint32_t lane = threadIdx.x & 31;
+    const int cur = ctl->pcur;
+    const T al = (T)ctl->alpha;
+    const T bt = (T)ctl->beta;
+    const T *__restrict__ pold = cur ? v.p[1] : v.p[0];
+    T *__restrict__ pnew = cur ? v.p[0] : v.p[1];
+    const T *__restrict__ zwo = cur ? v.zw[1] : v.zw[0];
+    T *__restrict__ zwn = cur ? v.zw[0] : v.zw[1];
+    const uint32_t s_beg = __ldg(A.cta_first + blockIdx.x), s_end = __ldg(A.cta_first + blockIdx.x + 1);
+    const uint64_t pol = stream_policy<HINT>();
+    if (threadIdx.x == 0) next_sl = s_beg + WPB;
+    __syncthreads();
+    for (uint32_t sl = s_beg + (threadIdx.x >> 5); sl < s_end;) {
+        const uint32_t row = __ldg(A.perm + (uint64_t)sl * 32 + lane);
+        const uint64_t g0 = __ldg(A.slice_ptr + sl);
+        const uint32_t len = (uint32_t)((__ldg(A.slice_ptr + sl + 1) - g0) >> 5);
+        T acc[S];
+#pragma unroll
+        for (int r = 0; r < S; r++) acc[r] = T(0);
+        uint32_t c[U];
+        T blk[U][S * S];
+        for (uint32_t j0 = 0; j0 < len; j0 += U) {
+            load_sell_group<S, U, T, HINT>(A, g0, j0, len, lane, c, blk, pol);
+            T zv[U][S], wv[U][S], pv[U][S];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+                    load_zw<S, T>(zwo, c[u], zv[u], wv[u]);
+                    load_x<S, T>(pold, c[u], pv[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (j0 + u < len) {
+#pragma unroll
+                    for (int cc = 0; cc < S; cc++) {
+                        const T pn = fused_dir<T>(zv[u][cc], wv[u][cc], pv[u][cc], al, bt);
+#pragma unroll
+                        for (int r = 0; r < S; r++) acc[r] = fma(blk[u][r * S + cc], pn, acc[r]);
+                    }
+                }
+            }
+        }
+        T dpq = T(0), dqz = T(0), dqw = T(0), drz = T(0), drr = T(0);
+        if (row < A.n_rows) {
+            T zo[S], wo[S];
+            load_zw<S, T>(zwo, row, zo, wo);
+#pragma unroll
+            for (int r = 0; r < S; r++) {
+                const uint64_t i = (uint64_t)row * S + r;
+                const T po = pold[i];
+                const T pn = fused_dir<T>(zo[r], wo[r], po, al, bt);
+                const T rk = fma(-al, v.q[i], v.r[i]);
+                const T d = v.dinv[i];
+                const T qk = acc[r];
+                const T zk = d * rk, wk = d * qk;
+                pnew[i] = pn;
+                v.r[i] = rk;
+                v.x[i] = fma(al, po, v.x[i]);
+                v.q[i] = qk;
+                zwn[(uint64_t)row * 2 * S + r] = zk;
+                zwn[(uint64_t)row * 2 * S + S + r] = wk;
+                dpq = fma(pn, qk, dpq);
+                dqz = fma(qk, zk, dqz);
+                dqw = fma(qk, wk, dqw);
+                drz = fma(rk, zk, drz);
+                drr = fma(rk, rk, drr);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            dpq += __shfl_xor_sync(0xffffffffu, dpq, o);
+            dqz += __shfl_xor_sync(0xffffffffu, dqz, o);
+            dqw += __shfl_xor_sync(0xffffffffu, dqw, o);
+            drz += __shfl_xor_sync(0xffffffffu, drz, o);
+            drr += __shfl_xor_sync(0xffffffffu, drr, o);
+        }
+        if (lane == 0) {
+            double *o5 = v.slice5 + 5 * (uint64_t)sl;
+            o5[0] = (double)dpq;
+            o5[1] = (double)dqz;
+            o5[2] = (double)dqw;
+            o5[3] = (double)drz;
+            o5[4] = (double)drr;
+        }
+        uint32_t nx = 0;
+        if (lane == 0) nx = atomicAdd(&next_sl, 1u);
+        sl = __shfl_sync(0xffffffffu, nx, 0);
+    }
+    __syncthreads();   // the CTA's slice partials are visible to all its threads
+    double a5[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (uint32_t i = s_beg + threadIdx.x; i < s_end; i += kVecThreads) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) a5[k] += v.slice5[5 * (uint64_t)i + k];
+    }
+    constexpr int NW = kVecThreads >> 5;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        a5[k] = warp_sum(a5[k]);
+        if (l == 0) sh[k * NW + w] = a5[k];
+    }
+    __syncthreads();
+    const uint32_t nb = gridDim.x;
+    if (threadIdx.x < 5) {
+        double t = 0.0;
+        for (int k = 0; k < NW; k++) t += sh[threadIdx.x * NW + k];
+        part[threadIdx.x * nb + blockIdx.x] = t;
+    }
+    if (!last_cta(&ctl->ticket, &flag, nb)) return;
+#pragma unroll
+    for (int k = 0; k < 5; k++) a5[k] = 0.0;
+    for (uint32_t i = threadIdx.x; i < nb; i += kVecThreads) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) a5[k] += __ldcg(part + k * nb + i);
+    }
+    __syncthreads();   // sh is reused
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        a5[k] = warp_sum(a5[k]);
+        if (l == 0) sh[k * NW + w] = a5[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t5[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            t5[k] = 0.0;
+            for (int j = 0; j < NW; j++) t5[k] += sh[k * NW + j];
+        }
+        const double pq = t5[0], qz = t5[1], qw = t5[2], rz = t5[3], rr = t5[4];
+        const bool first = ctl->first != 0;
+        const int64_t it = ctl->iterations + (first ? 0 : 1);
+        ctl->first = 0;
+        ctl->iterations = it;
+        ctl->rr = rr;
+        ctl->pq = pq;
+        const bool stop = rr <= ctl->tol2 || it >= ctl->maxit || !(rr == rr);
+        if (stop) {
+            // x, r are those of this step; p[pcur] is the last direction x moved
+            // along and ctl->rz its r.z (kept for a resumed run)
+            ctl->done = 1;
+            ctl->rz_prev = rz;
+        } else {
+            const double alpha = pq != 0.0 ? rz / pq : 0.0;
+            const double rz_next = rz - 2.0 * alpha * qz + alpha * alpha * qw;
+            ctl->alpha = alpha;
+            ctl->beta = (rz != 0.0 && rz_next > 0.0) ? rz_next / rz : 0.0;
+            ctl->rz = rz;
+            ctl->pcur = cur ^ 1;
+        }
+        ctl->ticket = 0;
+    }
+}
+
+// Set-up of a one-kernel PCG run on the residual in v.r: zw[pcur] = (D^-1 r, 0),
+// q = 0, p[pcur] *= scale (0: a fresh run, p = 0).  Partials of r.z; the last
+// CTA sets beta = r.z / (ctl->rz scale^2) for a kept direction (ctl->rz: the
+// r.z of the previous run's last direction, in that run's scale), else 0.
+template <int S, typename T>
+__global__ void __launch_bounds__(kVecThreads) k_fused_prep(FusedVecs<T> v, uint64_t n, double scale, double *part,
+                                                            PcgCtl *ctl)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    const int cur = ctl->pcur;
+    T *__restrict__ p = cur ? v.p[1] : v.p[0];
+    T *__restrict__ zw = cur ? v.zw[1] : v.zw[0];
+    double drz = 0.0;
+    for (uint64_t i = (uint64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kVecThreads) {
+        const uint64_t node = i / S, comp = i - node * S;
+        const T ri = v.r[i];
+        const T zi = v.dinv[i] * ri;
+        zw[node * 2 * S + comp] = zi;
+        zw[node * 2 * S + S + comp] = T(0);
+        v.q[i] = T(0);
+        p[i] = scale != 0.0 ? (T)(scale * (double)p[i]) : T(0);
+        drz += (double)ri * (double)zi;
+    }
+    const double b = block_sum(drz, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = b;
+    if (!last_cta(&ctl->ticket, &flag, gridDim.x)) return;
+    const double rz = ordered_sum(part, gridDim.x, sh);
+    if (threadIdx.x == 0) {
+        const double old = ctl->rz * scale * scale;
+        ctl->beta = (scale != 0.0 && old != 0.0) ? rz / old : 0.0;
+        ctl->alpha = 0.0;
+        ctl->first = 1;
         ctl->ticket = 0;
     }
 }
