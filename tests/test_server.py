@@ -86,6 +86,43 @@ def test_alone_equals_mix(gpu_ctx, monkeypatch, solver):
         t.close()
 
 
+@pytest.mark.parametrize("solver", ["mixed", "fp64"])
+def test_3d_requests_in_a_2d_mix(gpu_ctx, solver):
+    """Tetrahedral (3x3-block) requests batch with triangle requests: a batch with a
+    3D slot runs the kernels that hold both strides' bodies; each result equals
+    the same request served alone (1e-12) and a plain FP64 solve (1e-8)."""
+    import amie_gpu as G
+    import workloads as W
+    sv = G.SOLVER_PCG_FP64 if solver == "fp64" else G.SOLVER_PCG_MIXED
+    reqs = [W.voxel_cube(nv=6, seed=11)[:2], W.homogenisation_request(8000, 0.4, seed=7)[:2],
+            W.voxel_cube(nv=9, seed=12)[:2]]
+    alone = []
+    for m, bcs in reqs:
+        srv = G.Server(gpu_ctx, solver=sv, rtol=1e-10)
+        t = srv.submit(m, *bcs)
+        assert srv.drain(60.0) == G.AMIE_OK
+        (res, x), = _wait(srv, [t]).values()
+        assert res["status"] == G.AMIE_OK and res["relres"] <= 1e-10
+        alone.append(x)
+        srv.stop()
+    srv = G.Server(gpu_ctx, solver=sv, rtol=1e-10)
+    tickets = [srv.submit(m, *bcs) for _ in range(2) for m, bcs in reqs]
+    assert srv.drain(120.0) == G.AMIE_OK
+    res = _wait(srv, tickets)
+    for i, t in enumerate(tickets):
+        r, x = res[t]
+        assert r["status"] == G.AMIE_OK and r["relres"] <= 1e-10
+        assert rel(x, alone[i % len(reqs)]) <= 1e-12
+    srv.stop()
+    for (m, bcs), x in zip(reqs, alone):
+        t = G.Topology(gpu_ctx, m)
+        t.assemble()
+        t.apply_dirichlet(*bcs)
+        xr, st = t.solve(G.SOLVER_PCG_FP64, rtol=1e-12)
+        assert rel(x, xr) <= 1e-8
+        t.close()
+
+
 def test_failure_statuses(gpu_ctx):
     import amie_gpu as G
     (m, bcs, _), (m2, bcs2, _) = _requests()[:2]

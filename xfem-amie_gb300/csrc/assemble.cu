@@ -92,12 +92,10 @@ __device__ __forceinline__ void quad_default(int kind, const double *C, const do
 #pragma unroll
                 for (int r = 0; r < DIM; r++)
 #pragma unroll
-                    for (int c = 0; c < DIM; c++) {
-                        double a = 0.0;
+                    for (int c = 0; c < DIM; c++)
 #pragma unroll
-                        for (int k = 0; k < B::N; k++) a += d[i][g][B::comp(r, k)] * cb[g][B::col(r, k)][c];
-                        acc[r * DIM + c] += a;
-                    }
+                        for (int k = 0; k < B::N; k++)
+                            acc[r * DIM + c] = fma(d[i][g][B::comp(r, k)], cb[g][B::col(r, k)][c], acc[r * DIM + c]);
             double *Kij = K + (size_t)(i * NF + j) * DIM * DIM;
             double *Kji = K + (size_t)(j * NF + i) * DIM * DIM;
 #pragma unroll

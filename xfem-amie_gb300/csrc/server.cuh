@@ -62,6 +62,8 @@ struct SlotDesc {
     int32_t c0, c1;          // CTA range in the batch grid
     int32_t active;          // 1 = iterate
     int32_t mixed;
+    int32_t s;               // DOF per node: 2 (triangles) or 3 (tetrahedra)
+    int32_t pad_;
 };
 
 template <typename T>
@@ -91,8 +93,11 @@ __device__ __forceinline__ const SlotDesc *slot_of(const SlotDesc *slots, const 
 }
 
 // Batched kernel A (mixed): per slot, p = z + beta p folded into q = A p, p.q,
-// alpha -- the single-solve k_sell_dir on the slot's own CTAs.
-template <typename T>
+// alpha -- the single-solve k_sell_dir on the slot's own CTAs.  SMAX = 2: 2D
+// slots only; 3: the body of each slot's stride (the batch then has 3D slots;
+// a kernel holding both bodies needs more registers, so 2D-only batches keep
+// the smaller one).
+template <typename T, int SMAX = 2>
 __global__ void __launch_bounds__(kVecThreads) kb_sell_dir(const SlotDesc *slots, const int16_t *cta_slot)
 {
     // the slot table is the host's, fixed for the whole batch graph: look the
@@ -104,11 +109,12 @@ __global__ void __launch_bounds__(kVecThreads) kb_sell_dir(const SlotDesc *slots
     pdl_release();
     if (!live || d->ctl->done) return;
     const Cta c{blockIdx.x - (uint32_t)d->c0, (uint32_t)(d->c1 - d->c0)};
-    sell_dir_body<2, T>(slot_A<T>(*d), slot_v<T>(*d), d->parts.pq, d->ctl, true, c);
+    if (SMAX == 3 && d->s == 3) sell_dir_body<3, T>(slot_A<T>(*d), slot_v<T>(*d), d->parts.pq, d->ctl, true, c);
+    else sell_dir_body<2, T>(slot_A<T>(*d), slot_v<T>(*d), d->parts.pq, d->ctl, true, c);
 }
 
-// Batched kernel A (FP64): per slot q = A p, p.q, alpha.
-template <typename T>
+// Batched kernel A (FP64): per slot q = A p, p.q, alpha (SMAX as kb_sell_dir).
+template <typename T, int SMAX = 2>
 __global__ void __launch_bounds__(kVecThreads) kb_sell_pq(const SlotDesc *slots, const int16_t *cta_slot)
 {
     __shared__ double sh[33];
@@ -120,7 +126,10 @@ __global__ void __launch_bounds__(kVecThreads) kb_sell_pq(const SlotDesc *slots,
     const SlotDesc *d = slot_of(slots, cta_slot, &c);
     if (!d) return;
     const PcgVecs<T> &v = slot_v<T>(*d);
-    sell_pq_body<2, kSpmvUnroll, false, T, 0>(slot_A<T>(*d), v.p, v.q, d->parts.pq, d->ctl, sh, &flag, &next_sl, c);
+    if (SMAX == 3 && d->s == 3)
+        sell_pq_body<3, kSpmvUnroll, false, T, 0>(slot_A<T>(*d), v.p, v.q, d->parts.pq, d->ctl, sh, &flag, &next_sl, c);
+    else
+        sell_pq_body<2, kSpmvUnroll, false, T, 0>(slot_A<T>(*d), v.p, v.q, d->parts.pq, d->ctl, sh, &flag, &next_sl, c);
 }
 
 // Batched kernel B: per slot x, r, z updates, r.z, r.r; last CTA of the slot:
@@ -374,15 +383,10 @@ __global__ void __launch_bounds__(kVecThreads) kb_accumulate(const SlotDesc *slo
 
 constexpr int kResidualGroup = 4;   // lanes per block row in kb_residual
 
-// r = b - A x in FP64 over the slot's CTAs, |r|^2 in CTA order; the slot's last
-// CTA counts the run's iterations and decides what follows.
-__global__ void __launch_bounds__(kVecThreads) kb_residual(const SlotDesc *slots, const int16_t *cta_slot)
+// This CTA's part of r = b - A x for a slot of stride S and its partial |r|^2.
+template <int S>
+__device__ __forceinline__ double residual_rows(const SlotDesc *d, Cta c)
 {
-    __shared__ double sh[33];
-    __shared__ int flag;
-    Cta c;
-    const SlotDesc *d = slot_stopped(slots, cta_slot, kRunIterating, &c);
-    if (!d) return;
     constexpr int G = kResidualGroup;
     constexpr int RPB = kVecThreads / G;
     const BsrView<double> &A = d->v64.A;
@@ -395,17 +399,30 @@ __global__ void __launch_bounds__(kVecThreads) kb_residual(const SlotDesc *slots
         const uint32_t row = base + threadIdx.x / G;
         const bool valid = row < A.n_rows;
         const uint32_t rb = valid ? __ldg(A.row_ptr + row) : 0u, re = valid ? __ldg(A.row_ptr + row + 1) : 0u;
-        double acc[2];
-        row_spmv<2, G, double>(A, x, rb, re, lane, acc);
+        double acc[S];
+        row_spmv<S, G, double>(A, x, rb, re, lane, acc);
         if (valid && lane == 0) {
 #pragma unroll
-            for (int k = 0; k < 2; k++) {
-                const double y = b[(uint64_t)row * 2 + k] - acc[k];
-                r[(uint64_t)row * 2 + k] = y;
+            for (int k = 0; k < S; k++) {
+                const double y = b[(uint64_t)row * S + k] - acc[k];
+                r[(uint64_t)row * S + k] = y;
                 dot += y * y;
             }
         }
     }
+    return dot;
+}
+
+// r = b - A x in FP64 over the slot's CTAs, |r|^2 in CTA order; the slot's last
+// CTA counts the run's iterations and decides what follows.
+__global__ void __launch_bounds__(kVecThreads) kb_residual(const SlotDesc *slots, const int16_t *cta_slot)
+{
+    __shared__ double sh[33];
+    __shared__ int flag;
+    Cta c;
+    const SlotDesc *d = slot_stopped(slots, cta_slot, kRunIterating, &c);
+    if (!d) return;
+    double dot = d->s == 3 ? residual_rows<3>(d, c) : residual_rows<2>(d, c);
     dot = block_sum(dot, sh);
     if (threadIdx.x == 0) d->parts.spare[c.id] = dot;
     PcgCtl *ctl = d->ctl;
@@ -595,7 +612,9 @@ struct amie_server {
     amie::SlotRun *h_ring = nullptr;             // pinned, 2 x slots: d_run after each of two batches in flight
     cudaEvent_t ring_ev[2] = {nullptr, nullptr};
     int16_t *h_cta_slot = nullptr;               // pinned
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;    // batch of 2D slots
+    cudaGraphExec_t graph3 = nullptr;   // batch with 3D slots (each kernel holds both strides' bodies)
+    int n_active3 = 0;                  // active 3D slots (loop thread)
     std::string error;
     amie_server_stats stats{};   // written by the loop thread under `mu`
 };
@@ -658,8 +677,9 @@ struct ServerOps {
         amie_topo *t = nullptr;
         AMIE_TRY(amie_topology_build(adm, &r->mesh, &t));
         r->topo = t;
-        if (t->s != 2) {
-            set_error("the server batches 2D meshes only");
+        if (t->s != 2 && (t->s != 3 || srv->persistent)) {
+            set_error(srv->persistent ? "the persistent batch takes 2D meshes only"
+                                      : "the server batches 2D and 3D elasticity meshes only");
             return AMIE_BAD_INPUT;
         }
         AMIE_TRY(amie_assemble(t));
@@ -728,6 +748,7 @@ struct ServerOps {
         d.c1 = c1;
         d.active = 1;
         d.mixed = srv->mixed ? 1 : 0;
+        d.s = t->s;
     }
 
     // FP32 residual reduction between two FP64 residual replacements of a mixed slot.
@@ -782,6 +803,7 @@ struct ServerOps {
             srv->h_cta_slot[c0 + count - 1] = -1;   // test hook: one CTA of the slot is not launched
         srv->slot_req[slot] = r;
         r->slot = slot;
+        if (r->topo->s == 3) srv->n_active3++;
         {
             std::lock_guard<std::mutex> lk(srv->mu);
             srv->n_active++;
@@ -834,6 +856,7 @@ struct ServerOps {
             AMIE_CUDA(cudaMemcpyAsync(srv->d_cta_slot.p, srv->h_cta_slot, srv->grid * sizeof(int16_t), cudaMemcpyHostToDevice, st));
             srv->slot_req[slot] = nullptr;
             r->slot = -1;
+            if (t && t->s == 3) srv->n_active3--;
             std::lock_guard<std::mutex> lk(srv->mu);
             srv->n_active--;
         }
@@ -883,7 +906,11 @@ struct ServerOps {
         return AMIE_OK;
     }
 
-    static amie_status capture(amie_server *srv)
+    // The batch graphs: `iters_per_launch` PCG iterations over every active slot,
+    // then the refinement kernels; SMAX = 2 for batches of 2D slots, 3 when 3D
+    // slots are active.
+    template <int SMAX>
+    static amie_status capture_one(amie_server *srv, cudaGraphExec_t *out)
     {
         cudaStream_t st = srv->ctx->stream;
         const SlotDesc *sl = srv->d_slots.p;
@@ -894,23 +921,30 @@ struct ServerOps {
         for (int it = 0; it < srv->cfg.iters_per_launch; it++) {
             const bool pdl = it > 0;   // the first kernel follows the host's updates in plain stream order
             if (srv->mixed) {
-                launch_k(pdl, kb_sell_dir<float>, g, 0, st, sl, cs);
+                launch_k(pdl, kb_sell_dir<float, SMAX>, g, 0, st, sl, cs);
                 launch_k(true, kb_update<float>, g, 0, st, sl, cs);
             } else {
-                launch_k(pdl, kb_sell_pq<double>, g, 0, st, sl, cs);
+                launch_k(pdl, kb_sell_pq<double, SMAX>, g, 0, st, sl, cs);
                 launch_k(true, kb_update<double>, g, 0, st, sl, cs);
                 launch_k(true, kb_direction<double>, g, 0, st, sl, cs);
             }
         }
         launch_refine(srv, st);
         AMIE_CUDA(cudaStreamEndCapture(st, &graph));
-        cudaError_t e = cudaGraphInstantiate(&srv->graph, graph, 0);
+        cudaError_t e = cudaGraphInstantiate(out, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
+            *out = nullptr;
             set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
             return AMIE_CUDA_ERROR;
         }
         return AMIE_OK;
+    }
+
+    static amie_status capture(amie_server *srv)
+    {
+        AMIE_TRY(capture_one<2>(srv, &srv->graph));
+        return capture_one<3>(srv, &srv->graph3);
     }
 
     static bool any_active(amie_server *srv)
@@ -1014,7 +1048,7 @@ struct ServerOps {
             cudaMemcpyAsync(srv->h_err, srv->d_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
             launch_refine(srv, st);
         } else {
-            cudaGraphLaunch(srv->graph, st);
+            cudaGraphLaunch(srv->n_active3 > 0 ? srv->graph3 : srv->graph, st);
             g_launches += (srv->mixed ? 2 : 3) * srv->cfg.iters_per_launch;
         }
         g_launches += refine_kernels(srv);
@@ -1413,6 +1447,7 @@ extern "C" amie_status amie_server_stop(amie_server *srv)
     amie::set_free_stream(nullptr);
     cudaStreamSynchronize(srv->ctx->stream);
     if (srv->graph) cudaGraphExecDestroy(srv->graph);
+    if (srv->graph3) cudaGraphExecDestroy(srv->graph3);
     if (srv->h_slots) cudaFreeHost(srv->h_slots);
     if (srv->h_ctl) cudaFreeHost(srv->h_ctl);
     if (srv->h_err) cudaFreeHost(srv->h_err);
