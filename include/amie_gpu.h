@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define AMIE_GPU_ABI_VERSION 1
+#define AMIE_GPU_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define AMIE_API __attribute__((visibility("default")))
@@ -51,7 +51,7 @@ typedef enum amie_status {
 /* Element kinds (TriElement LINEAR / QUADRATIC, TetrahedralElement LINEAR). */
 enum { AMIE_TRI3 = 1, AMIE_TRI6 = 2, AMIE_TET4 = 3 };
 /* Enrichment function kinds. */
-enum { AMIE_ENR_TABULATED = 0, AMIE_ENR_HEAVISIDE = 1 };
+enum { AMIE_ENR_TABULATED = 0, AMIE_ENR_HEAVISIDE = 1, AMIE_ENR_TIP = 2 };
 /* Multiplier kinds: displacement (SET_ALONG_* / FIX_ALONG_*, eliminated) or
  * nodal force (SET_FORCE_*, added to the right-hand side). */
 enum { AMIE_BC_DISPLACEMENT = 0, AMIE_BC_FORCE = 1 };
@@ -104,6 +104,18 @@ typedef struct amie_mesh {
     uint64_t n_enr_gp;           /* entries of enr_jump / enr_grad (per dim) */
     const int8_t *enr_jump;      /* Heaviside: H(x_g) - H(x_k), per (function, GP) */
     const double *enr_grad;      /* Tabulated: local gradient, dim per (function, GP) */
+    /* Tip branch functions of BranchedCrack::enrichTip (features/crack.cpp:898-960):
+     * N_v^{P1} (F_j(x) - F_j(x_v)), F = sqrt(r) {sin(t/2), cos(t/2), sin(t/2) sin t,
+     * cos(t/2) sin t}, r and t about the tip in the frame of the crack direction
+     * (t as the reference's atan2 token gives it, see the implementation), on
+     * straight-sided 2D elements; evaluated with their exact gradients at every
+     * Gauss point (the reference differentiates them numerically, the two agree
+     * to ~2e-9).  enr_data[f] of an AMIE_ENR_TIP function indexes a record of 8
+     * doubles in enr_tip: x(0,0) - x_tip (2), dx/dxi (2), dx/deta (2) of the
+     * element's map x(xi, eta) = x(0,0) + xi dx/dxi + eta dx/deta, the crack
+     * angle at the tip, and the branch j (0..3). */
+    const double *enr_tip;       /* [8 * n_enr_tip] or NULL */
+    uint32_t n_enr_tip;
 } amie_mesh;
 
 typedef struct amie_solve_opts {

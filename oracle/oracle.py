@@ -52,10 +52,15 @@ def _p(a):
 
 
 def _mesh_struct(m):
+    # tip branch functions enter the C oracle tabulated (with_tabulated_tips); the
+    # converted mesh is kept on the struct so that its arrays outlive the call
+    if getattr(m, "enr_tip", None) is not None and len(m.enr_tip):
+        m = with_tabulated_tips(m)
     s = _OracleMesh(m.dim, m.stride, m.n_elem, m.ndofmax)
     for name in ("kind", "dof_ptr", "dof_ids", "gp_ptr", "gp", "jinv", "moved", "jinv_gp", "mat", "cmat_table", "cscale", "scale",
                  "enr_ptr", "enr_type", "enr_vertex", "enr_data", "enr_jump", "enr_grad"):
         setattr(s, name, _p(getattr(m, name)))
+    s._keep = m
     return s
 
 
@@ -215,3 +220,73 @@ def damage_update(law, centre, radius, score, state):
                                _p(np.ascontiguousarray(radius, np.float64)),
                                _p(np.ascontiguousarray(score, np.float64)), _p(st), _p(ch))
     return st, ch.astype(bool)
+
+
+def tip_gradients(rec, vertex, xi, eta):
+    """Local gradients (d/dxi, d/deta) of a tip branch function N_v (F_j(x) - F_j(x_v))
+    at local points (xi, eta), restated from BranchedCrack::enrichTip
+    (features/crack.cpp:898-960): F_j = sqrt(r) g_j(t), t = -atan2 of the position
+    relative to the tip in the frame of the crack angle (the sign the reference's
+    atan2 token gives), grad F = g_j grad r / (2 sqrt r) + sqrt(r) g_j'(t) grad t.
+    rec: the 8 doubles of amie_mesh.tip_record."""
+    xi = np.asarray(xi, float)
+    eta = np.asarray(eta, float)
+    a, j = rec[6], int(rec[7])
+
+    def F(s0, s1, grad):
+        dx = rec[0] + s0 * rec[2] + s1 * rec[4]
+        dy = rec[1] + s0 * rec[3] + s1 * rec[5]
+        r2 = dx * dx + dy * dy
+        r = np.sqrt(r2)
+        t = -np.arctan2(-np.sin(a) * dx + np.cos(a) * dy, np.cos(a) * dx + np.sin(a) * dy)
+        s2, c2, st, ct = np.sin(t / 2), np.cos(t / 2), np.sin(t), np.cos(t)
+        g = [s2, c2, s2 * st, c2 * st][j]
+        if not grad:
+            return np.sqrt(r) * g
+        gp = [c2 / 2, -s2 / 2, c2 / 2 * st + s2 * ct, -s2 / 2 * st + c2 * ct][j]
+        Fx = g / (2 * np.sqrt(r)) * dx / r + np.sqrt(r) * gp * dy / r2
+        Fy = g / (2 * np.sqrt(r)) * dy / r - np.sqrt(r) * gp * dx / r2
+        return np.sqrt(r) * g, Fx, Fy
+
+    vx, vy = [(0.0, 1.0), (0.0, 0.0), (1.0, 0.0)][vertex]
+    N = [eta, 1 - xi - eta, xi][vertex]
+    dN = [(0.0, 1.0), (-1.0, -1.0), (1.0, 0.0)][vertex]
+    Fg, Fx, Fy = F(xi, eta, True)
+    dF = Fg - F(vx, vy, False)
+    gxi = dN[0] * dF + N * (rec[2] * Fx + rec[3] * Fy)
+    geta = dN[1] * dF + N * (rec[4] * Fx + rec[5] * Fy)
+    return np.stack([gxi, geta], 1)
+
+
+def with_tabulated_tips(m):
+    """A copy of MeshData m whose tip branch functions (AMIE_ENR_TIP) are tabulated
+    with the gradients of tip_gradients at their element's Gauss points (the
+    oracle's element routines read tabulated gradients only)."""
+    import copy
+    import amie_mesh as am
+    out = copy.copy(m)
+    if m.enr_tip is None or not len(m.enr_tip):
+        return out
+    dim = m.dim
+    grad = [m.enr_grad.reshape(-1, dim)]
+    n_gp = len(m.enr_grad) // dim
+    enr_type = m.enr_type.copy()
+    enr_data = m.enr_data.copy()
+    gp = m.gp.reshape(-1, dim + 1)
+    for e in np.nonzero(np.diff(m.enr_ptr.astype(np.int64)))[0]:
+        pts = gp[m.gp_ptr[e]:m.gp_ptr[e + 1], :dim]
+        for f in range(m.enr_ptr[e], m.enr_ptr[e + 1]):
+            if enr_type[f] != am.ENR_TIP:
+                continue
+            rec = m.enr_tip[8 * int(m.enr_data[f]):8 * int(m.enr_data[f]) + 8]
+            grad.append(tip_gradients(rec, int(m.enr_vertex[f]), pts[:, 0], pts[:, 1]))
+            enr_type[f] = am.ENR_TABULATED
+            enr_data[f] = n_gp
+            n_gp += len(pts)
+    out.enr_type = enr_type
+    out.enr_data = enr_data
+    out.enr_grad = np.ascontiguousarray(np.concatenate(grad).reshape(-1))
+    if len(out.enr_jump) < n_gp:
+        out.enr_jump = np.concatenate([out.enr_jump, np.zeros(n_gp - len(out.enr_jump), np.int8)])
+    out.enr_tip = None
+    return out

@@ -34,7 +34,7 @@ def test_library_loads_and_exports_every_declared_symbol():
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
     lib.amie_abi_version.restype = ctypes.c_int32
-    assert lib.amie_abi_version() == 1
+    assert lib.amie_abi_version() == 2
 
 
 def test_python_binding_lists_every_symbol():

@@ -90,6 +90,7 @@ class _Mesh(C.Structure):
         ("mat", C.c_void_p), ("cmat_table", C.c_void_p), ("n_mat", C.c_uint32), ("cscale", C.c_void_p),
         ("scale", C.c_void_p), ("enr_ptr", C.c_void_p), ("enr_type", C.c_void_p), ("enr_vertex", C.c_void_p),
         ("enr_data", C.c_void_p), ("n_enr_gp", C.c_uint64), ("enr_jump", C.c_void_p), ("enr_grad", C.c_void_p),
+        ("enr_tip", C.c_void_p), ("n_enr_tip", C.c_uint32),
     ]
 
 
@@ -164,6 +165,9 @@ def mesh_struct(m: am.MeshData):
     s.n_enr_gp = len(m.enr_jump) if len(m.enr_jump) else (len(m.enr_grad) // m.dim)
     if len(m.enr_grad) // m.dim > s.n_enr_gp:
         s.n_enr_gp = len(m.enr_grad) // m.dim
+    if m.enr_tip is not None and len(m.enr_tip):
+        s.enr_tip = _p(m.enr_tip)
+        s.n_enr_tip = len(m.enr_tip) // 8
     if m.enr_ptr is not None and int(m.enr_ptr[-1]) == 0:
         s.enr_ptr = None
     return s

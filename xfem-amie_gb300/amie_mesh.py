@@ -28,7 +28,7 @@ from typing import Optional
 import numpy as np
 
 TRI3, TRI6, TET4 = 1, 2, 3
-ENR_TABULATED, ENR_HEAVISIDE = 0, 1
+ENR_TABULATED, ENR_HEAVISIDE, ENR_TIP = 0, 1, 2
 NSHAPE = {TRI3: 3, TRI6: 6, TET4: 4}
 
 # Multiplier kinds accepted by the Dirichlet step.
@@ -58,6 +58,7 @@ class MeshData:
     enr_data: Optional[np.ndarray] = None     # uint32 [n_enr]
     enr_jump: Optional[np.ndarray] = None     # int8 [n_enr_gp]
     enr_grad: Optional[np.ndarray] = None     # float64 [dim*n_enr_gp]
+    enr_tip: Optional[np.ndarray] = None      # float64 [8*n_enr_tip]: tip branch-function records
     extra: dict = field(default_factory=dict)
 
     @property
@@ -88,6 +89,8 @@ class MeshData:
         self.enr_data = np.ascontiguousarray(self.enr_data, dtype=np.uint32)
         self.enr_jump = np.ascontiguousarray(self.enr_jump, dtype=np.int8)
         self.enr_grad = np.ascontiguousarray(self.enr_grad, dtype=np.float64)
+        if self.enr_tip is not None:
+            self.enr_tip = np.ascontiguousarray(self.enr_tip, dtype=np.float64)
         if self.moved is not None:
             self.moved = np.ascontiguousarray(self.moved, dtype=np.uint8)
             self.jinv_gp = np.ascontiguousarray(self.jinv_gp, dtype=np.float64)
@@ -125,13 +128,45 @@ class MeshData:
         assert int(self.mat.max(initial=0)) < len(self.cmat_table) // (self.nv * self.nv)
 
 
-def from_golden(d, enrichment: str = "auto") -> MeshData:
+def tip_record(first, second, third, tip, angle, branch):
+    """The 8 doubles of an AMIE_ENR_TIP function of a straight-sided triangle with
+    corners first (local (0,1)), second (0,0), third (1,0): x(0,0) - tip,
+    dx/dxi, dx/deta, the crack angle at the tip, the branch index."""
+    o = np.asarray(second, float) - np.asarray(tip, float)
+    a = np.asarray(third, float) - np.asarray(second, float)
+    b = np.asarray(first, float) - np.asarray(second, float)
+    return np.array([o[0], o[1], a[0], a[1], b[0], b[1], float(angle), float(branch)])
+
+
+def tip_values(rec, vertex, xi, eta):
+    """Values of the tip branch function of `rec` attached to P1 vertex `vertex` at
+    local points (xi, eta): N_v (F_j(x) - F_j(x_v)) (BranchedCrack::enrichTip,
+    features/crack.cpp:898-960; t as the reference's atan2 token gives it)."""
+    xi = np.asarray(xi, float)
+    eta = np.asarray(eta, float)
+    a, j = rec[6], int(rec[7])
+
+    def F(s0, s1):
+        dx = rec[0] + s0 * rec[2] + s1 * rec[4]
+        dy = rec[1] + s0 * rec[3] + s1 * rec[5]
+        t = -np.arctan2(-np.sin(a) * dx + np.cos(a) * dy, np.cos(a) * dx + np.sin(a) * dy)
+        g = [np.sin(t / 2), np.cos(t / 2), np.sin(t / 2) * np.sin(t), np.cos(t / 2) * np.sin(t)][j]
+        return np.sqrt(np.hypot(dx, dy)) * g
+
+    vx, vy = [(0.0, 1.0), (0.0, 0.0), (1.0, 0.0)][vertex]
+    N = [eta, 1 - xi - eta, xi][vertex]
+    return N * (F(xi, eta) - F(vx, vy))
+
+
+def from_golden(d, enrichment: str = "auto", tips=()) -> MeshData:
     """Build MeshData from a reference fixture (tests/golden/*.npz).
 
     enrichment = "tabulated": every enrichment function carries the gradients
     the reference's VM produced (finite differences included); "auto": functions
     whose values are exactly N_k^{P1} * {-2, 0, 2} become Heaviside jumps, the
-    rest stay tabulated.
+    rest stay tabulated; "tip": as "auto", and functions whose values are those
+    of a tip branch function of one of `tips` ((x, y), angle) to 1e-12 on a
+    straight-sided triangle become AMIE_ENR_TIP records.
     """
     dim = int(d["dim"][0])
     kind = d["elem_kind"].astype(np.uint8)
@@ -148,7 +183,8 @@ def from_golden(d, enrichment: str = "auto") -> MeshData:
     enr_jump = np.zeros(int(egp[-1]) if nenr else 0, np.int8)
     enr_grad = d["enr_grad"].copy()
     enr_data = egp[:-1].astype(np.uint32) if nenr else np.zeros(0, np.uint32)
-    if nenr and enrichment == "auto":
+    tip_recs = []
+    if nenr and enrichment in ("auto", "tip"):
         g2 = gp.reshape(-1, dim + 1)
         for e in np.nonzero(np.diff(enr_ptr))[0]:
             pts = g2[gp_ptr[e]:gp_ptr[e + 1], :dim]
@@ -164,6 +200,26 @@ def from_golden(d, enrichment: str = "auto") -> MeshData:
                 if np.all(np.abs(q - r) < 1e-9) and np.all(np.isin(r, (-2, 0, 2))):
                     enr_type[j] = ENR_HEAVISIDE
                     enr_jump[egp[j]:egp[j + 1]] = r.astype(np.int8)
+                    continue
+                if enrichment != "tip" or dim != 2 or ("elem_moved" in d and d["elem_moved"][e]):
+                    continue
+                ns = 6 if kind[e] == TRI6 else 3
+                xy0 = int(np.sum(np.where(kind[:e] == TRI6, 6, 3))) * 2
+                pts_xy = d["elem_xy"][xy0:xy0 + 2 * ns].reshape(ns, 2)
+                first, second, third = pts_xy[[0, 2, 4]] if ns == 6 else pts_xy
+                scale = max(np.abs(vals).max(), 1e-300)
+                for tip, angle in tips:
+                    hit = None
+                    for br in range(4):
+                        rec = tip_record(first, second, third, tip, angle, br)
+                        if np.abs(tip_values(rec, k, pts[:, 0], pts[:, 1]) - vals).max() <= 1e-12 * scale:
+                            hit = rec
+                            break
+                    if hit is not None:
+                        enr_type[j] = ENR_TIP
+                        enr_data[j] = len(tip_recs)
+                        tip_recs.append(hit)
+                        break
     vert = d["enr_vertex"].astype(np.int64)
     vert[vert > 2] = 0
     m = MeshData(dim=dim, stride=dim, kind=kind, dof_ptr=d["elem_dof_ptr"], dof_ids=d["elem_dof_ids"],
@@ -173,7 +229,7 @@ def from_golden(d, enrichment: str = "auto") -> MeshData:
                  cmat_table=table.reshape(-1), ndofmax=int(d["ndofmax"][0]),
                  scale=d["elem_scale"], enr_ptr=enr_ptr, enr_type=enr_type,
                  enr_vertex=vert.astype(np.uint8), enr_data=enr_data, enr_jump=enr_jump,
-                 enr_grad=enr_grad)
+                 enr_grad=enr_grad, enr_tip=np.concatenate(tip_recs) if tip_recs else None)
     return m
 
 

@@ -243,20 +243,7 @@ __device__ void warp_quad_range(const MeshView &m, uint32_t e, int gb, int ge, W
             if (f < nshape) {
                 shape_grad(kind, f, p[0], p[1], lg);
             } else {
-                const uint32_t fj = f0 + (f - nshape);
-                const uint64_t off = (uint64_t)m.enr_data[fj] + g;
-                if (m.enr_type[fj] == AMIE_ENR_HEAVISIDE) {
-                    // grad(N_k^{P1} (H - H_k)) = grad N_k^{P1} * jump away from the crack
-                    // (features/crack.cpp:1316,1332,1347)
-                    const int v = m.enr_vertex[fj];
-                    const double jump = (double)m.enr_jump[off];
-                    const double gx[3] = {0.0, -1.0, 1.0}, gy[3] = {1.0, -1.0, 0.0};
-                    lg[0] = gx[v] * jump;
-                    lg[1] = gy[v] * jump;
-                } else {
-#pragma unroll
-                    for (int c = 0; c < DIM; c++) lg[c] = m.enr_grad[off * DIM + c];
-                }
+                enr_local_grad<DIM>(m, f0 + (f - nshape), g, p, lg);
             }
             const double *J = moved ? m.jinv_gp + (size_t)(g0 + g) * DIM * DIM : Je;
             double d[3];
@@ -671,18 +658,7 @@ __global__ void k_elem_forces(MeshView m, double *fstage)
             if (f < nshape) {
                 shape_grad(kind, f, p[0], p[1], lg);
             } else {
-                const uint32_t fj = f0 + (f - nshape);
-                const uint64_t off = (uint64_t)m.enr_data[fj] + g;
-                if (m.enr_type[fj] == AMIE_ENR_HEAVISIDE) {
-                    const int v = m.enr_vertex[fj];
-                    const double jump = (double)m.enr_jump[off];
-                    const double gx[3] = {0.0, -1.0, 1.0}, gy[3] = {1.0, -1.0, 0.0};
-                    lg[0] = gx[v] * jump;
-                    lg[1] = gy[v] * jump;
-                } else {
-#pragma unroll
-                    for (int c = 0; c < DIM; c++) lg[c] = m.enr_grad[off * DIM + c];
-                }
+                enr_local_grad<DIM>(m, f0 + (f - nshape), g, p, lg);
             }
             double d[3];
             phys_grad<DIM>(J, lg, d);
@@ -737,6 +713,7 @@ MeshView mesh_view(amie_topo *t)
     m.mat = t->mat.p; m.cmat_table = t->cmat_table.p; m.cscale = t->has_cscale ? t->cscale.p : nullptr;
     m.enr_ptr = t->enr_ptr.p; m.enr_type = t->enr_type.p; m.enr_vertex = t->enr_vertex.p;
     m.enr_data = t->enr_data.p; m.enr_jump = t->enr_jump.p; m.enr_grad = t->enr_grad.p;
+    m.enr_tip = t->enr_tip.p;
     m.blk_off = t->blk_off.p; m.ke = t->ke.p;
     m.imposed = t->has_imposed ? t->imposed.p : nullptr;
     return m;
@@ -792,6 +769,20 @@ amie_status validate_mesh(const amie_mesh *m, std::vector<uint32_t> &nf, uint64_
             const uint32_t ngp = m->gp_ptr[e + 1] - m->gp_ptr[e];
             const uint32_t ngp_eff = ngp ? ngp : (m->kind[e] == AMIE_TRI6 ? 4 : 1);
             for (uint32_t j = m->enr_ptr[e]; j < m->enr_ptr[e + 1]; j++) {
+                if (m->enr_type[j] == AMIE_ENR_TIP) {
+                    // a record of its own; the element's map is affine (straight sides)
+                    if (!m->enr_tip || m->enr_data[j] >= m->n_enr_tip || m->enr_vertex[j] > 2 || m->dim != 2 ||
+                        (m->moved && m->moved[e])) {
+                        set_error("element %u: bad tip enrichment function %u", e, j);
+                        return AMIE_BAD_INPUT;
+                    }
+                    const double br = m->enr_tip[(uint64_t)m->enr_data[j] * 8 + 7];
+                    if (!(br == 0.0 || br == 1.0 || br == 2.0 || br == 3.0)) {
+                        set_error("element %u: tip enrichment function %u: branch %g not in 0..3", e, j, br);
+                        return AMIE_BAD_INPUT;
+                    }
+                    continue;
+                }
                 if ((uint64_t)m->enr_data[j] + ngp_eff > m->n_enr_gp) {
                     set_error("element %u: enrichment data of function %u out of range", e, j);
                     return AMIE_BAD_INPUT;
@@ -908,6 +899,7 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
         UP(t->enr_data, mesh->enr_data, n_enr);
         if (mesh->enr_jump) UP(t->enr_jump, mesh->enr_jump, mesh->n_enr_gp);
         if (mesh->enr_grad) UP(t->enr_grad, mesh->enr_grad, mesh->n_enr_gp * t->dim);
+        if (mesh->enr_tip && mesh->n_enr_tip) UP(t->enr_tip, mesh->enr_tip, (size_t)mesh->n_enr_tip * 8);
     }
     UP(t->blk_off, blk_off.data(), E + 1);
     UP(t->simple_list, simple.data(), simple.size());

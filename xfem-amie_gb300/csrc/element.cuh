@@ -115,4 +115,72 @@ __device__ inline void bcb(const double *di, const double *dj, const double *C, 
     }
 }
 
+
+// Local gradient of one tip branch function N_v^{P1} (F_j(x) - F_j(x_v)) at
+// local coordinates (xi, eta) (BranchedCrack::enrichTip, features/crack.cpp:898-960).
+// rec: x(0,0) - x_tip, dx/dxi, dx/deta, crack angle a, branch j.  With (u, w)
+// the position relative to the tip in the frame rotated by a, the reference's
+// atan2 token gives t = -atan2(w, u) (its values of the four functions match
+// this to 1e-14); F_j = sqrt(r) g_j(t), grad F = g_j grad r / (2 sqrt r) +
+// sqrt(r) g_j'(t) grad t with grad t = (dy, -dx) / r^2.
+__device__ inline void tip_function_grad(const double *rec, int v, double xi, double eta, double lg[3])
+{
+    const double a = rec[6];
+    const int j = (int)rec[7];
+    const double ca = cos(a), sa = sin(a);
+    double F[2], Fx = 0.0, Fy = 0.0;
+    // k = 0: the Gauss point, k = 1: the vertex the function is attached to
+    const double vxi[3] = {0.0, 0.0, 1.0}, veta[3] = {1.0, 0.0, 0.0};
+    for (int k = 0; k < 2; k++) {
+        const double s0 = k ? vxi[v] : xi, s1 = k ? veta[v] : eta;
+        const double dx = rec[0] + s0 * rec[2] + s1 * rec[4];
+        const double dy = rec[1] + s0 * rec[3] + s1 * rec[5];
+        const double r2 = dx * dx + dy * dy, r = sqrt(r2), sr = sqrt(r);
+        const double t = -atan2(-sa * dx + ca * dy, ca * dx + sa * dy);
+        const double s2 = sin(0.5 * t), c2 = cos(0.5 * t), st = sin(t), ct = cos(t);
+        double g, gp;
+        if (j == 0) { g = s2; gp = 0.5 * c2; }
+        else if (j == 1) { g = c2; gp = -0.5 * s2; }
+        else if (j == 2) { g = s2 * st; gp = 0.5 * c2 * st + s2 * ct; }
+        else { g = c2 * st; gp = -0.5 * s2 * st + c2 * ct; }
+        F[k] = sr * g;
+        if (k == 0) {
+            const double gr = g / (2.0 * sr * r);   // g / (2 sqrt r) / r, times dx or dy
+            Fx = gr * dx + sr * gp * (dy / r2);
+            Fy = gr * dy - sr * gp * (dx / r2);
+        }
+    }
+    // P1 hat function of vertex v: vertex 0 at (0, 1), 1 at (0, 0), 2 at (1, 0)
+    const double N = v == 0 ? eta : (v == 1 ? 1.0 - xi - eta : xi);
+    const double dNx[3] = {0.0, -1.0, 1.0}, dNy[3] = {1.0, -1.0, 0.0};
+    const double dF = F[0] - F[1];
+    lg[0] = dNx[v] * dF + N * (rec[2] * Fx + rec[3] * Fy);
+    lg[1] = dNy[v] * dF + N * (rec[4] * Fx + rec[5] * Fy);
+    lg[2] = 0.0;
+}
+
+// Local gradient of enrichment function fj at Gauss point g of its element
+// (local coordinates p): Heaviside (closed form), tip branch (closed form) or
+// tabulated.
+template <int DIM>
+__device__ inline void enr_local_grad(const MeshView &m, uint32_t fj, uint32_t g, const double *p, double lg[3])
+{
+    const uint8_t type = m.enr_type[fj];
+    if (DIM == 2 && type == AMIE_ENR_HEAVISIDE) {
+        // grad(N_k^{P1} (H - H_k)) = grad N_k^{P1} * jump away from the crack
+        // (features/crack.cpp:1316,1332,1347)
+        const int v = m.enr_vertex[fj];
+        const double jump = (double)m.enr_jump[(uint64_t)m.enr_data[fj] + g];
+        const double gx[3] = {0.0, -1.0, 1.0}, gy[3] = {1.0, -1.0, 0.0};
+        lg[0] = gx[v] * jump;
+        lg[1] = gy[v] * jump;
+    } else if (DIM == 2 && type == AMIE_ENR_TIP) {
+        tip_function_grad(m.enr_tip + (uint64_t)m.enr_data[fj] * 8, m.enr_vertex[fj], p[0], p[1], lg);
+    } else {
+        const uint64_t off = (uint64_t)m.enr_data[fj] + g;
+#pragma unroll
+        for (int c = 0; c < DIM; c++) lg[c] = m.enr_grad[off * DIM + c];
+    }
+}
+
 }  // namespace amie

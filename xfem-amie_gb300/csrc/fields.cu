@@ -54,18 +54,7 @@ __global__ void k_element_fields(MeshView m, const double *x, double *strain, do
             if (f < nshape) {
                 shape_grad(kind, f, p[0], p[1], lg);
             } else {
-                const uint32_t fj = f0 + (f - nshape);
-                const uint64_t off = (uint64_t)m.enr_data[fj] + g;
-                if (m.enr_type[fj] == AMIE_ENR_HEAVISIDE) {
-                    const int v = m.enr_vertex[fj];
-                    const double jump = (double)m.enr_jump[off];
-                    const double gx[3] = {0.0, -1.0, 1.0}, gy[3] = {1.0, -1.0, 0.0};
-                    lg[0] = gx[v] * jump;
-                    lg[1] = gy[v] * jump;
-                } else {
-#pragma unroll
-                    for (int c = 0; c < DIM; c++) lg[c] = m.enr_grad[off * DIM + c];
-                }
+                enr_local_grad<DIM>(m, f0 + (f - nshape), g, p, lg);
             }
             double d[3];
             phys_grad<DIM>(J, lg, d);

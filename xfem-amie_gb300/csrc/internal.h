@@ -122,6 +122,7 @@ struct MeshView {
     const uint32_t *enr_data;
     const int8_t *enr_jump;
     const double *enr_grad;
+    const double *enr_tip;    // tip branch-function records (8 doubles each)
     const uint64_t *blk_off;  // first staged block of each element (in s*s blocks)
     double *ke;               // staged element matrices: nf*nf blocks of s*s, row-major
     const double *imposed;    // imposed strain per element (Voigt, nv), or null
@@ -193,7 +194,7 @@ struct amie_topo {
     // element data
     amie::DevArray<uint8_t> kind, moved, enr_type, enr_vertex;
     amie::DevArray<uint32_t> dof_ptr, dof_ids, gp_ptr, mat, enr_ptr, enr_data;
-    amie::DevArray<double> gp, jinv, jinv_gp, cmat_table, cscale, scale, enr_grad;
+    amie::DevArray<double> gp, jinv, jinv_gp, cmat_table, cscale, scale, enr_grad, enr_tip;
     amie::DevArray<int8_t> enr_jump;
     amie::DevArray<uint64_t> blk_off;
     amie::DevArray<uint32_t> simple_list, warp_list;   // elements per quadrature kernel

@@ -569,7 +569,7 @@ struct amie_server {
         // deep copies of the request arrays
         std::vector<uint8_t> kind, moved, enr_type, enr_vertex, bc_kinds;
         std::vector<uint32_t> dof_ptr, dof_ids, gp_ptr, mat, enr_ptr, enr_data, bc_ids;
-        std::vector<double> gp, jinv, jinv_gp, cmat, cscale, scale, enr_grad, bc_vals, x0;
+        std::vector<double> gp, jinv, jinv_gp, cmat, cscale, scale, enr_grad, enr_tip, bc_vals, x0;
         std::vector<int8_t> enr_jump;
         amie_mesh mesh{};
         uint64_t footprint = 0;
@@ -1335,6 +1335,7 @@ extern "C" amie_status amie_submit(amie_server *srv, const amie_request *req, ui
         copy_vec(r->enr_data, m.enr_data, nenr);
         copy_vec(r->enr_jump, m.enr_jump, m.enr_jump ? m.n_enr_gp : 0);
         copy_vec(r->enr_grad, m.enr_grad, m.enr_grad ? m.n_enr_gp * d : 0);
+        copy_vec(r->enr_tip, m.enr_tip, m.enr_tip ? (size_t)m.n_enr_tip * 8 : 0);
     }
     copy_vec(r->bc_ids, req->bc_ids, req->n_bc);
     copy_vec(r->bc_vals, req->bc_values, req->n_bc);
@@ -1359,6 +1360,7 @@ extern "C" amie_status amie_submit(amie_server *srv, const amie_request *req, ui
         r->mesh.enr_data = r->enr_data.data();
         r->mesh.enr_jump = r->enr_jump.empty() ? nullptr : r->enr_jump.data();
         r->mesh.enr_grad = r->enr_grad.empty() ? nullptr : r->enr_grad.data();
+        r->mesh.enr_tip = r->enr_tip.empty() ? nullptr : r->enr_tip.data();
     }
     uint32_t max_id = 0;
     for (uint32_t k : r->dof_ids) max_id = std::max(max_id, k);

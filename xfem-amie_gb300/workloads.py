@@ -20,7 +20,8 @@ consumes built the way the reference defines it:
   and tip branch functions sqrt(r){sin t/2, cos t/2, sin t/2 sin t, cos t/2 sin t}
   times N_k^{P1} (features/crack.cpp:919-960) on the tip element, integrated with
   512 seeded random points as the reference's Monte-Carlo fallback does
-  (mesher/delaunay.cpp:2941-2949), passed as tabulated gradients;
+  (mesher/delaunay.cpp:2941-2949), passed as AMIE_ENR_TIP records (closed form
+  on the device) or as tabulated gradients;
 * Dirichlet multipliers of BoundingBoxDefinedBoundaryCondition on the box faces.
 """
 from __future__ import annotations
@@ -196,8 +197,11 @@ def _split_triangle_by_line(P, y0):
 
 def cracked_square(N, L=0.1, order=2, n_inclusions=4000, E_matrix=25e9, E_inc=60e9, nu=0.2, rmin=1e-4,
                    rmax=2e-3, exponent=-2.5, crack_frac=0.3, disp=1e-5, seed=1, jitter=0.15, tip=True,
-                   n_mc=512):
-    """Config-1 family: P2 (or P1) square with power-law inclusions and a straight crack."""
+                   n_mc=512, tip_closed_form=True):
+    """Config-1 family: P2 (or P1) square with power-law inclusions and a straight crack.
+    The tip element's branch functions are AMIE_ENR_TIP records (evaluated with
+    their exact gradients on the device, angle 0 at the crack's end xb), or, with
+    tip_closed_form=False, gradients tabulated per Gauss point."""
     rng = np.random.default_rng(seed)
     x, y, conn, vx, vy, M = structured_triangles(N, L, order, jitter, rng)
     E_count = len(conn)
@@ -281,7 +285,14 @@ def cracked_square(N, L=0.1, order=2, n_inclusions=4000, E_matrix=25e9, E_inc=60
                 jumps = (Hg - H(x[nid], y[nid])).astype(np.int8)
                 funcs.append((am.ENR_HEAVISIDE, k, jumps))
                 ids.append(heav_id[nid])
-        if e == tip_elem:
+        if e == tip_elem and tip_closed_form:
+            corners = [(x[int(vert_ids[e, k])], y[int(vert_ids[e, k])]) for k in range(3)]
+            for k in range(3):
+                nid = int(vert_ids[e, k])
+                for fi in range(4):
+                    funcs.append((am.ENR_TIP, k, am.tip_record(corners[0], corners[1], corners[2], (xb, y0), 0.0, fi)))
+                    ids.append(tip_ids[nid] + fi)
+        elif e == tip_elem:
             Nk = [pts[:, 1], 1 - pts[:, 0] - pts[:, 1], pts[:, 0]]
             dN = [(0.0, 1.0), (-1.0, -1.0), (1.0, 0.0)]
             rx, ry = gpx - xb, gpy - y0
@@ -359,7 +370,7 @@ def cracked_square(N, L=0.1, order=2, n_inclusions=4000, E_matrix=25e9, E_inc=60
     enr_type = np.zeros(n_enr, np.uint8)
     enr_vertex = np.zeros(n_enr, np.uint8)
     enr_data = np.zeros(n_enr, np.uint32)
-    jumps_all, grads_all = [], []
+    jumps_all, grads_all, tip_recs = [], [], []
     cursor = 0
     for e in sorted(enr_functions):
         pts, wts = gp_lists[e]
@@ -374,6 +385,10 @@ def cracked_square(N, L=0.1, order=2, n_inclusions=4000, E_matrix=25e9, E_inc=60
             fj = int(enr_ptr[e]) + j
             enr_type[fj] = typ
             enr_vertex[fj] = k
+            if typ == am.ENR_TIP:   # a record, no per-point data
+                enr_data[fj] = len(tip_recs)
+                tip_recs.append(data)
+                continue
             enr_data[fj] = cursor
             if typ == am.ENR_HEAVISIDE:
                 jumps_all.append(data.astype(np.int8))
@@ -387,7 +402,7 @@ def cracked_square(N, L=0.1, order=2, n_inclusions=4000, E_matrix=25e9, E_inc=60
     m = am.MeshData(dim=2, stride=2, kind=kind, dof_ptr=dof_ptr, dof_ids=dof_ids, gp_ptr=gp_ptr, gp=gp,
                     jinv=Jinv.reshape(-1), mat=mat, cmat_table=cmat, ndofmax=next_id, enr_ptr=enr_ptr,
                     enr_type=enr_type, enr_vertex=enr_vertex, enr_data=enr_data, enr_jump=enr_jump,
-                    enr_grad=enr_grad)
+                    enr_grad=enr_grad, enr_tip=np.concatenate(tip_recs) if tip_recs else None)
     bcs = _box_bcs(x, y, L, 2, disp)
     meta = dict(n_nodes=n_nodes, n_elem=E_count, n_inclusions=len(cr), n_cut=len(cut), n_enriched=len(enr_elems),
                 tip_elem=int(tip_elem), crack_y=y0, n_dof=2 * next_id, order=order)
