@@ -121,32 +121,3 @@ def test_one_kernel_pcg_solves(gpu_ctx, monkeypatch, name):
         assert np.abs(x1[s] - xo[s]).max() <= 1e-8 * np.abs(xo[s]).max()
     finally:
         t.close()
-
-
-@pytest.mark.parametrize("name", ["incl_p1", "crack_p1"])
-def test_fp32_blocks_with_bf16_residual_solve(gpu_ctx, monkeypatch, name):
-    """AMIE_SELL_LO=1: the mixed solver's 2x2 FP32 SpMV applies every block as its
-    FP32 values plus the BF16 rounding of their residual; the solve reaches the
-    oracle's solution, repeats bit for bit, and needs no more iterations than
-    with the FP32 values alone."""
-    import amie_gpu
-    d = load_golden(name)
-    m = am.from_golden(d, "tabulated")
-    its = {}
-    for flag in ("0", "1"):
-        monkeypatch.setenv("AMIE_SELL_LO", flag)
-        t = amie_gpu.Topology(gpu_ctx, m)
-        try:
-            t.assemble()
-            t.apply_dirichlet(*am.golden_bcs(d))
-            x1, st1 = t.solve(amie_gpu.SOLVER_PCG_MIXED, rtol=1e-10)
-            x2, st2 = t.solve(amie_gpu.SOLVER_PCG_MIXED, rtol=1e-10)
-            assert st1["relres"] <= 1e-10 and relres(d, m, x1) <= 2e-10
-            assert np.array_equal(x1, x2)
-            xo, _, _, _ = O.pcg(m.stride, d["row_size"], d["column_index"], d["array"], d["rhs"], rtol=1e-13)
-            s = node_dofs(m)
-            assert np.abs(x1[s] - xo[s]).max() <= 1e-8 * np.abs(xo[s]).max()
-            its[flag] = st1["iterations"]
-        finally:
-            t.close()
-    assert its["1"] <= its["0"] * 1.05

@@ -11,7 +11,6 @@
 #include "internal.h"
 
 #include <cub/cub.cuh>
-#include <cuda_bf16.h>
 
 #include <algorithm>
 #include <chrono>
@@ -456,7 +455,9 @@ __global__ void k_gather(uint64_t nnzb, const uint64_t *map_ptr, const uint32_t 
 #pragma unroll
         for (int q = 0; q < S * S; q++) { a[q] = 0.0; c[q] = 0.0; }
     }
-    for (uint64_t k = k0 + 1; k < k1; k++) {
+    // the middle contributions with the full update; the compensation of the last
+    // one would never be used, so its update stops at a = t
+    for (uint64_t k = k0 + 1; k + 1 < k1; k++) {
         const uint32_t blk = map[k];
         const double sc = scale ? scale[blk_elem[blk]] : 1.0;
         const double *src = ke + (uint64_t)blk * S * S;
@@ -467,6 +468,13 @@ __global__ void k_gather(uint64_t nnzb, const uint64_t *map_ptr, const uint32_t 
             c[q] = (t - a[q]) - y;
             a[q] = t;
         }
+    }
+    if (k1 > k0 + 1) {
+        const uint32_t blk = map[k1 - 1];
+        const double sc = scale ? scale[blk_elem[blk]] : 1.0;
+        const double *src = ke + (uint64_t)blk * S * S;
+#pragma unroll
+        for (int q = 0; q < S * S; q++) a[q] = a[q] + (sc * src[q] - c[q]);
     }
 #pragma unroll
     for (int q = 0; q < S * S; q++) val[b * S * S + q] = a[q];
@@ -602,22 +610,6 @@ __global__ void k_to_sell(uint64_t n_slots, const uint32_t *sell_blk, const doub
         for (int c = 0; c < S * S; c++) {
             const double v = blk != kSellNone ? val[(uint64_t)blk * (S * S) + c] : 0.0;
             group[sell_off<S, T>(c, (int)lane)] = (T)v;
-        }
-    }
-}
-
-// BF16 residual of the FP32 2x2 SELL values: lo = bf16(v - float(v)), 4 per slot
-// in slot order, so that float(v) + lo carries ~32 bits of v's significand.
-__global__ void k_sell_lo(uint64_t n_slots, const uint32_t *sell_blk, const double *val, uint16_t *lo)
-{
-    for (uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; slot < n_slots;
-         slot += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t blk = sell_blk[slot];
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const double v = blk != kSellNone ? val[(uint64_t)blk * 4 + c] : 0.0;
-            const float r = (float)(v - (double)(float)v);
-            lo[slot * 4 + c] = __bfloat16_as_ushort(__float2bfloat16_rn(r));
         }
     }
 }
@@ -1184,7 +1176,6 @@ amie_status finalize_matrix_async(amie_topo *t, bool want32)
     const uint64_t n = t->n;
     t->sell64_ok = false;
     t->sell32_ok = false;
-    t->sell_lo_ok = false;
     float *inv32 = nullptr;
     if (want32) {
         if (!t->val32.p) AMIE_TRY(t->val32.alloc(t->ctx, t->nnzb * t->s * t->s));
@@ -1225,18 +1216,6 @@ amie_status ensure_sell(amie_topo *t, bool want64, bool want32)
         t->sell32_ok = true;
     }
     AMIE_CUDA(cudaGetLastError());
-    return AMIE_OK;
-}
-
-// The BF16 residual of the FP32 2x2 SELL copy (after ensure_sell's FP32 values).
-amie_status ensure_sell_lo(amie_topo *t)
-{
-    if (t->s != 2 || t->sell_lo_ok) return AMIE_OK;
-    if (!t->sell_lo.p) AMIE_TRY(t->sell_lo.alloc(t->ctx, t->n_slots * 4));
-    k_sell_lo<<<t->ctx->num_sms * 8, 256, 0, t->ctx->stream>>>(t->n_slots, t->sell_blk.p, t->val.p, t->sell_lo.p);
-    AMIE_LAUNCHED();
-    AMIE_CUDA(cudaGetLastError());
-    t->sell_lo_ok = true;
     return AMIE_OK;
 }
 

@@ -170,9 +170,6 @@ struct SellView {
     const uint32_t *cta_first;   // [grid + 1] first slice of each CTA of the launch (slot-balanced ranges)
     T *slice_dot;                // [n_slices] per-slice partial of the fused dot product (scratch)
     uint32_t prefetch_bytes = 0; // k_sell_dir: L2 prefetch of the start of each CTA's range before its wait
-    // FP32 2x2 copy: per slot the BF16 rounding of (value - FP32 value), 4 per
-    // slot in slot order (8 bytes a lane), or null; k_sell_dir<.., LO> adds it
-    const uint16_t *lo = nullptr;
 };
 
 }  // namespace amie
@@ -227,8 +224,6 @@ struct amie_topo {
     amie::DevArray<uint64_t> sell_ptr;
     amie::DevArray<double> sell_val;
     amie::DevArray<float> sell_val32;
-    amie::DevArray<uint16_t> sell_lo;                          // BF16 residual of the FP32 2x2 copy
-    bool sell_lo_ok = false;
     uint32_t n_slices = 0;
     uint64_t n_slots = 0;
     std::vector<uint64_t> h_sell_ptr;                          // host copy of sell_ptr

@@ -24,17 +24,10 @@ amie_status assemble_async(amie_topo *t);
 amie_status finalize_matrix_async(amie_topo *t, bool want32);
 amie_status amie_cg_solve(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *st);
 
-// k_sell_dir instance for the stride and the matrix-stream hint (lo: the FP32
-// 2x2 blocks plus their BF16 residual)
+// k_sell_dir instance for the stride and the matrix-stream hint
 template <typename T>
-const void *sell_dir_kernel(int s, int hint, bool lo = false)
+const void *sell_dir_kernel(int s, int hint)
 {
-    if constexpr (sizeof(T) == 4) {
-        if (lo && s == 2) {
-            if (hint == 0) return (const void *)k_sell_dir<2, T, 0, true>;
-            return (const void *)k_sell_dir<2, T, 1, true>;   // (hint 2 streams with the hint 1 loads)
-        }
-    }
     if (s == 2) {
         if (hint == 1) return (const void *)k_sell_dir<2, T, 1>;
         if (hint == 2) return (const void *)k_sell_dir<2, T, 2>;
@@ -83,9 +76,6 @@ struct SolverState {
     // gathered entry instead of one per vector entry, and FP64 issue is the
     // scarce resource of this GPU (the folded FP64 solve ran 1.4x slower)
     bool fold_dir = true;
-    // FP32 2x2 graphs apply every block as its FP32 values plus the BF16 residual
-    // (AMIE_SELL_LO=1): the FP32 runs then iterate with ~32 bits of the FP64 matrix
-    bool sell_lo = false;
     // L2 eviction hint of the matrix stream in k_sell_dir (see ld_stream);
     // AMIE_MATRIX_HINT overrides it for measurements
     int matrix_hint = kMatrixHint;
@@ -182,7 +172,6 @@ void dispatch_group(int group, F &&f)
 }
 
 amie_status ensure_sell(amie_topo *t, bool want64, bool want32);
-amie_status ensure_sell_lo(amie_topo *t);
 amie_status ensure_sell_partition(amie_topo *t, int grid);
 
 // SELL copy of the current matrix in precision T (val == nullptr if not converted).
@@ -346,8 +335,7 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         s->grid_vec[1] = resident((const void *)k_update<double>, 0);
         if (const char *e = std::getenv("AMIE_MATRIX_HINT")) s->matrix_hint = std::min(2, std::max(0, std::atoi(e)));
         if (const char *e = std::getenv("AMIE_PREFETCH_KB")) s->prefetch_bytes = (uint32_t)std::min(1024, std::max(0, std::atoi(e))) * 1024u;
-        if (const char *e = std::getenv("AMIE_SELL_LO")) s->sell_lo = std::atoi(e) != 0;
-        s->grid_dir[0] = resident(sell_dir_kernel<float>(t->s, s->matrix_hint, s->sell_lo), 0);
+        s->grid_dir[0] = resident(sell_dir_kernel<float>(t->s, s->matrix_hint), 0);
         s->grid_dir[1] = resident(sell_dir_kernel<double>(t->s, s->matrix_hint), 0);
         s->grid_cgcg = std::min(resident(sell_cgcg_kernel<false>(t->s, s->matrix_hint), 0),
                                 resident(sell_cgcg_kernel<true>(t->s, s->matrix_hint), 0));
@@ -437,16 +425,14 @@ PcgVecs<float> vecs_of<float>(amie_topo *t)
 // k_sell_dir); false when the SELL copy or the CTA table for `grid` is missing.
 template <typename T>
 bool launch_spmv_dir(amie_topo *t, int grid, const PcgVecs<T> &v, double *part, PcgCtl *ctl, bool fin,
-                     cudaStream_t st, bool pdl, int hint, uint32_t prefetch_bytes = 0, const uint16_t *lo = nullptr)
+                     cudaStream_t st, bool pdl, int hint, uint32_t prefetch_bytes = 0)
 {
     SellView<T> sv = sell_of<T>(t);
     sv.prefetch_bytes = prefetch_bytes;
-    sv.lo = sizeof(T) == 4 && t->s == 2 ? lo : nullptr;
     auto it = t->sell_cta_first.find(grid);
     if (!sv.val || it == t->sell_cta_first.end() || !v.p2) return false;
     sv.cta_first = it->second.p;
-    auto kern = (void (*)(SellView<T>, PcgVecs<T>, double *, PcgCtl *, int))sell_dir_kernel<T>(t->s, hint,
-                                                                                               sv.lo != nullptr);
+    auto kern = (void (*)(SellView<T>, PcgVecs<T>, double *, PcgCtl *, int))sell_dir_kernel<T>(t->s, hint);
     launch_k(pdl, kern, grid, 0, st, sv, v, part, ctl, fin ? 1 : 0);
     AMIE_LAUNCHED();
     return true;
@@ -573,13 +559,6 @@ amie_status graph_fused(amie_topo *t, SolverState *s)
     return AMIE_OK;
 }
 
-// The BF16 residual the FP32 2x2 SpMV adds, when it is on and built.
-template <typename T>
-const uint16_t *lo_of(amie_topo *t, SolverState *s)
-{
-    return sizeof(T) == 4 && t->s == 2 && s->sell_lo && t->sell_lo_ok ? t->sell_lo.p : nullptr;
-}
-
 template <typename T>
 amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
 {
@@ -599,8 +578,7 @@ amie_status graph_for(amie_topo *t, SolverState *s, cudaGraphExec_t *g)
     for (int it = 0; it < kGraphIters; it++) {
         // the first kernel follows the previous graph launch in plain stream order
         if (fold<T>(s)) {
-            launch_spmv_dir<T>(t, gd, v, parts.pq, ctl, true, st, s->pdl && it > 0, s->matrix_hint, s->prefetch_bytes,
-                               lo_of<T>(t, s));
+            launch_spmv_dir<T>(t, gd, v, parts.pq, ctl, true, st, s->pdl && it > 0, s->matrix_hint, s->prefetch_bytes);
             launch_k(s->pdl, k_update<T>, gv, 0, st, v, n, parts, ctl);
         } else {
             PcgVecs<T> v1 = v;
@@ -838,7 +816,6 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
     AMIE_TRY(ensure_state(t, mixed, &s));
     if (mixed && !t->have32) AMIE_TRY(finalize_matrix_async(t, true));
     AMIE_TRY(ensure_sell(t, !mixed, mixed));   // before any graph of this topology is captured
-    if (mixed && s->sell_lo) AMIE_TRY(ensure_sell_lo(t));
     cudaStream_t st = t->ctx->stream;
     const double rtol = o && o->rtol > 0 ? o->rtol : 1e-10;
     const int64_t maxit = o && o->maxit > 0 ? o->maxit : std::max<int64_t>(1000, (int64_t)t->n);
@@ -1072,7 +1049,6 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
     AMIE_TRY(ensure_state(t, precision == 32, &s));
     if (precision == 32 && !t->have32) AMIE_TRY(finalize_matrix_async(t, true));
     AMIE_TRY(ensure_sell(t, precision == 64, precision == 32));
-    if (precision == 32 && s->sell_lo) AMIE_TRY(ensure_sell_lo(t));
     cudaStream_t st = t->ctx->stream;
     // zeroed inputs keep every value defined; the kernel's cost does not depend on them
     const size_t w = precision == 64 ? 8 : 4;
@@ -1117,7 +1093,7 @@ extern "C" amie_status amie_profile_spmv(amie_topo *t, int32_t precision, int32_
             launch_cgcg(t, s, false, false, st);
         } else if (precision == 32 && fold<float>(s)) {
             launch_spmv_dir<float>(t, s->grid_dir[pi], vecs_of<float>(t), parts.pq, s->ctl.p, false, st, false,
-                                   s->matrix_hint, 0, lo_of<float>(t, s));
+                                   s->matrix_hint);
         } else {
             if (precision == 64) launch_spmv_pq<double>(t, s->grid_sell[pi], vecs_of<double>(t), parts.pq, nullptr, nullptr, st);
             else launch_spmv_pq<float>(t, s->grid_sell[pi], vecs_of<float>(t), parts.pq, nullptr, nullptr, st);

@@ -562,11 +562,7 @@ __global__ void __launch_bounds__(kVecThreads, (S == 2 && sizeof(T) == 4) ? MINB
 // pq and alpha.  p_old / p_new are chosen by ctl->pcur (flipped by k_update),
 // so a graph of iterations needs no copies.  Same scheduling, FMA order and
 // fixed-order dot as k_sell_pq; p_new equals k_direction's fma(beta, p, z).
-// With LO (2x2 FP32 blocks only) every block is applied as its FP32 values plus
-// the BF16 rounding of their residual (A.lo): ~32 bits of the FP64 matrix for 8
-// more bytes per block, so that the FP32 runs iterate with (nearly) the FP64
-// operator.
-template <int S, typename T, int HINT = kMatrixHint, bool LO = false>
+template <int S, typename T, int HINT = kMatrixHint>
 __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs<T> v, double *part_pq, PcgCtl *ctl,
                                                           int fin)
 {
@@ -613,21 +609,6 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
         T blk[U][S * S];
         for (uint32_t j0 = 0; j0 < len; j0 += U) {
             load_sell_group<S, U, T, HINT>(A, g0, j0, len, lane, c, blk, pol);
-            T lo[U][S * S];
-            if constexpr (LO) {
-                static_assert(S == 2 && sizeof(T) == 4, "the BF16 residual exists for 2x2 FP32 blocks");
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    if (j0 + u < len) {
-                        const uint2 *p = reinterpret_cast<const uint2 *>(A.lo) + g0 + (uint64_t)(j0 + u) * 32 + lane;
-                        const uint2 w = HINT == 0 ? __ldg(p) : __ldcs(p);
-                        lo[u][0] = __uint_as_float(w.x << 16);
-                        lo[u][1] = __uint_as_float(w.x & 0xffff0000u);
-                        lo[u][2] = __uint_as_float(w.y << 16);
-                        lo[u][3] = __uint_as_float(w.y & 0xffff0000u);
-                    }
-                }
-            }
             T zv[U][S], pv[U][S];
 #pragma unroll
             for (int u = 0; u < U; u++) {
@@ -642,11 +623,8 @@ __global__ void __launch_bounds__(kVecThreads) k_sell_dir(SellView<T> A, PcgVecs
 #pragma unroll
                     for (int r = 0; r < S; r++)
 #pragma unroll
-                        for (int cc = 0; cc < S; cc++) {
-                            const T pn = fma(bt, pv[u][cc], zv[u][cc]);
-                            acc[r] = fma(blk[u][r * S + cc], pn, acc[r]);
-                            if constexpr (LO) acc[r] = fma(lo[u][r * S + cc], pn, acc[r]);
-                        }
+                        for (int cc = 0; cc < S; cc++)
+                            acc[r] = fma(blk[u][r * S + cc], fma(bt, pv[u][cc], zv[u][cc]), acc[r]);
                 }
             }
         }
