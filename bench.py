@@ -79,7 +79,7 @@ def parse_args():
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrival rate, requests/s")
     ap.add_argument("--damage-only", action="store_true", help="run only the config-3 damage loop (--damage-steps) "
                                                                "and print its statistics")
-    ap.add_argument("--damage-steps", type=int, default=30, help="config-3 damage-loop load steps of 1 um "
+    ap.add_argument("--damage-steps", type=int, default=60, help="config-3 damage-loop load steps of 0.5 um "
                                                                  "deflection each (0 = skip)")
     return ap.parse_args()
 
@@ -370,7 +370,7 @@ def run_ours(args, world, rank, local, dist):
         ctx.close()
         return 0
     if args.damage_only:
-        print(json.dumps({"damage_loop": run_damage_loop(ctx, solver, args.damage_steps, 1e-6 * args.damage_steps)}))
+        print(json.dumps({"damage_loop": run_damage_loop(ctx, solver, args.damage_steps, 0.5e-6 * args.damage_steps)}))
         ctx.close()
         return 0
     m, bcs, meta, name = make_workload(args.config, args.size)
@@ -524,7 +524,7 @@ def run_ours(args, world, rank, local, dist):
         result["serving"] = run_serving(ctx, args.serve, args.serve_rate, solver, iters=args.serve_iters)
     # damage loop (config 3)
     if args.damage_steps > 0:
-        result["damage_loop"] = run_damage_loop(ctx, solver, args.damage_steps, 1e-6 * args.damage_steps)
+        result["damage_loop"] = run_damage_loop(ctx, solver, args.damage_steps, 0.5e-6 * args.damage_steps)
 
     # CPU baseline: the oracle port on this machine's host cores, bounded sample, rank 0 at N = 1
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -609,14 +609,14 @@ def run_serving(ctx, n_requests: int, rate: float, solver: int, seed: int = 7, i
             "host_loop_s": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in loop_stats.items()}}
 
 
-def run_damage_loop(ctx, solver: int, steps: int = 30, deflection_max: float = 30e-6, max_passes: int = 400,
+def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 30e-6, max_passes: int = 400,
                     radius: float = 0.005):
     """Config-3 loop: notched beam in three-point bending (400 x 100 mm, 20 x 2 mm
     notch, P1, ~250k DOF, E 35 GPa, 20 mm loading plate) with the reference's
     StiffnessAndFracture damage: NonLocalMazars (threshold 1e-4, Gf 100 N/m,
     material radius 5 mm) graded on the device and FiberBasedIsotropicLinearDamage
     (0.1 per event, fractured at 0.6).  Each load step raises the plate's
-    deflection by deflection_max / steps (1 um) and runs FeatureTree::stepInternal's
+    deflection by deflection_max / steps (0.5 um) and runs FeatureTree::stepInternal's
     passes on the device (damaged stiffness, elimination, warm-started solve,
     grading, update) until no element changes, at most max_passes per step.  The
     beam stays elastic up to about 27 um; damage then starts at the notch tip and

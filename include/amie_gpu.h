@@ -245,10 +245,13 @@ AMIE_API amie_status amie_pcg_solve_noalloc(int32_t stride, uint32_t n_rows, con
                                             amie_solve_stats *stats);
 
 /* ------------------------------------------------------------------ serving
- * Continuous-batching solve server: independent meshes (microstructure or
- * damage-step solves) are admitted while others run, as free HBM allows; all
- * admitted solves advance together in one batched PCG iteration captured in a
- * CUDA graph. */
+ * Continuous-batching solve server: independent meshes (2D or 3D elasticity:
+ * microstructure or damage-step solves) are admitted while others run, as free
+ * HBM allows; all admitted solves advance together in batched PCG iterations
+ * captured in a CUDA graph, which also replaces the residuals of the solves
+ * whose inner run stopped and decides on the device whether each is finished,
+ * resumes or restarts.  Admission runs on two host threads (env
+ * AMIE_SERVER_ADMITTERS, 1-8), the batch loop on a third. */
 typedef struct amie_server_config {
     int32_t solver;              /* AMIE_SOLVER_PCG_FP64 or AMIE_SOLVER_PCG_MIXED */
     double rtol;                 /* per request relative residual target */

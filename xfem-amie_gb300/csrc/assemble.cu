@@ -333,22 +333,27 @@ __global__ void __launch_bounds__(32) k_quad_chunk(MeshView m, const QuadChunk *
     for (int i = threadIdx.x; i < npair * DIM * DIM; i += 32) partial[c.out + i] = sm.acc[i];
 }
 
+constexpr int kChunkSumThreads = 256;
+
 template <int DIM>
-__global__ void __launch_bounds__(32) k_quad_chunk_sum(MeshView m, const QuadLong *longs, uint32_t count,
-                                                       const QuadChunk *chunks, const double *partial)
+__global__ void __launch_bounds__(kChunkSumThreads) k_quad_chunk_sum(MeshView m, const QuadLong *longs, uint32_t count,
+                                                                     const QuadChunk *chunks, const double *partial)
 {
     __shared__ double acc[WarpQuadSmem<DIM>::NPAIR * DIM * DIM];
     if (blockIdx.x >= count) return;
     const QuadLong L = longs[blockIdx.x];
     const int nf = nf_of(m, L.elem);
     const int n = nf * (nf + 1) / 2 * DIM * DIM;
-    for (int i = threadIdx.x; i < n; i += 32) {
+    // an element's chunks are consecutive, n partial sums apart
+    const double *p0 = partial + chunks[L.chunk_first].out;
+    for (int i = threadIdx.x; i < n; i += kChunkSumThreads) {
         double a = 0.0;
-        for (uint32_t c = L.chunk_first; c < L.chunk_first + L.chunk_count; c++) a += partial[chunks[c].out + i];
+#pragma unroll 8
+        for (uint32_t c = 0; c < L.chunk_count; c++) a += p0[(uint64_t)c * n + i];
         acc[i] = a;
     }
-    __syncwarp();
-    warp_quad_store<DIM>(m, L.elem, nf, acc);
+    __syncthreads();
+    if (threadIdx.x < 32) warp_quad_store<DIM>(m, L.elem, nf, acc);
 }
 
 // Pattern keys: (row << 32 | col) for every (ids[j], ids[k]) of every element
@@ -1137,11 +1142,11 @@ amie_status assemble_async(amie_topo *t)
     if (t->n_long) {
         if (t->dim == 2) {
             k_quad_chunk<2><<<t->n_chunks, 32, 0, st>>>(m, t->quad_chunks.p, t->n_chunks, t->quad_partial.p);
-            k_quad_chunk_sum<2><<<t->n_long, 32, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
+            k_quad_chunk_sum<2><<<t->n_long, kChunkSumThreads, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
                                                            t->quad_partial.p);
         } else {
             k_quad_chunk<3><<<t->n_chunks, 32, 0, st>>>(m, t->quad_chunks.p, t->n_chunks, t->quad_partial.p);
-            k_quad_chunk_sum<3><<<t->n_long, 32, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
+            k_quad_chunk_sum<3><<<t->n_long, kChunkSumThreads, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
                                                            t->quad_partial.p);
         }
         g_launches += 2;

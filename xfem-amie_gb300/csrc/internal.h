@@ -18,7 +18,7 @@ constexpr int kSMs = 152;          // GB300: 2 dies x 76 SMs
 constexpr int kMaxFunctions = 32;  // shape + enrichment functions per element
 constexpr int kMaxGpWarpTile = 8;  // Gauss points staged per tile in the warp quadrature kernel
 constexpr int kLongGp = 64;        // enriched elements with more Gauss points are split into chunks
-constexpr int kChunkGp = 16;       // Gauss points per chunk of a long element
+constexpr int kChunkGp = 4;        // Gauss points per chunk of a long element (one warp each)
 
 // One chunk of the Gauss points of a long enriched element and where its
 // partial pair sums go; a long element and its chunks.
