@@ -334,26 +334,34 @@ __global__ void __launch_bounds__(32) k_quad_chunk(MeshView m, const QuadChunk *
 }
 
 constexpr int kChunkSumThreads = 256;
+constexpr int kChunkSumSplit = 4;   // CTAs per long element, each on a quarter of its pair sums
 
+// Sum of the chunk partials of each long element in chunk order, written as
+// blocks (i,j) and (j,i) of its staged K_e: CTA (element, part) takes every
+// kChunkSumSplit-th group of its pair sums.
 template <int DIM>
 __global__ void __launch_bounds__(kChunkSumThreads) k_quad_chunk_sum(MeshView m, const QuadLong *longs, uint32_t count,
                                                                      const QuadChunk *chunks, const double *partial)
 {
-    __shared__ double acc[WarpQuadSmem<DIM>::NPAIR * DIM * DIM];
-    if (blockIdx.x >= count) return;
-    const QuadLong L = longs[blockIdx.x];
+    const uint32_t li = blockIdx.x / kChunkSumSplit, part = blockIdx.x % kChunkSumSplit;
+    if (li >= count) return;
+    const QuadLong L = longs[li];
     const int nf = nf_of(m, L.elem);
-    const int n = nf * (nf + 1) / 2 * DIM * DIM;
+    const int npair = nf * (nf + 1) / 2;
+    const int n = npair * DIM * DIM;
+    double *K = m.ke + m.blk_off[L.elem] * DIM * DIM;
     // an element's chunks are consecutive, n partial sums apart
     const double *p0 = partial + chunks[L.chunk_first].out;
-    for (int i = threadIdx.x; i < n; i += kChunkSumThreads) {
+    for (int k = (int)part * kChunkSumThreads + threadIdx.x; k < n; k += kChunkSumSplit * kChunkSumThreads) {
         double a = 0.0;
 #pragma unroll 8
-        for (uint32_t c = 0; c < L.chunk_count; c++) a += p0[(uint64_t)c * n + i];
-        acc[i] = a;
+        for (uint32_t c = 0; c < L.chunk_count; c++) a += p0[(uint64_t)c * n + k];
+        const int pidx = k / (DIM * DIM), q = k % (DIM * DIM), r = q / DIM, cc = q % DIM;
+        int i, j;
+        pair_of(pidx, i, j);
+        K[(size_t)(i * nf + j) * DIM * DIM + r * DIM + cc] = a;
+        if (i != j) K[(size_t)(j * nf + i) * DIM * DIM + cc * DIM + r] = a;
     }
-    __syncthreads();
-    if (threadIdx.x < 32) warp_quad_store<DIM>(m, L.elem, nf, acc);
 }
 
 // Pattern keys: (row << 32 | col) for every (ids[j], ids[k]) of every element
@@ -1142,11 +1150,11 @@ amie_status assemble_async(amie_topo *t)
     if (t->n_long) {
         if (t->dim == 2) {
             k_quad_chunk<2><<<t->n_chunks, 32, 0, st>>>(m, t->quad_chunks.p, t->n_chunks, t->quad_partial.p);
-            k_quad_chunk_sum<2><<<t->n_long, kChunkSumThreads, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
+            k_quad_chunk_sum<2><<<t->n_long * kChunkSumSplit, kChunkSumThreads, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
                                                            t->quad_partial.p);
         } else {
             k_quad_chunk<3><<<t->n_chunks, 32, 0, st>>>(m, t->quad_chunks.p, t->n_chunks, t->quad_partial.p);
-            k_quad_chunk_sum<3><<<t->n_long, kChunkSumThreads, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
+            k_quad_chunk_sum<3><<<t->n_long * kChunkSumSplit, kChunkSumThreads, 0, st>>>(m, t->quad_long.p, t->n_long, t->quad_chunks.p,
                                                            t->quad_partial.p);
         }
         g_launches += 2;
