@@ -578,6 +578,160 @@ int run_damage(Out &o, std::map<std::string, std::string> &kv)
     return 0;
 }
 
+// Read access to the smoothing weights of a 3D cache (Mesh::coefs, protected).
+struct MeshCoefs3D : public Mesh<DelaunayTetrahedron, DelaunayTreeItem3D> {
+    static const std::vector<std::vector<double>> &of(Mesh<DelaunayTetrahedron, DelaunayTreeItem3D> *m, int id)
+    {
+        return static_cast<MeshCoefs3D *>(m)->coefs[id];
+    }
+};
+
+// 3D damage: an n^3 voxel cube (VoxelFilter, 6 tetrahedra per voxel, [0, 1e-4]^3 m)
+// whose voxels take one of `nphase` phases, phase p StiffnessAndFracture with a
+// seeded lognormal Young's modulus, NonLocalMazars and
+// FiberBasedIsotropicLinearDamage; pulled along x (left face fixed in x, bottom
+// in y, back in z, right face displaced) by load steps through FeatureTree::step.
+// Exports as the 2D damage case: element data, centres, circumradii, volumes,
+// the multipliers of one step with the pull at 1, and per step the
+// displacements, damage, scores, smoothed principal stresses and strains (3 + 3)
+// and element strains (6), then the smoothing and maximum neighbourhoods.
+int run_damage3d(Out &o, std::map<std::string, std::string> &kv)
+{
+    const int n = (int)getd(kv, "n", 6);
+    const int nphase = (int)getd(kv, "nphase", 8);
+    const double E = getd(kv, "E", 30e9), nu = getd(kv, "nu", 0.2), sig = getd(kv, "sigma_log", 0.4);
+    const double thr = getd(kv, "eps0", 1e-4), Gf = getd(kv, "Gf", 100.0), R = getd(kv, "radius", 2e-5);
+    const double fibre = getd(kv, "fibre", 0.1), cutoff = getd(kv, "cutoff", 0.6);
+    const double dmax = getd(kv, "displacement", 3e-8);
+    const int steps = (int)getd(kv, "steps", 6);
+    const int maxit = (int)getd(kv, "maxit", 200);
+    const int seed = (int)getd(kv, "seed", 7);
+    const char *path = "/tmp/ref_harness_damage3d.txt";
+
+    std::mt19937 gen(seed);
+    std::lognormal_distribution<double> lnd(std::log(E), sig);
+    std::uniform_int_distribution<int> pick(0, nphase - 1);
+    std::map<unsigned char, Form *> behaviours;
+    std::vector<double> phaseE;
+    for (int p = 0; p < nphase; p++) {
+        const double Ep = lnd(gen);
+        phaseE.push_back(Ep);
+        behaviours[(unsigned char)('A' + p)] = new StiffnessAndFracture(
+            Ep, nu, new NonLocalMazars(thr, Ep, nu, Gf, R, PLANE_STRESS), new FiberBasedIsotropicLinearDamage(fibre, cutoff),
+            SPACE_THREE_DIMENSIONAL);
+    }
+    {
+        FILE *f = std::fopen(path, "w");
+        std::fprintf(f, "voxels amie %d %d %d\n", n, n, n);
+        for (int v = 0; v < n * n * n; v++) std::fputc('A' + pick(gen), f);
+        std::fputc('\n', f);
+        std::fclose(f);
+    }
+    FeatureTree F(path, behaviours);
+    F.setMaxIterationsPerStep(maxit);
+    BoundingBoxDefinedBoundaryCondition *pull = new BoundingBoxDefinedBoundaryCondition(SET_ALONG_XI, RIGHT, 0.);
+    std::vector<BoundaryCondition *> bcs = {new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, LEFT),
+                                            new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ETA, BOTTOM),
+                                            new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_ZETA, BACK), pull};
+    for (auto bc : bcs) F.addBoundaryCondition(bc);
+
+    Assembly *K = F.getAssembly(true);
+    VirtualMachine vm;
+    ElementExport X;
+    std::vector<DelaunayTetrahedron *> elems;
+    std::vector<double> centre, radius, volume;
+    for (size_t ie = 0; ie < K->element3d.size(); ie++) {
+        DelaunayTetrahedron *t = dynamic_cast<DelaunayTetrahedron *>(K->element3d[ie]);
+        elems.push_back(t);
+        export_element(t, 3, K->scales[ie], {}, vm, X);
+        centre.push_back(t->getCenter().getX());
+        centre.push_back(t->getCenter().getY());
+        centre.push_back(t->getCenter().getZ());
+        radius.push_back(t->getRadius());
+        volume.push_back(t->volume());
+    }
+    write_elements(o, X);
+    {
+        Assembly A;
+        A.add(elems[0]);
+        pull->setData(1.0);
+        for (auto bc : bcs) bc->apply(&A, F.get3DMesh(), &vm);
+        pull->setData(0.0);
+        write_multipliers(o, &A);
+    }
+    o.d("elem_centre", centre);
+    o.d("elem_radius", radius);
+    o.d("elem_volume", volume);
+    o.d("phase_E", phaseE);
+    o.scalar("ndofmax", (double)K->ndofmax);
+    o.scalar("dim", 3);
+    o.scalar("eps0", thr);
+    o.scalar("Gf", Gf);
+    o.scalar("nu", nu);
+    o.scalar("radius", R);
+    o.scalar("fibre", fibre);
+    o.scalar("cutoff", cutoff);
+    o.scalar("steps", steps);
+    o.scalar("displacement", dmax);
+
+    const size_t ne = elems.size();
+    std::vector<double> sub;
+    for (int k = 1; k <= steps; k++) {
+        pull->setData(dmax * k / steps);
+        const double t0 = now_s();
+        F.step();
+        const double t1 = now_s();
+        const Vector &u = F.getDisplacements();
+        std::vector<double> uu(std::begin(u), std::end(u)), dmg(ne), score(ne), sm(6 * ne), eps(6 * ne);
+        size_t damaged = 0;
+        for (size_t i = 0; i < ne; i++) {
+            Form *b = elems[i]->getBehaviour();
+            const Matrix Ceff = b->getTensor(Point());
+            dmg[i] = 1.0 - Ceff[0][0] / b->param[0][0];
+            damaged += dmg[i] > 0;
+            FractureCriterion *fc = b->getFractureCriterion();
+            score[i] = fc->getScoreAtState();
+            std::pair<Vector, Vector> f = fc->getSmoothedFields(PRINCIPAL_REAL_STRESS_FIELD, PRINCIPAL_TOTAL_STRAIN_FIELD,
+                                                                 elems[i]->getState(), 0.);
+            for (int c = 0; c < 3; c++) {
+                sm[6 * i + c] = f.first.size() > (size_t)c ? f.first[c] : 0.0;
+                sm[6 * i + 3 + c] = f.second.size() > (size_t)c ? f.second[c] : 0.0;
+            }
+            Vector es(6);
+            elems[i]->getState().getAverageField(MECHANICAL_STRAIN_FIELD, es, &vm, 0.);
+            for (int c = 0; c < 6; c++) eps[6 * i + c] = es[c];
+        }
+        const std::string sfx = "_" + std::to_string(k);
+        o.d("u" + sfx, uu);
+        o.d("damage" + sfx, dmg);
+        o.d("score" + sfx, score);
+        o.d("smoothed" + sfx, sm);
+        o.d("strain" + sfx, eps);
+        o.scalar("step_time_s" + sfx, t1 - t0);
+        std::fprintf(stderr, "harness damage3d: step %d displacement %.3e damaged %zu avg %.3e time %.2fs\n", k,
+                     dmax * k / steps, damaged, F.averageDamage, t1 - t0);
+    }
+    std::map<int, uint32_t> pos;
+    for (size_t i = 0; i < ne; i++) pos[elems[i]->index] = (uint32_t)i;
+    std::vector<uint32_t> cptr{0}, cidx, aptr{0}, aidx;
+    std::vector<double> ccoef;
+    for (size_t i = 0; i < ne; i++) {
+        FractureCriterion *fc = elems[i]->getBehaviour()->getFractureCriterion();
+        for (int id : F.get3DMesh()->getCache(CriterionCaches::core(fc))) cidx.push_back(pos.count(id) ? pos[id] : 0xffffffffu);
+        cptr.push_back((uint32_t)cidx.size());
+        for (const auto &w : MeshCoefs3D::of(F.get3DMesh(), CriterionCaches::core(fc))) ccoef.push_back(w.empty() ? -1.0 : w[0]);
+        for (int id : F.get3DMesh()->getCache(CriterionCaches::all(fc))) aidx.push_back(pos.count(id) ? pos[id] : 0xffffffffu);
+        aptr.push_back((uint32_t)aidx.size());
+    }
+    o.u("cache_ptr", cptr);
+    o.u("cache_idx", cidx);
+    o.d("cache_coef", ccoef);
+    o.u("cache_all_ptr", aptr);
+    o.u("cache_all_idx", aidx);
+    o.scalar("n_elem", (double)ne);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -593,6 +747,7 @@ int main(int argc, char **argv)
     if (which == "incl" || which == "crack" || which == "plate" || which == "imposed") return run_2d(which, o, kv);
     if (which == "voxel") return run_voxel(o, kv);
     if (which == "damage") return run_damage(o, kv);
+    if (which == "damage3d") return run_damage3d(o, kv);
     std::fprintf(stderr, "unknown case %s\n", which.c_str());
     return 2;
 }
