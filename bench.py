@@ -483,7 +483,9 @@ def run_ours(args, world, rank, local, dist):
         "mixed_vs_fp64_dof_it": value / world / fp64_value if solver == G.SOLVER_PCG_MIXED else 1.0,
         "mixed_vs_fp64_solve_time": ms64 / (t_local * 1e3 / args.steps) if solver == G.SOLVER_PCG_MIXED else 1.0,
         "assembly_ms": ms_asm,
-        "roofline_assembly": {"bound": "hbm", "alg_bytes": asm_alg["total"], "parts": asm_alg,
+        "roofline_assembly": {"bound": "fp64 issue (ncu: FP64 pipe 84-87 % busy, DRAM 7-8 %, "
+                                       "profiles/k_quad_simple_k_gather_cfg1_n280.md)",
+                              "alg_bytes": asm_alg["total"], "parts": asm_alg,
                               "achieved": asm_alg["total"] / (ms_asm / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                               "frac": asm_alg["total"] / (ms_asm / 1e3) / 1e9 / peak,
                               "timed": "quadrature + gather + Dirichlet elimination + FP32/FP64 solver copies"},
