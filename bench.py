@@ -538,6 +538,15 @@ def run_ours(args, world, rank, local, dist):
         result["cpu_baseline"] = {"value": v_cpu, "unit": UNIT, "cores": O.threads(), "kind": "port",
                                   "sample": f"{it_cpu} Jacobi-PCG iterations (Kahan SpMV/dots) on the same "
                                             f"{n}-DOF matrix, {dt_cpu:.1f} s"}
+        # the same comparison in time to solution: a CPU FP64 solve needs the FP64
+        # iteration count at the CPU rate; the GPU step is assembly + mixed solve
+        cpu_solve_s = n * st64["iterations"] / v_cpu
+        step_s = t_max / args.steps
+        result["time_to_solution"] = {"gpu_step_s": step_s, "gpu_e2e_s": result.get("e2e", {}).get("ms", 0.0) / 1e3,
+                                      "gpu_fp64_s": ms64 / 1e3, "cpu_fp64_solve_s_estimate": cpu_solve_s,
+                                      "speedup_step": cpu_solve_s / step_s,
+                                      "note": "CPU time = FP64 iterations x DOF / cpu_baseline rate (assembly "
+                                              "excluded on the CPU side)"}
     topo.close()
     ctx.close()
     if rank == 0:

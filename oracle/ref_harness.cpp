@@ -235,19 +235,33 @@ void write_elements(Out &o, ElementExport &X)
     o.d("elem_imposed", X.imposed);
 }
 
-// Dirichlet multipliers as stored by the Assembly (before make_final sorts them).
+// Dirichlet multipliers as stored by the Assembly (before make_final sorts them);
+// a SET_PROPORTIONAL_DISPLACEMENT multiplier (u_id = offset + sum coefs u_propid,
+// Assembly::setPointProportional, solvers/assembly.cpp:1636-1760) also gives its
+// DOFs and coefficients (bc_prop_ptr / bc_prop_ids / bc_prop_coefs).
 void write_multipliers(Out &o, Assembly *K)
 {
-    std::vector<uint32_t> ids, types;
-    std::vector<double> vals;
+    std::vector<uint32_t> ids, types, pptr{0}, pids;
+    std::vector<double> vals, pco;
     for (auto &m : K->multipliers) {
         ids.push_back((uint32_t)m.getId());
         types.push_back((uint32_t)m.type);
         vals.push_back(m.getValue());
+        if (m.type == SET_PROPORTIONAL_DISPLACEMENT) {
+            const std::valarray<unsigned int> d = m.getDofIds();
+            for (size_t k = 0; k < d.size(); k++) {
+                pids.push_back(d[k]);
+                pco.push_back(m.coefs[k]);
+            }
+        }
+        pptr.push_back((uint32_t)pids.size());
     }
     o.u("bc_ids", ids);
     o.u("bc_types", types);
     o.d("bc_values", vals);
+    o.u("bc_prop_ptr", pptr);
+    o.u("bc_prop_ids", pids);
+    o.d("bc_prop_coefs", pco);
 }
 
 // make_final + the ConjugateGradient call of Assembly::cgsolve, then export.
@@ -274,6 +288,17 @@ void finish_and_solve(Out &o, Assembly *K)
     double t3 = now_s();
     std::vector<double> x(std::begin(cg.x), std::end(cg.x));
     o.d("u", x);
+    // the displacements Assembly::cgsolve reports: a proportional multiplier's DOF
+    // set from its DOFs after the solve, in multiplier order (solvers/assembly.cpp:1881-1892)
+    std::vector<double> xp(x);
+    for (auto &m : K->multipliersBuffer)   // filled by setBoundaryConditions in multiplier order
+        if (m.type == SET_PROPORTIONAL_DISPLACEMENT) {
+            const std::valarray<unsigned int> d = m.getDofIds();
+            double v = m.getValue();
+            for (size_t k = 0; k < d.size(); k++) v += m.coefs[k] * xp[d[k]];
+            xp[m.getId()] = v;
+        }
+    o.d("u_post", xp);
     o.scalar("cg_iterations", (double)cg.nit);
     o.scalar("cg_converged", ok ? 1.0 : 0.0);
     o.scalar("epsilon", K->epsilon);
@@ -344,6 +369,9 @@ int run_2d(const std::string &which, Out &o, std::map<std::string, std::string> 
                new BoundingBoxDefinedBoundaryCondition(FIX_ALONG_XI, BOTTOM_LEFT),
                new BoundingBoxDefinedBoundaryCondition(SET_STRESS_ETA, TOP, getd(kv, "stress", 1e6))};
     }
+    if (getd(kv, "prop", 0.0) != 0.0)   // an inclined roller on RIGHT: u_x = prop * u_y
+        bcs.push_back(new BoundingBoxDefinedBoundaryCondition(SET_PROPORTIONAL_DISPLACEMENT_XI_ETA, RIGHT,
+                                                              getd(kv, "prop", 0.0)));
     F.setSamplingNumber(sampling);
     if (order == 2) F.setOrder(QUADRATIC);
 
