@@ -194,6 +194,24 @@ AMIE_API amie_status amie_element_matrices(const amie_topo *topo, double *ke, ui
 AMIE_API amie_status amie_apply_dirichlet(amie_topo *topo, uint32_t n_bc, const uint32_t *ids, const double *values,
                                  const uint8_t *kinds, const double *rhs0);
 
+/* Proportional displacements of Assembly::setPointProportional
+ * (solvers/assembly.cpp:1636-1760; SET_PROPORTIONAL_DISPLACEMENT multipliers,
+ * e.g. the inclined rollers SET_PROPORTIONAL_DISPLACEMENT_XI_ETA of
+ * features/boundarycondition.cpp:256-264): u[ids[i]] = offsets[i] +
+ * sum_k coefs[k] u[prop_ids[k]], k in [ptr[i], ptr[i+1]).  Stored on the
+ * topology and applied after the Dirichlet elimination and the force
+ * multipliers of every later elimination, multiplier after multiplier in the
+ * order given (setBoundaryConditions, solvers/assembly.cpp:279-318: the DOF's
+ * column moves onto its DOFs, its row is added to theirs, it becomes a unit row
+ * with a zero right-hand side; an entry outside the pattern is dropped, as the
+ * reference's sparse access drops it), and to the solution at the end of every
+ * solve (Assembly::cgsolve, solvers/assembly.cpp:1881-1892).  An assembled
+ * topology is assembled and eliminated again with every stored multiplier;
+ * amie_assemble applies them with or without a Dirichlet list.  n = 0 removes
+ * them. */
+AMIE_API amie_status amie_set_proportional(amie_topo *topo, uint32_t n, const uint32_t *ids, const double *offsets,
+                                           const uint32_t *ptr, const uint32_t *prop_ids, const double *coefs);
+
 /* Matrix and right-hand side in AMIE's own layout (CoordinateIndexedSparseMatrix::array,
  * blocks column-major with even-padded columns, sparse/sparse_vector.cpp:50-58):
  * array [nnzb * s * (s + s%2)], rhs [n] (Assembly::getForces, solvers/assembly.h:343). */

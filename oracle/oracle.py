@@ -290,3 +290,73 @@ def with_tabulated_tips(m):
         out.enr_jump = np.concatenate([out.enr_jump, np.zeros(n_gp - len(out.enr_jump), np.int8)])
     out.enr_tip = None
     return out
+
+
+def proportional(stride, rs, ci, arr, rhs, ids, offsets, ptr, prop_ids, coefs):
+    """The SET_PROPORTIONAL_DISPLACEMENT branch of Assembly::setBoundaryConditions
+    (solvers/assembly.cpp:279-318), restated entry by entry on AMIE's padded
+    column-major block layout, in place: for each multiplier u_id = offset +
+    sum c_k u_pk, in order, every other row j moves A_j,id onto A_j,pk and offset
+    A_j,id onto f_j, the rows p_k take c_k times row id (and f_id), row id becomes
+    a unit row with f_id = 0.  A missing entry reads as 0 and a write to it is
+    dropped (SparseVector::operator[], sparse/sparse_vector.cpp:38-48)."""
+    s = int(stride)
+    cl = s + s % 2
+    starts = np.concatenate([[0], np.cumsum(rs.astype(np.int64))])
+    n = len(rs) * s
+
+    def pos(i, j):
+        row, cb = i // s, j // s
+        a, b = int(starts[row]), int(starts[row + 1])
+        k = int(np.searchsorted(ci[a:b], cb))
+        if k < b - a and ci[a + k] == cb:
+            return (a + k) * s * cl + (j % s) * cl + (i % s)
+        return -1
+
+    def get(i, j):
+        p = pos(i, j)
+        return arr[p] if p >= 0 else 0.0
+
+    def add(i, j, v):
+        p = pos(i, j)
+        if p >= 0:
+            arr[p] += v
+
+    def put(i, j, v):
+        p = pos(i, j)
+        if p >= 0:
+            arr[p] = v
+
+    for m in range(len(ids)):
+        i0, off = int(ids[m]), float(offsets[m])
+        P = [int(q) for q in prop_ids[ptr[m]:ptr[m + 1]]]
+        Cf = [float(c) for c in coefs[ptr[m]:ptr[m + 1]]]
+        for j in range(n):
+            if j == i0 or j in P:
+                continue
+            a = get(j, i0)
+            rhs[j] -= off * a
+            for p, c in zip(P, Cf):
+                add(j, p, c * a)
+            put(j, i0, 0.0)
+        for p, c in zip(P, Cf):
+            for j in range(n):
+                add(p, j, c * get(i0, j))
+            rhs[p] += c * rhs[i0]
+            for p2, c2 in zip(P, Cf):
+                add(p, p2, c2 * get(p, i0))
+            rhs[p] -= off * get(p, i0)
+            put(p, i0, 0.0)
+        for j in range(n):
+            put(i0, j, 1.0 if j == i0 else 0.0)
+        rhs[i0] = 0.0
+
+
+def proportional_solution(x, ids, offsets, ptr, prop_ids, coefs):
+    """The proportional DOFs of a solution, in multiplier order (Assembly::cgsolve,
+    solvers/assembly.cpp:1881-1892); in place."""
+    for m in range(len(ids)):
+        v = float(offsets[m])
+        for k in range(int(ptr[m]), int(ptr[m + 1])):
+            v += coefs[k] * x[prop_ids[k]]
+        x[ids[m]] = v

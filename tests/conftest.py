@@ -14,10 +14,11 @@ for sub in ("xfem-amie_gb300", "oracle"):
 
 GOLDEN_DIR = os.path.join(REPO, "tests", "golden")
 # assembly / solve fixtures (one assembled system each); the damage fixtures hold
-# load-step histories instead and have their own tests
+# load-step histories instead, and the proportional-multiplier fixture needs its
+# own multipliers: both have their own tests
 GOLDEN_CASES = sorted(n for n in (os.path.splitext(os.path.basename(p))[0]
                                   for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
-                      if not n.startswith("damage"))
+                      if not n.startswith("damage") and not n.startswith("prop"))
 
 
 def pytest_configure(config):

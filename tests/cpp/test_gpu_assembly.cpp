@@ -2,7 +2,8 @@
 //
 // Reads one case as raw arrays from a directory (written by
 // tests/test_cpp_assembly.py), adds the elements one by one, sets the Dirichlet
-// multipliers with setPointAlong, runs cgsolve with the requested solver and
+// multipliers with setPointAlong (and the proportional ones, when the case has
+// them, with setPointProportional), runs cgsolve with the requested solver and
 // writes the displacements and the matrix back as raw arrays.
 //
 //   test_gpu_assembly <dir> <solver: 0 fp64 | 1 mixed | 2 amie_cg>
@@ -51,6 +52,10 @@ int main(int argc, char **argv)
     auto bc_ids = load<uint32_t>(dir + "/bc_ids.bin");
     auto bc_vals = load<double>(dir + "/bc_vals.bin");
     auto meta = load<double>(dir + "/meta.bin");   // dim, ndofmax, eps, nssor
+    auto prop_ids = load<uint32_t>(dir + "/prop_ids.bin");   // u[prop_ids] = coefs u[prop_dofs] + offsets
+    auto prop_dofs = load<uint32_t>(dir + "/prop_dofs.bin");
+    auto prop_offsets = load<double>(dir + "/prop_offsets.bin");
+    auto prop_coefs = load<double>(dir + "/prop_coefs.bin");
     if (kind.empty() || meta.size() < 4) return 3;
     const int dim = (int)meta[0];
     const int nv = dim == 2 ? 3 : 6;
@@ -70,6 +75,11 @@ int main(int argc, char **argv)
         K.setSSORIterations((size_t)meta[3]);
         for (size_t i = 0; i < bc_ids.size(); i++)
             K.setPointAlong((gpu::Variable)(bc_ids[i] % dim), bc_vals[i], bc_ids[i] / dim);
+        for (size_t i = 0; i < prop_ids.size(); i++) {
+            if (prop_dofs[i] / dim != prop_ids[i] / dim) return 5;   // one node per setPointProportional
+            K.setPointProportional((gpu::Variable)(prop_ids[i] % dim), (gpu::Variable)(prop_dofs[i] % dim), prop_coefs[i],
+                                   prop_offsets[i], prop_ids[i] / dim);
+        }
         K.setSolver(solver, 1e-12);
         const bool ok = K.cgsolve();
         save(dir + "/u.bin", K.getDisplacements());

@@ -42,6 +42,9 @@ CASES = {
     # same plate, free on rollers, imposed strain 1e-3 (induced force multipliers)
     # -> strain_yy = 1e-3, real stress 0
     "imposed": ("imposed", ["size=0.01", "E=10e9", "nu=0.2", "sampling=4", "imposed=1e-3"]),
+    # incl_p1 with an inclined roller on RIGHT (SET_PROPORTIONAL_DISPLACEMENT_XI_ETA,
+    # u_x = 0.5 u_y: Assembly::setPointProportional multipliers)
+    "prop_p1": ("incl", ["sampling=12", "ninc=30", "seed=7", "order=1", "prop=0.5"]),
     # config-2 style: voxel file -> 6 linear tets per voxel, 16 lognormal phases,
     # uniaxial imposed strain 1e-4
     "voxel_t4": ("voxel", ["n=6", "nphase=16", "seed=5", "strain=1e-4"]),

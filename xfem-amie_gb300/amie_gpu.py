@@ -37,7 +37,7 @@ EXPORTED = [
     "amie_topology_spmv_lanes", "amie_profile_stream", "amie_average_field", "amie_set_imposed_strain",
     "amie_server_query", "amie_cut_rules", "amie_extrapolate", "amie_damage_setup", "amie_damage_set_state",
     "amie_damage_get_state", "amie_damage_grade", "amie_damage_update", "amie_damage_load_step",
-    "amie_solution_upload",
+    "amie_solution_upload", "amie_set_proportional",
 ]
 
 
@@ -280,6 +280,18 @@ class Topology:
         rhs0 = None if rhs0 is None else np.ascontiguousarray(rhs0, np.float64)
         check(lib().amie_apply_dirichlet(self.ptr, C.c_uint32(len(ids)), _p(ids), _p(values), _p(kinds), _p(rhs0)),
               "amie_apply_dirichlet")
+
+    def set_proportional(self, ids, offsets, ptr, prop_ids, coefs):
+        """Proportional displacements u[ids[i]] = offsets[i] + sum coefs[k] u[prop_ids[k]],
+        k in [ptr[i], ptr[i+1]) (Assembly::setPointProportional), applied after every
+        elimination and to every solution; empty arrays remove them."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        offsets = np.ascontiguousarray(offsets, np.float64)
+        ptr = np.ascontiguousarray(ptr, np.uint32)
+        prop_ids = np.ascontiguousarray(prop_ids, np.uint32)
+        coefs = np.ascontiguousarray(coefs, np.float64)
+        check(lib().amie_set_proportional(self.ptr, C.c_uint32(len(ids)), _p(ids), _p(offsets), _p(ptr), _p(prop_ids),
+                                          _p(coefs)), "amie_set_proportional")
 
     def matrix(self):
         """(array in AMIE's padded column-major block layout, rhs)."""

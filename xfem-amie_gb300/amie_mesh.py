@@ -234,20 +234,45 @@ def from_golden(d, enrichment: str = "auto", tips=()) -> MeshData:
 
 
 # LagrangeMultiplierType values (solvers/assembly.h:36-96): the force types are
-# added to the right-hand side after elimination, GENERAL and
-# SET_PROPORTIONAL_DISPLACEMENT are not supported, every other type is an
-# eliminated displacement (solvers/assembly.cpp:163-169).
+# added to the right-hand side after elimination, SET_PROPORTIONAL_DISPLACEMENT
+# multipliers are substituted after it (golden_proportional), GENERAL is not
+# supported, every other type is an eliminated displacement
+# (solvers/assembly.cpp:163-169).
 LM_FORCE_TYPES = (34, 35, 36, 37)          # SET_FORCE_XI, _ETA, _ZETA, _INDEXED_AXIS
-LM_UNSUPPORTED = (0, 23)                   # GENERAL, SET_PROPORTIONAL_DISPLACEMENT
+LM_PROPORTIONAL = 23                       # SET_PROPORTIONAL_DISPLACEMENT
+LM_UNSUPPORTED = (0,)                      # GENERAL
 
 
 def golden_bcs(d):
-    """Multipliers of a fixture as (ids, values, kinds), sorted by id as make_final sorts them."""
+    """Displacement and force multipliers of a fixture as (ids, values, kinds), sorted by
+    id as make_final sorts them (proportional ones: golden_proportional)."""
     ids = d["bc_ids"].astype(np.uint32)
     vals = d["bc_values"].astype(np.float64)
     types = d["bc_types"].astype(np.int64)
     if np.isin(types, LM_UNSUPPORTED).any():
-        raise ValueError("GENERAL / proportional multipliers are not supported")
+        raise ValueError("GENERAL multipliers are not supported")
+    keep = types != LM_PROPORTIONAL
+    ids, vals, types = ids[keep], vals[keep], types[keep]
     kinds = np.where(np.isin(types, LM_FORCE_TYPES), BC_FORCE, BC_DISPLACEMENT).astype(np.uint8)
     order = np.argsort(ids, kind="stable")
     return ids[order], vals[order], kinds[order]
+
+
+def golden_proportional(d):
+    """SET_PROPORTIONAL_DISPLACEMENT multipliers of a fixture, sorted by id as
+    make_final sorts them: (ids, offsets, ptr, prop_ids, coefs)."""
+    types = d["bc_types"].astype(np.int64)
+    sel = np.nonzero(types == LM_PROPORTIONAL)[0]
+    if not len(sel) or "bc_prop_ptr" not in d:
+        return (np.zeros(0, np.uint32), np.zeros(0), np.zeros(1, np.uint32), np.zeros(0, np.uint32), np.zeros(0))
+    pp = d["bc_prop_ptr"].astype(np.int64)
+    sel = sel[np.argsort(d["bc_ids"][sel], kind="stable")]
+    ids = d["bc_ids"][sel].astype(np.uint32)
+    offs = d["bc_values"][sel].astype(np.float64)
+    ptr = [0]
+    pids, coefs = [], []
+    for i in sel:
+        pids.extend(d["bc_prop_ids"][pp[i]:pp[i + 1]].tolist())
+        coefs.extend(d["bc_prop_coefs"][pp[i]:pp[i + 1]].tolist())
+        ptr.append(len(pids))
+    return ids, offs, np.array(ptr, np.uint32), np.array(pids, np.uint32), np.array(coefs)

@@ -1306,12 +1306,136 @@ amie_status add_induced_forces_async(amie_topo *t)
     return AMIE_OK;
 }
 
+
+// ------------------------------------------------------------------ proportional displacements
+// Position of block (row, col) in the block-CSR pattern, or -1 (columns of a
+// row are sorted).
+__device__ __forceinline__ int64_t find_block(const uint32_t *row_ptr, const uint32_t *col, uint32_t row, uint32_t c)
+{
+    uint32_t lo = row_ptr[row], hi = row_ptr[row + 1];
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (col[mid] < c) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < row_ptr[row + 1] && col[lo] == c) ? (int64_t)lo : -1;
+}
+
+// The SET_PROPORTIONAL_DISPLACEMENT branch of Assembly::setBoundaryConditions
+// (solvers/assembly.cpp:279-318) for every proportional multiplier in order, one
+// CTA: u_id = offset + sum_k c_k u_(p_k) is substituted.  (1) every other row j
+// of column id: f_j -= offset A_j,id, A_j,pk += c_k A_j,id, A_j,id = 0; (2) for
+// each k in order: row p_k += c_k row id, f_pk += c_k f_id, A_pk,pj += c_j A_pk,id,
+// f_pk -= offset A_pk,id, A_pk,id = 0; (3) row id = unit row, f_id = 0.  The
+// rows holding column id are the columns of row id (symmetric pattern); an
+// entry outside the pattern is dropped, as SparseVector::operator[] drops it
+// (sparse/sparse_vector.cpp:38-48).  Every entry sees the reference's
+// operations in the reference's order.
+template <int S>
+__global__ void __launch_bounds__(256) k_proportional(const uint32_t *row_ptr, const uint32_t *col, double *val,
+                                                     double *rhs, uint32_t n_prop, const uint32_t *ids,
+                                                     const double *offs, const uint32_t *ptr, const uint32_t *dofs,
+                                                     const double *coefs)
+{
+    for (uint32_t m = 0; m < n_prop; m++) {
+        const uint32_t id = ids[m], B = id / S, ci = id % S;
+        const double off = offs[m];
+        const uint32_t k0 = ptr[m], k1 = ptr[m + 1];
+        const uint32_t b0 = row_ptr[B], b1 = row_ptr[B + 1];
+        // (1) column id, rows other than id and its DOFs
+        for (uint32_t t = b0 * S + threadIdx.x; t < b1 * S; t += blockDim.x) {
+            const uint32_t J = col[t / S], r = t % S, j = J * S + r;
+            bool skip = j == id;
+            for (uint32_t k = k0; k < k1; k++) skip |= j == dofs[k];
+            if (skip) continue;
+            const int64_t q = find_block(row_ptr, col, J, B);
+            if (q < 0) continue;
+            double *aj = val + (uint64_t)q * S * S + r * S + ci;
+            const double a = *aj;
+            rhs[j] -= off * a;
+            for (uint32_t k = k0; k < k1; k++) {
+                const uint32_t p = dofs[k];
+                const int64_t qp = find_block(row_ptr, col, J, p / S);
+                if (qp >= 0) val[(uint64_t)qp * S * S + r * S + p % S] += coefs[k] * a;
+            }
+            *aj = 0.0;
+        }
+        __syncthreads();
+        // (2) the rows of its DOFs, in order
+        for (uint32_t k = k0; k < k1; k++) {
+            const uint32_t p = dofs[k], P = p / S, pr = p % S;
+            const double c = coefs[k];
+            for (uint32_t t = b0 * S + threadIdx.x; t < b1 * S; t += blockDim.x) {
+                const uint32_t C = col[t / S], cc = t % S;
+                const int64_t qp = find_block(row_ptr, col, P, C);
+                if (qp >= 0) val[(uint64_t)qp * S * S + pr * S + cc] += c * val[(uint64_t)(t / S) * S * S + ci * S + cc];
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                rhs[p] += c * rhs[id];
+                const int64_t qi = find_block(row_ptr, col, P, B);
+                for (uint32_t k2 = k0; k2 < k1; k2++) {
+                    const uint32_t p2 = dofs[k2];
+                    const int64_t q2 = find_block(row_ptr, col, P, p2 / S);
+                    const double api = qi >= 0 ? val[(uint64_t)qi * S * S + pr * S + ci] : 0.0;
+                    if (q2 >= 0) val[(uint64_t)q2 * S * S + pr * S + p2 % S] += coefs[k2] * api;
+                }
+                const double api = qi >= 0 ? val[(uint64_t)qi * S * S + pr * S + ci] : 0.0;
+                rhs[p] -= off * api;
+                if (qi >= 0) val[(uint64_t)qi * S * S + pr * S + ci] = 0.0;
+            }
+            __syncthreads();
+        }
+        // (3) row id
+        for (uint32_t t = b0 * S + threadIdx.x; t < b1 * S; t += blockDim.x) {
+            const uint32_t C = col[t / S], cc = t % S;
+            val[(uint64_t)(t / S) * S * S + ci * S + cc] = (C * S + cc == id) ? 1.0 : 0.0;
+        }
+        if (threadIdx.x == 0) rhs[id] = 0.0;
+        __syncthreads();
+    }
+}
+
+// The proportional DOFs of the solution, in multiplier order (Assembly::cgsolve,
+// solvers/assembly.cpp:1881-1892): u_id = offset, then u_id += c_k u_(p_k).
+__global__ void k_proportional_solution(uint32_t n_prop, const uint32_t *ids, const double *offs, const uint32_t *ptr,
+                                        const uint32_t *dofs, const double *coefs, double *x)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (uint32_t m = 0; m < n_prop; m++) {
+        double v = offs[m];
+        for (uint32_t k = ptr[m]; k < ptr[m + 1]; k++) v += coefs[k] * x[dofs[k]];
+        x[ids[m]] = v;
+    }
+}
+
+amie_status proportional_solution_async(amie_topo *t)
+{
+    if (!t->n_prop) return AMIE_OK;
+    k_proportional_solution<<<1, 32, 0, t->ctx->stream>>>(t->n_prop, t->prop_ids.p, t->prop_off.p, t->prop_ptr.p,
+                                                          t->prop_dofs.p, t->prop_coefs.p, t->x.p);
+    AMIE_LAUNCHED();
+    AMIE_CUDA(cudaGetLastError());
+    return AMIE_OK;
+}
+
 amie_status reapply_dirichlet_async(amie_topo *t)
 {
     cudaStream_t st = t->ctx->stream;
     if (t->has_rhs0) AMIE_CUDA(cudaMemcpyAsync(t->rhs.p, t->rhs0.p, t->n * 8, cudaMemcpyDeviceToDevice, st));
     AMIE_TRY(add_induced_forces_async(t));
-    return dirichlet_async(t, t->n_bc, t->bc_ids.p, t->bc_vals.p, t->has_bc_kinds ? t->bc_kinds.p : nullptr);
+    AMIE_TRY(dirichlet_async(t, t->n_bc, t->bc_ids.p, t->bc_vals.p, t->has_bc_kinds ? t->bc_kinds.p : nullptr));
+    if (t->n_prop) {
+        if (t->s == 2)
+            k_proportional<2><<<1, 256, 0, st>>>(t->row_ptr.p, t->col.p, t->val.p, t->rhs.p, t->n_prop, t->prop_ids.p,
+                                                t->prop_off.p, t->prop_ptr.p, t->prop_dofs.p, t->prop_coefs.p);
+        else
+            k_proportional<3><<<1, 256, 0, st>>>(t->row_ptr.p, t->col.p, t->val.p, t->rhs.p, t->n_prop, t->prop_ids.p,
+                                                t->prop_off.p, t->prop_ptr.p, t->prop_dofs.p, t->prop_coefs.p);
+        AMIE_LAUNCHED();
+        AMIE_CUDA(cudaGetLastError());
+    }
+    return AMIE_OK;
 }
 
 }  // namespace amie
@@ -1321,7 +1445,7 @@ extern "C" amie_status amie_assemble(amie_topo *t)
     if (!t) return AMIE_BAD_INPUT;
     AMIE_CUDA(cudaSetDevice(t->ctx->device));
     AMIE_TRY(assemble_async(t));
-    if (t->bc_set) AMIE_TRY(reapply_dirichlet_async(t));
+    if (t->bc_set || t->n_prop) AMIE_TRY(reapply_dirichlet_async(t));
     else AMIE_TRY(add_induced_forces_async(t));
     AMIE_TRY(finalize_matrix_async(t, false));
     AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
@@ -1453,6 +1577,51 @@ extern "C" amie_status amie_apply_dirichlet(amie_topo *t, uint32_t n_bc, const u
     t->bc_set = true;
     AMIE_TRY(reapply_dirichlet_async(t));
     AMIE_TRY(finalize_matrix_async(t, false));
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    return AMIE_OK;
+}
+
+extern "C" amie_status amie_set_proportional(amie_topo *t, uint32_t n, const uint32_t *ids, const double *offsets,
+                                             const uint32_t *ptr, const uint32_t *prop_ids, const double *coefs)
+{
+    if (!t || (n && (!ids || !offsets || !ptr))) return AMIE_BAD_INPUT;
+    if (n) {
+        if (ptr[0] != 0 || (ptr[n] && (!prop_ids || !coefs))) {
+            set_error("proportional multipliers: ptr must start at 0 and the DOF arrays be given");
+            return AMIE_BAD_INPUT;
+        }
+        for (uint32_t i = 0; i < n; i++) {
+            if (ids[i] >= t->n || ptr[i + 1] < ptr[i]) {
+                set_error("proportional multiplier %u: id %u (n %llu) or ptr out of order", i, ids[i],
+                          (unsigned long long)t->n);
+                return AMIE_BAD_INPUT;
+            }
+            for (uint32_t k = ptr[i]; k < ptr[i + 1]; k++)
+                if (prop_ids[k] >= t->n || prop_ids[k] == ids[i]) {
+                    set_error("proportional multiplier %u: DOF %u out of range or the constrained DOF", i, prop_ids[k]);
+                    return AMIE_BAD_INPUT;
+                }
+        }
+    }
+    AMIE_CUDA(cudaSetDevice(t->ctx->device));
+    cudaStream_t st = t->ctx->stream;
+    AMIE_CUDA(cudaStreamSynchronize(st));   // the stored arrays are replaced below
+    t->n_prop = n;
+    if (n) {
+        AMIE_TRY(upload(t->ctx, t->prop_ids, ids, n));
+        AMIE_TRY(upload(t->ctx, t->prop_off, offsets, n));
+        AMIE_TRY(upload(t->ctx, t->prop_ptr, ptr, (size_t)n + 1));
+        if (ptr[n]) {
+            AMIE_TRY(upload(t->ctx, t->prop_dofs, prop_ids, ptr[n]));
+            AMIE_TRY(upload(t->ctx, t->prop_coefs, coefs, ptr[n]));
+        }
+    }
+    if (t->assembled) {   // the original matrix, eliminated again with every stored multiplier
+        AMIE_TRY(assemble_async(t));
+        if (t->bc_set || t->n_prop) AMIE_TRY(reapply_dirichlet_async(t));
+        else AMIE_TRY(add_induced_forces_async(t));
+        AMIE_TRY(finalize_matrix_async(t, false));
+    }
     AMIE_CUDA(cudaStreamSynchronize(st));
     return AMIE_OK;
 }

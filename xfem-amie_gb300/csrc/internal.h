@@ -179,6 +179,9 @@ struct DamageState;
 }
 void release_damage(amie_topo *t);   // damage.cu
 void release_topology(amie_topo *t);   // assemble.cu: frees everything, no synchronisation
+namespace amie {
+amie_status proportional_solution_async(amie_topo *t);   // assemble.cu: u[id] = offset + sum c u[p]
+}
 
 // Opaque handles of the C-ABI.
 struct amie_ctx : public amie::Ctx {};
@@ -262,6 +265,10 @@ struct amie_topo {
     amie::DevArray<double> force_vals;
     uint32_t n_force = 0;
     bool force_unique = true;             // no DOF has two force multipliers
+    // proportional displacements (amie_set_proportional), applied after the elimination
+    amie::DevArray<uint32_t> prop_ids, prop_ptr, prop_dofs;
+    amie::DevArray<double> prop_off, prop_coefs;
+    uint32_t n_prop = 0;
     amie::DevArray<double> scal;   // solver scalars
     amie::DevArray<int32_t> flags; // solver control flags
 

@@ -936,6 +936,7 @@ amie_status solve_dispatch(amie_topo *t, const amie_solve_opts *o, amie_solve_st
         set_error("unknown solver %d", solver);
         return AMIE_BAD_INPUT;
     }
+    if (rc == AMIE_OK) AMIE_TRY(proportional_solution_async(t));
     AMIE_CUDA(cudaStreamSynchronize(t->ctx->stream));
     stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     t->last_solve_s = stats->seconds;

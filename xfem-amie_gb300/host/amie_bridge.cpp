@@ -63,7 +63,13 @@ bool gpuCgsolve(Assembly *K, gpu::Assembly &G, bool reuseTopology)
         G.setMaxDof(K->ndofmax);
     }
     for (auto &m : K->multipliers) {                                               // solvers/assembly.cpp:1590
-        if (m.type == SET_FORCE_XI || m.type == SET_FORCE_ETA || m.type == SET_FORCE_ZETA)
+        if (m.type == SET_PROPORTIONAL_DISPLACEMENT) {                             // :1636-1760
+            const std::valarray<unsigned int> dofs = m.getDofIds();
+            std::vector<std::pair<gpu::Variable, double>> val;
+            for (size_t k = 0; k < dofs.size(); k++)
+                val.emplace_back((gpu::Variable)(dofs[k] % K->ndof), m.coefs[k]);
+            G.setPointProportional((gpu::Variable)(m.getId() % K->ndof), val, m.getValue(), m.getId() / K->ndof);
+        } else if (m.type == SET_FORCE_XI || m.type == SET_FORCE_ETA || m.type == SET_FORCE_ZETA)
             G.setForceOn((gpu::Variable)(m.getId() % K->ndof), m.getValue(), m.getId() / K->ndof);
         else
             G.setPointAlong((gpu::Variable)(m.getId() % K->ndof), m.getValue(), m.getId() / K->ndof);

@@ -40,7 +40,31 @@ void Assembly::add(const Element &e)
 void Assembly::setPointAlong(Variable v, double val, size_t id)
 {
     const int s = dim_ ? dim_ : 2;
+    proportional_.erase((uint32_t)(id * s + (int)v));   // a later multiplier on a DOF replaces the earlier one
     multipliers_[(uint32_t)(id * s + (int)v)] = {val, (uint8_t)AMIE_BC_DISPLACEMENT};
+}
+
+void Assembly::setPointProportional(Variable v1, Variable v2, double val, double offset, size_t id)
+{
+    if (v1 == v2) return;
+    const int s = dim_ ? dim_ : 2;
+    const uint32_t dof = (uint32_t)(id * s + (int)v1);
+    multipliers_.erase(dof);
+    proportional_[dof] = Proportional{offset, {(uint32_t)(id * s + (int)v2)}, {val}};
+}
+
+void Assembly::setPointProportional(Variable v1, const std::vector<std::pair<Variable, double>> &val, double offset,
+                                    size_t id)
+{
+    const int s = dim_ ? dim_ : 2;
+    Proportional p{offset, {}, {}};
+    for (const auto &vc : val) {
+        p.dofs.push_back((uint32_t)(id * s + (int)vc.first));
+        p.coefs.push_back(vc.second);
+    }
+    const uint32_t dof = (uint32_t)(id * s + (int)v1);
+    multipliers_.erase(dof);
+    proportional_[dof] = std::move(p);
 }
 
 void Assembly::setForceOn(Variable v, double val, size_t id)
@@ -55,6 +79,7 @@ void Assembly::clear()
 {
     clearElements();
     multipliers_.clear();
+    proportional_.clear();
     history_.clear();
     displacements_.clear();
 }
@@ -166,6 +191,18 @@ void Assembly::make_final()
         vals.push_back(kv.second.first);
         kinds.push_back(kv.second.second);
     }
+    std::vector<uint32_t> pids, pptr{0}, pdofs;
+    std::vector<double> poff, pco;
+    for (const auto &kv : proportional_) {
+        pids.push_back(kv.first);
+        poff.push_back(kv.second.offset);
+        pdofs.insert(pdofs.end(), kv.second.dofs.begin(), kv.second.dofs.end());
+        pco.insert(pco.end(), kv.second.coefs.begin(), kv.second.coefs.end());
+        pptr.push_back((uint32_t)pdofs.size());
+    }
+    check(amie_set_proportional(topo_, (uint32_t)pids.size(), pids.data(), poff.data(), pptr.data(), pdofs.data(),
+                                pco.data()),
+          "amie_set_proportional");
     check(amie_apply_dirichlet(topo_, (uint32_t)ids.size(), ids.data(), vals.data(), kinds.data(), nullptr),
           "amie_apply_dirichlet");
 }

@@ -7,6 +7,8 @@
 //                            element at a time from plain element data
 //   setPointAlong / fixPoint Assembly::setPointAlong / fixPoint (:1590-1634, :1762)
 //   setForceOn               Assembly::setForceOn (SET_FORCE_INDEXED_AXIS, :1560-1588)
+//   setPointProportional     Assembly::setPointProportional (:1636-1697, :1699-1761): v1 =
+//                            sum val_k v_k + offset at one node (SET_PROPORTIONAL_DISPLACEMENT)
 //   setMaxDof, setEpsilon, setSSORIterations
 //   cgsolve(maxit)           Assembly::cgsolve (:1829-1953): make_final + solve,
 //                            warm start from extrapolate() (:1772-1814), keeps the
@@ -73,6 +75,9 @@ public:
     void setPointAlong(Variable v, double val, size_t id);
     void fixPoint(size_t id, Variable v) { setPointAlong(v, 0.0, id); }
     void setForceOn(Variable v, double val, size_t id);
+    void setPointProportional(Variable v1, Variable v2, double val, double offset, size_t id);
+    void setPointProportional(Variable v1, const std::vector<std::pair<Variable, double>> &val, double offset,
+                              size_t id);
 
     bool cgsolve(int maxit = -1, bool verbose = false);
 
@@ -102,6 +107,12 @@ private:
     int solver_ = AMIE_SOLVER_AMIE_CG;
     std::vector<Element> elements_;
     std::map<uint32_t, std::pair<double, uint8_t>> multipliers_;
+    struct Proportional {
+        double offset;
+        std::vector<uint32_t> dofs;
+        std::vector<double> coefs;
+    };
+    std::map<uint32_t, Proportional> proportional_;   // by constrained DOF, as make_final sorts them
     std::vector<double> displacements_;
     std::vector<std::vector<double>> history_;
     amie_solve_stats stats_{};
