@@ -640,7 +640,7 @@ def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 3
     t_setup = time.perf_counter()
     topo.damage_setup(law, meta["corners"])
     setup_s = time.perf_counter() - t_setup
-    per_step, total_passes, total_iters = [], 0, 0
+    per_step, total_passes, total_iters, total_smoothed = [], 0, 0, 0
     ctx.timer_start()
     for k in range(1, steps + 1):
         topo.apply_dirichlet(*bcs_at(deflection_max * k / steps))
@@ -649,6 +649,7 @@ def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 3
         per_step.append((st["sub_iterations"], st["damaged"], st["fractured"]))
         total_passes += st["sub_iterations"]
         total_iters += st["cg_iterations"]
+        total_smoothed += st["smoothed"]
     ms = ctx.timer_stop()
     dmg = topo.damage_state()
     topo.close()
@@ -660,6 +661,7 @@ def run_damage_loop(ctx, solver: int, steps: int = 60, deflection_max: float = 3
     out = {"steps": steps, "n_dof": int(n), "deflection_max_m": deflection_max, "ms_total": ms,
            "ms_per_step": ms / steps, "setup_s": setup_s, "passes_total": int(total_passes),
            "iterations_total": int(total_iters), "dof_iterations_per_s": n * total_iters / (ms / 1e3),
+           "smoothed_fraction": total_smoothed / max(1, total_passes * len(cen)),
            "first_damaged_step": first, "damaged_elements": int(hit.sum()),
            "fractured_elements": int((dmg >= 0.6).sum()), "max_damage": float(dmg.max()),
            "passes_per_step": [p[0] for p in per_step], "damaged_per_step": [p[1] for p in per_step],

@@ -415,7 +415,12 @@ AMIE_API amie_status amie_damage_set_state(amie_topo *topo, const double *damage
 AMIE_API amie_status amie_damage_get_state(amie_topo *topo, double *damage);
 /* Grade every element from the current solution; score [n_elem] (-1 for a
  * fractured element) and smoothed [n_elem*4] (principal smoothed stress, then
- * principal smoothed strain, each in toPrincipal's order) are optional host outputs. */
+ * principal smoothed strain, each in toPrincipal's order) are optional host outputs.
+ * Without `smoothed` (and in amie_damage_load_step) an element is not smoothed
+ * where a bound shows its smoothed strain below the threshold: no unfractured
+ * element of its neighbourhood's grid cells strains above it (the tensile
+ * strain norm is convex, the smoothing an average); its score is then -d, the
+ * same bits the smoothing gives. */
 AMIE_API amie_status amie_damage_grade(amie_topo *topo, double *score, double *smoothed);
 /* Step the damage model of every element from the last grade; n_changed:
  * elements whose damage grew. */
@@ -436,6 +441,7 @@ typedef struct amie_damage_step_stats {
     uint32_t damaged;          /* elements with damage > 0 at the end */
     uint32_t fractured;        /* elements at the cutoff */
     uint64_t changes;          /* damage increments of all passes */
+    uint64_t smoothed;         /* element smoothings of all passes (the others' scores were bounded) */
     double seconds;
 } amie_damage_step_stats;
 AMIE_API amie_status amie_damage_load_step(amie_topo *topo, const amie_solve_opts *opts, int32_t max_sub_iterations,

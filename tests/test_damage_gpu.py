@@ -2,7 +2,8 @@
 reference's notched beam (fixture damage_p1) and the oracle.
 
 * grading: from the reference's displacements and damage after each load step,
-  the device scores and smoothed principal fields equal the reference's to 1e-12;
+  the device scores and smoothed principal fields equal the reference's to 1e-12,
+  and the bounded grading (no smoothed fields wanted) gives the same score bits;
 * update: on a state with elements about to fracture, the device step equals
   the oracle's (same damage, same number of changes), including the rule that
   an element fractured earlier in a pass leaves the neighbourhood maxima of the
@@ -50,6 +51,9 @@ def test_device_grade_matches_reference(gpu_ctx):
             t.damage_set_state(state_of(d[f"damage_{k}"]))
             t.solution_upload(d[f"u_{k}"])
             score, sm = t.damage_grade()
+            bounded, none = t.damage_grade(smoothed=False)
+            assert none is None
+            assert np.array_equal(bounded.view(np.uint64), score.view(np.uint64)), k
             ref = d[f"score_{k}"]
             assert np.array_equal(score == -1.0, ref == -1.0), k
             assert np.abs(score - ref).max() <= 1e-12, k
@@ -112,6 +116,11 @@ def test_device_load_steps_match_reference(gpu_ctx, solver, rtol, utol):
             t.apply_dirichlet(ids, d["bc_values"] * (float(d["deflection"][0]) * k / nsteps), kinds)
             st = t.damage_load_step(sv, rtol=rtol, warm=k > 1)
             assert st["sub_iterations"] == int(d["sub_iterations"][k - 1]), (k, st)
+            assert st["smoothed"] <= st["sub_iterations"] * m.n_elem, (k, st)
+            if k > 1:   # damage grows: the elements that meet the criterion were smoothed
+                assert st["smoothed"] > 0, (k, st)
+            else:   # below the threshold away from the notch: most elements skip the smoothing
+                assert st["smoothed"] < m.n_elem, st
             state = t.damage_state()
             assert np.abs(exported(state) - d[f"damage_{k}"]).max() <= 1e-12, k
             assert st["damaged"] == int((d[f"damage_{k}"] > 0).sum())

@@ -65,7 +65,7 @@ class DamageLaw(C.Structure):
 class DamageStepStats(C.Structure):
     _fields_ = [("sub_iterations", C.c_int32), ("status", C.c_int32), ("cg_iterations", C.c_int64),
                 ("damaged", C.c_uint32), ("fractured", C.c_uint32), ("changes", C.c_uint64),
-                ("seconds", C.c_double)]
+                ("smoothed", C.c_uint64), ("seconds", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -377,12 +377,13 @@ class Topology:
         check(lib().amie_damage_get_state(self.ptr, _p(dm)), "amie_damage_get_state")
         return dm
 
-    def damage_grade(self):
-        """(score [n_elem], smoothed principal stress and strain [n_elem, 4]) from the device solution."""
+    def damage_grade(self, smoothed=True):
+        """(score [n_elem], smoothed principal stress and strain [n_elem, 4]) from the device solution;
+        with smoothed=False only the scores (bounded grading, the same scores), smoothed None."""
         sc = np.zeros(self.mesh.n_elem, np.float64)
-        sm = np.zeros(self.mesh.n_elem * 4, np.float64)
-        check(lib().amie_damage_grade(self.ptr, _p(sc), _p(sm)), "amie_damage_grade")
-        return sc, sm.reshape(-1, 4)
+        sm = np.zeros(self.mesh.n_elem * 4, np.float64) if smoothed else None
+        check(lib().amie_damage_grade(self.ptr, _p(sc), _p(sm) if smoothed else None), "amie_damage_grade")
+        return sc, (sm.reshape(-1, 4) if smoothed else None)
 
     def damage_update(self) -> int:
         n = C.c_uint32()

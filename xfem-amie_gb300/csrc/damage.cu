@@ -68,6 +68,11 @@ struct DamageState {
     DevArray<double> nmax;
     size_t cub_bytes = 0;
     bool dirty = false;   // damage changed since the stiffness was last assembled
+    // the centres' grid of the set-up, kept for the bounded grading: per cell the
+    // largest equivalent strain of its unfractured elements (float bits, rounded up)
+    Grid grid{};
+    DevArray<uint32_t> cell_start, cell_items, cell_of, cell_max;
+    DevArray<unsigned long long> n_smoothed;   // elements smoothed by the gradings since the last reset
 };
 
 namespace {
@@ -115,20 +120,31 @@ __device__ __forceinline__ void principal(const double *v, bool engineering, dou
 
 // NonLocalMazars::gradeAtTime, 2D plane stress: the branch sets tensionOnly,
 // so talpha = 1, calpha = 0.
+// The tensile strain norm of gradeAtTime (mazars.cpp:100-112) from principal
+// strains: sqrt(<e0>+^2 + <e1>+^2 + <ezz>+^2), ezz = -nu (e0 + e1) / (1 - nu).
+// As a function of the strain tensor it is convex (a symmetric convex function
+// of the eigenvalues, the positive parts of linear forms under a monotone norm),
+// so on a weighted average of strains it is at most the largest value on the
+// averaged strains.
+__device__ __forceinline__ double mazars_norm(const DamageConst &k, const double *strain)
+{
+    const double strainzz = -k.nu * (strain[0] + strain[1]) / (1. - k.nu);
+    const double p0 = 0.5 * (fabs(strain[0]) + strain[0]);
+    const double p1 = 0.5 * (fabs(strain[1]) + strain[1]);
+    const double pz = 0.5 * (fabs(strainzz) + strainzz);
+    return sqrt(p0 * p0 + p1 * p1 + pz * pz);
+}
+
 __device__ __forceinline__ double mazars(const DamageConst &k, const double *stress, const double *strain,
                                          double dama_predict)
 {
-    const double strainzz = -k.nu * (strain[0] + strain[1]) / (1. - k.nu);
     double gamma = 1.0;
     const double Trtsig = 0.5 * (fabs(stress[0]) + stress[0]) + 0.5 * (fabs(stress[1]) + stress[1]);
     const double Trcsig = fmin(0.0, stress[0]) + fmin(0.0, stress[1]);
     if (Trcsig < -kPointTolerance && fabs(Trtsig / Trcsig) < 1e-8)
         gamma = sqrt(fmin(0.0, stress[0]) * fmin(0.0, stress[0]) + fmin(0.0, stress[1]) * fmin(0.0, stress[1])) /
                 (-Trcsig);
-    const double p0 = 0.5 * (fabs(strain[0]) + strain[0]);
-    const double p1 = 0.5 * (fabs(strain[1]) + strain[1]);
-    const double pz = 0.5 * (fabs(strainzz) + strainzz);
-    const double maxStrain = gamma * fmax(0.0, sqrt(p0 * p0 + p1 * p1 + pz * pz));
+    const double maxStrain = gamma * fmax(0.0, mazars_norm(k, strain));
     const double talpha = 1.0, calpha = 1.0 - talpha;
     const double tt = k.threshold < maxStrain ? maxStrain : k.threshold;
     const double t = talpha * (1. - (k.threshold / tt) * exp(-k.B_t * (tt - k.threshold))) +
@@ -214,14 +230,46 @@ __global__ void k_dmg_cache_norm(uint32_t E, const uint64_t *ptr, double *coef)
 // most POINT_TOLERANCE contributes a zero strain but its weight,
 // elements/integrable_entity.cpp:2112-2131), the element's own damaged stress
 // from it, principal values, Mazars score (-1 for a fractured element).
+//
+// Bounded (cell_max != nullptr, smoothed fields not wanted): an element whose
+// smoothing cells hold no unfractured element with an equivalent strain above
+// the threshold (with a relative margin of 1e-6 for rounding) has a smoothed
+// equivalent strain at or below the threshold (mazars_norm is convex and the
+// smoothing a weighted average), so gradeAtTime's score is 0 - d whatever the
+// smoothed strain: it is formed from zero strains, bit for bit the value of
+// the full evaluation, and the smoothing is skipped.  A fractured element's
+// score is -1 either way.  Its smoothed fields are then not written.
 __global__ void __launch_bounds__(128) k_dmg_grade(uint32_t E, DamageConst k, const double *strain,
                                                    const uint32_t *mat, const double *cmat_table, const double *state,
                                                    const double *area, const double *gpw, const uint64_t *ptr,
                                                    const uint32_t *idx, const double *coef, double *score,
-                                                   double *smoothed)
+                                                   double *smoothed, Grid grid, const uint32_t *cell_max,
+                                                   const double *centre, const double *radius,
+                                                   unsigned long long *n_smoothed)
 {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
+    if (cell_max) {
+        const bool fre = state[e] >= k.cutoff;
+        float m = 0.f;
+        if (!fre) {   // the cells k_dmg_cache searched for this element's neighbours
+            const double re = radius[e], Re = reff(k.radius, re), rho = smoothing_radius(Re, re);
+            const double cx = centre[2 * e], cy = centre[2 * e + 1];
+            const int ix0 = max(0, (int)floor((cx - rho * 1.01 - grid.x0) / grid.h));
+            const int ix1 = min(grid.nx - 1, (int)floor((cx + rho * 1.01 - grid.x0) / grid.h));
+            const int iy0 = max(0, (int)floor((cy - rho * 1.01 - grid.y0) / grid.h));
+            const int iy1 = min(grid.ny - 1, (int)floor((cy + rho * 1.01 - grid.y0) / grid.h));
+            for (int iy = iy0; iy <= iy1; iy++)
+                for (int ix = ix0; ix <= ix1; ix++) m = fmaxf(m, __uint_as_float(cell_max[iy * grid.nx + ix]));
+        }
+        if (fre || (double)m * (1. + 1e-6) <= k.threshold) {
+            const double zero[2] = {0., 0.};
+            score[e] = fre ? -1. : mazars(k, zero, zero, state[e]);
+            return;
+        }
+        const unsigned act = __activemask();
+        if ((int)(threadIdx.x & 31) == __ffs(act) - 1) atomicAdd(n_smoothed, (unsigned long long)__popc(act));
+    }
     double sc[3] = {0, 0, 0}, corr[3] = {0, 0, 0}, sum = 0;
     for (uint64_t q = ptr[e]; q < ptr[e + 1]; q++) {
         const uint32_t j = idx[q];
@@ -253,11 +301,25 @@ __global__ void __launch_bounds__(128) k_dmg_grade(uint32_t E, DamageConst k, co
     double ps[2], pe[2];
     principal(sig, false, ps);
     principal(sc, true, pe);
+    score[e] = fr ? -1. : mazars(k, ps, pe, state[e]);
+    if (cell_max) return;
     smoothed[4 * (size_t)e] = ps[0];
     smoothed[4 * (size_t)e + 1] = ps[1];
     smoothed[4 * (size_t)e + 2] = pe[0];
     smoothed[4 * (size_t)e + 3] = pe[1];
-    score[e] = fr ? -1. : mazars(k, ps, pe, state[e]);
+}
+
+// Per grid cell, the largest tensile strain norm of its unfractured elements'
+// own strains (rounded up to float; non-negative floats order like their bits).
+__global__ void k_dmg_cell_max(uint32_t E, DamageConst k, const double *strain, const double *state,
+                               const uint32_t *cell_of, uint32_t *cell_max)
+{
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E || state[e] >= k.cutoff) return;
+    double pe[2];
+    principal(strain + (size_t)e * 3, true, pe);
+    const double f = mazars_norm(k, pe);
+    if (f > 0.) atomicMax(cell_max + cell_of[e], __float_as_uint(__double2float_ru(f)));
 }
 
 __global__ void k_dmg_met(uint32_t E, const double *score, uint8_t *flag)
@@ -518,13 +580,18 @@ extern "C" amie_status amie_damage_setup(amie_topo *t, const amie_damage_law *la
         std::vector<uint32_t> fill(cell_start.begin(), cell_start.end() - 1);
         for (uint32_t e = 0; e < E; e++) items[fill[cell_of[e]]++] = e;
     }
-    DevArray<uint32_t> d_cell_start, d_items;
-    AMIE_TRY(d_cell_start.alloc(c, ncell + 1));
-    AMIE_TRY(d_items.alloc(c, E));
-    AMIE_CUDA(cudaMemcpyAsync(d_cell_start.p, cell_start.data(), (ncell + 1) * 4, cudaMemcpyHostToDevice, st));
-    AMIE_CUDA(cudaMemcpyAsync(d_items.p, items.data(), (size_t)E * 4, cudaMemcpyHostToDevice, st));
-    g.cell_start = d_cell_start.p;
-    g.items = d_items.p;
+    AMIE_TRY(d->cell_start.alloc(c, ncell + 1));
+    AMIE_TRY(d->cell_items.alloc(c, E));
+    AMIE_TRY(d->cell_of.alloc(c, E));
+    AMIE_TRY(d->cell_max.alloc(c, ncell));
+    AMIE_TRY(d->n_smoothed.alloc(c, 1));
+    AMIE_CUDA(cudaMemsetAsync(d->n_smoothed.p, 0, 8, st));
+    AMIE_CUDA(cudaMemcpyAsync(d->cell_start.p, cell_start.data(), (ncell + 1) * 4, cudaMemcpyHostToDevice, st));
+    AMIE_CUDA(cudaMemcpyAsync(d->cell_items.p, items.data(), (size_t)E * 4, cudaMemcpyHostToDevice, st));
+    AMIE_CUDA(cudaMemcpyAsync(d->cell_of.p, cell_of.data(), (size_t)E * 4, cudaMemcpyHostToDevice, st));
+    g.cell_start = d->cell_start.p;
+    g.items = d->cell_items.p;
+    d->grid = g;
 
     // neighbourhoods: count, scan, fill, normalise
     DevArray<uint64_t> counts;
@@ -612,14 +679,26 @@ extern "C" amie_status amie_damage_get_state(amie_topo *t, double *damage)
 namespace amie {
 namespace {
 
-amie_status grade_async(amie_topo *t)
+// Scores of every element from the current solution; with `bounded` the
+// smoothing is skipped where the cell bound proves the score (k_dmg_grade) and
+// the smoothed fields are not written.
+amie_status grade_async(amie_topo *t, bool bounded)
 {
     DamageState *d = t->dmg;
     cudaStream_t st = t->ctx->stream;
     AMIE_TRY(element_strain_async(t));
+    if (bounded) {
+        const Grid &g = d->grid;
+        AMIE_CUDA(cudaMemsetAsync(d->cell_max.p, 0, (size_t)g.nx * g.ny * 4, st));
+        k_dmg_cell_max<<<blocks(d->n_elem, 256), 256, 0, st>>>(d->n_elem, d->k, t->strain.p, d->state.p,
+                                                               d->cell_of.p, d->cell_max.p);
+        AMIE_LAUNCHED();
+    }
     k_dmg_grade<<<blocks(d->n_elem, 128), 128, 0, st>>>(d->n_elem, d->k, t->strain.p, t->mat.p, t->cmat_table.p,
                                                         d->state.p, d->area.p, d->gpw.p, d->nb_ptr.p, d->nb_idx.p,
-                                                        d->nb_coef.p, d->score.p, d->smoothed.p);
+                                                        d->nb_coef.p, d->score.p, d->smoothed.p, d->grid,
+                                                        bounded ? d->cell_max.p : nullptr, d->centre.p, d->radius.p,
+                                                        d->n_smoothed.p);
     AMIE_LAUNCHED();
     AMIE_CUDA(cudaGetLastError());
     return AMIE_OK;
@@ -662,7 +741,7 @@ extern "C" amie_status amie_damage_grade(amie_topo *t, double *score, double *sm
     AMIE_TRY(need_damage(t));
     AMIE_CUDA(cudaSetDevice(t->ctx->device));
     cudaStream_t st = t->ctx->stream;
-    AMIE_TRY(grade_async(t));
+    AMIE_TRY(grade_async(t, smoothed == nullptr));
     const uint32_t E = t->dmg->n_elem;
     if (score) AMIE_CUDA(cudaMemcpyAsync(score, t->dmg->score.p, (size_t)E * 8, cudaMemcpyDeviceToHost, st));
     if (smoothed) AMIE_CUDA(cudaMemcpyAsync(smoothed, t->dmg->smoothed.p, (size_t)E * 32, cudaMemcpyDeviceToHost, st));
@@ -696,6 +775,7 @@ extern "C" amie_status amie_damage_load_step(amie_topo *t, const amie_solve_opts
     amie_solve_opts o = opts ? *opts : amie_solve_opts{AMIE_SOLVER_PCG_FP64, 1e-10, 1e-10, 32, 0, 0.0, 0};
     const int32_t cap = max_sub_iterations > 0 ? max_sub_iterations : 10000;
     s.status = AMIE_NOT_CONVERGED;
+    AMIE_CUDA(cudaMemsetAsync(d->n_smoothed.p, 0, 8, st));
     for (int32_t pass = 0; pass < cap; pass++) {
         if (d->dirty) {   // the damaged stiffness, eliminated with the stored multipliers
             AMIE_TRY(amie_assemble(t));
@@ -710,7 +790,7 @@ extern "C" amie_status amie_damage_load_step(amie_topo *t, const amie_solve_opts
         o.use_x0 = 1;   // the next passes start from this solution
         s.cg_iterations += ss.iterations;
         s.sub_iterations++;
-        AMIE_TRY(grade_async(t));
+        AMIE_TRY(grade_async(t, true));
         uint32_t changed = 0;
         AMIE_TRY(update(t, &changed));
         s.changes += changed;
@@ -723,10 +803,13 @@ extern "C" amie_status amie_damage_load_step(amie_topo *t, const amie_solve_opts
     k_dmg_counts<<<blocks(d->n_elem, 256), 256, 0, st>>>(d->n_elem, d->state.p, d->k.cutoff, d->counters.p);
     AMIE_LAUNCHED();
     uint32_t h[2] = {0, 0};
+    unsigned long long ns = 0;
     AMIE_CUDA(cudaMemcpyAsync(h, d->counters.p + 2, 8, cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaMemcpyAsync(&ns, d->n_smoothed.p, 8, cudaMemcpyDeviceToHost, st));
     AMIE_CUDA(cudaStreamSynchronize(st));
     s.damaged = h[0];
     s.fractured = h[1];
+    s.smoothed = ns;
     s.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) *stats = s;
     return (amie_status)s.status;
