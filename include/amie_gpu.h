@@ -208,7 +208,10 @@ AMIE_API amie_status amie_apply_dirichlet(amie_topo *topo, uint32_t n_bc, const 
  * solve (Assembly::cgsolve, solvers/assembly.cpp:1881-1892).  An assembled
  * topology is assembled and eliminated again with every stored multiplier;
  * amie_assemble applies them with or without a Dirichlet list.  n = 0 removes
- * them. */
+ * them.  A DOF carries one multiplier, as the reference's setters keep it (each
+ * erases an earlier multiplier of its DOF): an id given twice here, or given
+ * here and as a displacement to amie_apply_dirichlet (in either order), is
+ * AMIE_BAD_INPUT and changes nothing. */
 AMIE_API amie_status amie_set_proportional(amie_topo *topo, uint32_t n, const uint32_t *ids, const double *offsets,
                                            const uint32_t *ptr, const uint32_t *prop_ids, const double *coefs);
 

@@ -84,3 +84,86 @@ def test_device_proportional(gpu_ctx, solver):
         t2.close()
     finally:
         t.close()
+
+
+@pytest.mark.gpu
+def test_device_proportional_conflicts(gpu_ctx):
+    """One multiplier per DOF: a proportional id given twice, or also fixed by the
+    Dirichlet list (in either order), is refused and leaves the topology as it was."""
+    import amie_gpu as G
+    d = load_golden("prop_p1")
+    m = am.from_golden(d, "auto")
+    ids, offs, ptr, pids, coefs = am.golden_proportional(d)
+    bc_ids, bc_vals, bc_kinds = am.golden_bcs(d)
+    t = G.Topology(gpu_ctx, m)
+    try:
+        t.assemble()
+        t.set_proportional(ids, offs, ptr, pids, coefs)
+        t.apply_dirichlet(bc_ids, bc_vals, bc_kinds)
+        arr, rhs = t.matrix()
+        dup = np.concatenate([ids, ids[:1]])
+        with pytest.raises(G.AmieError, match="BAD_INPUT"):
+            t.set_proportional(dup, np.concatenate([offs, offs[:1]]), np.concatenate([ptr, ptr[-1:] + 1]),
+                               np.concatenate([pids, pids[:1]]), np.concatenate([coefs, coefs[:1]]))
+        fixed = np.concatenate([bc_ids, ids[:1]])
+        order = np.argsort(fixed, kind="stable")
+        with pytest.raises(G.AmieError, match="BAD_INPUT"):
+            t.apply_dirichlet(fixed[order], np.concatenate([bc_vals, [0.0]])[order],
+                              np.concatenate([bc_kinds, [am.BC_DISPLACEMENT]]).astype(np.uint8)[order])
+        arr2, rhs2 = t.matrix()
+        assert np.array_equal(arr2, arr) and np.array_equal(rhs2, rhs)
+        # the other order: the Dirichlet list first, then a proportional multiplier on a fixed DOF
+        t2 = G.Topology(gpu_ctx, m)
+        t2.assemble()
+        t2.apply_dirichlet(bc_ids, bc_vals, bc_kinds)
+        with pytest.raises(G.AmieError, match="BAD_INPUT"):
+            t2.set_proportional(bc_ids[:1], np.zeros(1), np.array([0, 1], np.uint32),
+                                np.array([bc_ids[0] ^ 1], np.uint32), np.ones(1))
+        t2.close()
+    finally:
+        t.close()
+
+
+@pytest.mark.gpu
+def test_assembly_mirror_proportional(gpu_ctx):
+    """The Python Assembly mirror: setPointProportional gives the reference's
+    post-solve displacements; moving a DOF between the displacement and the
+    proportional multipliers between two solves gives what a fresh Assembly
+    with the final multipliers gives."""
+    import amie_gpu as G
+    d = load_golden("prop_p1")
+    m = am.from_golden(d, "auto")
+    ids, offs, ptr, pids, coefs = am.golden_proportional(d)
+    bc_ids, bc_vals, _ = am.golden_bcs(d)
+
+    def build():
+        A = G.Assembly(gpu_ctx)
+        A.add(m)
+        for i, v in zip(bc_ids, bc_vals):
+            A.setPointAlong(int(i) % 2, float(v), int(i) // 2)
+        for k, i in enumerate(ids):
+            assert ptr[k + 1] - ptr[k] == 1 and pids[ptr[k]] // 2 == i // 2
+            A.setPointProportional(int(i) % 2, int(pids[ptr[k]]) % 2, float(coefs[ptr[k]]), float(offs[k]),
+                                   int(i) // 2)
+        A.setSolver(G.SOLVER_PCG_FP64, 1e-12)
+        return A
+
+    A = build()
+    assert A.cgsolve()
+    assert rel(A.getDisplacements(), d["u_post"]) <= 1e-8
+    # the first proportional DOF becomes fixed, the first fixed DOF of another node proportional
+    moved_fixed = int(ids[0])
+    free = next(int(i) for i in bc_ids if i // 2 != moved_fixed // 2)
+    for B in (A, None):
+        B = B or build()
+        B.setPointAlong(moved_fixed % 2, 0.0, moved_fixed // 2)
+        B.setPointProportional(free % 2, [(1 - free % 2, 0.25)], None, 0.0, free // 2)
+        assert B.cgsolve()
+        if B is A:
+            u_moved = A.getDisplacements().copy()
+            arr_moved = A.getMatrix()[2].copy()
+        else:
+            assert np.array_equal(B.getMatrix()[2], arr_moved)
+            assert rel(B.getDisplacements(), u_moved) <= 1e-10
+    assert abs(u_moved[moved_fixed]) <= 1e-10 * np.abs(u_moved).max()
+    assert abs(u_moved[free] - 0.25 * u_moved[free ^ 1]) <= 1e-15 * np.abs(u_moved).max()

@@ -487,6 +487,8 @@ class Assembly:
         self.mesh: Optional[am.MeshData] = None
         self.topo: Optional[Topology] = None
         self.multipliers = {}        # dof id -> (value, kind)
+        self.proportional = {}       # dof id -> (offset, [dof ids], [coefficients])
+        self._topo_has_proportional = False
         self.epsilon = 1e-10
         self.nssor = 32
         self.solver = SOLVER_PCG_FP64
@@ -523,15 +525,31 @@ class Assembly:
 
     # multipliers -------------------------------------------------------
     def setPointAlong(self, axis: int, value: float, node_id: int):
-        self.multipliers[node_id * self.mesh.stride + axis] = (float(value), am.BC_DISPLACEMENT)
+        dof = node_id * self.mesh.stride + axis
+        self.proportional.pop(dof, None)   # one multiplier per DOF, the last one set
+        self.multipliers[dof] = (float(value), am.BC_DISPLACEMENT)
+
+    def setPointProportional(self, axis: int, other, value, offset: float, node_id: int):
+        """Assembly::setPointProportional (solvers/assembly.cpp:1636-1761): u_axis = value u_other
+        + offset at one node; `other` may instead be a list of (axis, coefficient) pairs (value
+        then unused), the reference's second overload."""
+        s = self.mesh.stride
+        pairs = list(other) if isinstance(other, (list, tuple)) else [(other, value)]
+        if len(pairs) == 1 and pairs[0][0] == axis:
+            return   # v1 == v2 is ignored by the reference
+        dof = node_id * s + axis
+        self.multipliers.pop(dof, None)
+        self.proportional[dof] = (float(offset), [node_id * s + int(a) for a, _ in pairs],
+                                  [float(c) for _, c in pairs])
 
     def fixPoint(self, node_id: int, axis: int):
         self.setPointAlong(axis, 0.0, node_id)
 
     def setForceOn(self, axis: int, value: float, node_id: int):
         key = node_id * self.mesh.stride + axis
-        old = self.multipliers.get(key, (0.0, am.BC_FORCE))
-        self.multipliers[key] = (old[0] + float(value), am.BC_FORCE)
+        old = self.multipliers.get(key)
+        base = old[0] if old is not None and old[1] == am.BC_FORCE else 0.0   # forces on a DOF accumulate
+        self.multipliers[key] = (base + float(value), am.BC_FORCE)
 
     def setMultipliers(self, ids, values, kinds=None):
         kinds = np.zeros(len(ids), np.uint8) if kinds is None else kinds
@@ -540,6 +558,7 @@ class Assembly:
 
     def clear(self):
         self.multipliers.clear()
+        self.proportional.clear()
         self.topo = None
         self.history.clear()
 
@@ -550,11 +569,24 @@ class Assembly:
                 self.mesh.ndofmax = self.ndofmax
             self.topo = Topology(self.ctx, self.mesh)
             self._dirty_topology = False
+            self._topo_has_proportional = False
         self.topo.assemble()
         ids = np.array(sorted(self.multipliers), np.uint32)
         vals = np.array([self.multipliers[i][0] for i in ids], np.float64)
         kinds = np.array([self.multipliers[i][1] for i in ids], np.uint8)
+        if self._topo_has_proportional:   # a DOF may have moved between the lists: old ones go first
+            self.topo.set_proportional(np.zeros(0, np.uint32), np.zeros(0), np.zeros(1, np.uint32),
+                                       np.zeros(0, np.uint32), np.zeros(0))
+            self._topo_has_proportional = False
         self.topo.apply_dirichlet(ids, vals, kinds)
+        if self.proportional:
+            pids = sorted(self.proportional)
+            ptr = np.cumsum([0] + [len(self.proportional[i][1]) for i in pids]).astype(np.uint32)
+            self.topo.set_proportional(np.array(pids, np.uint32),
+                                       np.array([self.proportional[i][0] for i in pids], np.float64), ptr,
+                                       np.array([d for i in pids for d in self.proportional[i][1]], np.uint32),
+                                       np.array([c for i in pids for c in self.proportional[i][2]], np.float64))
+            self._topo_has_proportional = True
 
     def extrapolate(self):
         """Assembly::extrapolate (factor 1): 2 u_k - u_(k-1) from the two-entry

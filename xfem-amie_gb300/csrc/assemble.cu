@@ -1542,6 +1542,15 @@ extern "C" amie_status amie_apply_dirichlet(amie_topo *t, uint32_t n_bc, const u
             set_error("multiplier %u: id %u >= n %llu", i, ids[i], (unsigned long long)t->n);
             return AMIE_BAD_INPUT;
         }
+    std::vector<uint32_t> fixed;
+    for (uint32_t i = 0; i < n_bc; i++)
+        if (!kinds || kinds[i] != AMIE_BC_FORCE) fixed.push_back(ids[i]);
+    std::sort(fixed.begin(), fixed.end());
+    for (uint32_t id : fixed)
+        if (std::binary_search(t->prop_sorted.begin(), t->prop_sorted.end(), id)) {
+            set_error("DOF %u has a displacement and a proportional multiplier", id);
+            return AMIE_BAD_INPUT;
+        }
     AMIE_CUDA(cudaSetDevice(t->ctx->device));
     cudaStream_t st = t->ctx->stream;
     if (t->eliminated) {   // re-eliminating needs the original matrix
@@ -1571,6 +1580,7 @@ extern "C" amie_status amie_apply_dirichlet(amie_topo *t, uint32_t n_bc, const u
             AMIE_TRY(upload(t->ctx, t->force_vals, fval.data(), fval.size()));
         }
     }
+    t->fixed_sorted = std::move(fixed);
     t->has_rhs0 = rhs0 != nullptr;
     if (rhs0) AMIE_TRY(upload(t->ctx, t->rhs0, rhs0, t->n));
     else AMIE_CUDA(cudaMemsetAsync(t->rhs.p, 0, t->n * 8, st));
@@ -1603,10 +1613,23 @@ extern "C" amie_status amie_set_proportional(amie_topo *t, uint32_t n, const uin
                 }
         }
     }
+    std::vector<uint32_t> sorted(ids, ids + n);
+    std::sort(sorted.begin(), sorted.end());
+    for (uint32_t i = 0; i < n; i++) {
+        if (i && sorted[i] == sorted[i - 1]) {
+            set_error("proportional multipliers: DOF %u appears twice", sorted[i]);
+            return AMIE_BAD_INPUT;
+        }
+        if (std::binary_search(t->fixed_sorted.begin(), t->fixed_sorted.end(), sorted[i])) {
+            set_error("DOF %u has a displacement and a proportional multiplier", sorted[i]);
+            return AMIE_BAD_INPUT;
+        }
+    }
     AMIE_CUDA(cudaSetDevice(t->ctx->device));
     cudaStream_t st = t->ctx->stream;
     AMIE_CUDA(cudaStreamSynchronize(st));   // the stored arrays are replaced below
     t->n_prop = n;
+    t->prop_sorted = std::move(sorted);
     if (n) {
         AMIE_TRY(upload(t->ctx, t->prop_ids, ids, n));
         AMIE_TRY(upload(t->ctx, t->prop_off, offsets, n));

@@ -269,6 +269,9 @@ struct amie_topo {
     amie::DevArray<uint32_t> prop_ids, prop_ptr, prop_dofs;
     amie::DevArray<double> prop_off, prop_coefs;
     uint32_t n_prop = 0;
+    // sorted host copies for the check that no DOF is both fixed and proportional
+    // (the reference's setters keep one multiplier per DOF)
+    std::vector<uint32_t> fixed_sorted, prop_sorted;
     amie::DevArray<double> scal;   // solver scalars
     amie::DevArray<int32_t> flags; // solver control flags
 

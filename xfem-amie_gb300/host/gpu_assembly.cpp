@@ -180,6 +180,7 @@ void Assembly::make_final()
         if (topo_) amie_topology_destroy(topo_);
         topo_ = nullptr;
         check(amie_topology_build(ctx_, &m, &topo_), "amie_topology_build");
+        topoHasProportional_ = false;
         topologyDirty_ = false;
     }
     check(amie_assemble(topo_), "amie_assemble");
@@ -200,11 +201,21 @@ void Assembly::make_final()
         pco.insert(pco.end(), kv.second.coefs.begin(), kv.second.coefs.end());
         pptr.push_back((uint32_t)pdofs.size());
     }
-    check(amie_set_proportional(topo_, (uint32_t)pids.size(), pids.data(), poff.data(), pptr.data(), pdofs.data(),
-                                pco.data()),
-          "amie_set_proportional");
+    // a DOF may have moved between the two lists since the last make_final: the
+    // old proportional multipliers go first, so that no DOF is in both at once
+    if (topoHasProportional_) {
+        const uint32_t zero = 0;
+        check(amie_set_proportional(topo_, 0, nullptr, nullptr, &zero, nullptr, nullptr), "amie_set_proportional");
+        topoHasProportional_ = false;
+    }
     check(amie_apply_dirichlet(topo_, (uint32_t)ids.size(), ids.data(), vals.data(), kinds.data(), nullptr),
           "amie_apply_dirichlet");
+    if (!pids.empty()) {
+        check(amie_set_proportional(topo_, (uint32_t)pids.size(), pids.data(), poff.data(), pptr.data(),
+                                    pdofs.data(), pco.data()),
+              "amie_set_proportional");
+        topoHasProportional_ = true;
+    }
 }
 
 std::vector<double> Assembly::extrapolate() const

@@ -100,6 +100,7 @@ private:
     amie_ctx *ctx_ = nullptr;
     amie_topo *topo_ = nullptr;
     bool topologyDirty_ = true;
+    bool topoHasProportional_ = false;   // the topology holds proportional multipliers
     size_t ndofmax_ = 0;
     double epsilon_ = 1e-10;
     double rtol_ = 1e-10;
