@@ -11,6 +11,7 @@
 //                          with its search direction kept (no Krylov restart).
 //   AMIE_SOLVER_AMIE_CG    ConjugateGradient::solve semantics (amie_cg.cu).
 #include "solver.cuh"
+#include "persist.cuh"
 
 #include <chrono>
 #include <cstdlib>
@@ -119,6 +120,21 @@ struct SolverState {
     DevArray<float> zw32[2];         // per node: z then w = D^-1 q (2 s floats), double-buffered
     DevArray<double> slice5;
     cudaGraphExec_t graph_fused = nullptr;
+    // Runs of the standard PCG as one cooperative launch (k_pcg_persist) instead
+    // of graphs of kernels; opt-in (AMIE_PERSIST=1).  Measured against the graphs
+    // (mixed, rtol 1e-10): 44.6 k-DOF P1 23.4 vs 22.6 ms (25.2 ms with an
+    // atomicAdd arrival and a sleeping poll), the 250 k-DOF notched beam's
+    // 60-step damage loop 35.0 vs 32.0 s, 824 k-DOF voxel tetrahedra 73.1 vs
+    // 63.7 ms; same iterations.  A grid barrier with the partial sums after it
+    // costs more than a PDL kernel boundary, and the SpMV phase with 24 warps
+    // per SM runs slower than k_sell_dir with 32 and its early prefetch.
+    int persist_mode = 0;
+    int grid_persist[2] = {0, 0};    // FP32 / FP64: one CTA per SM, 0 = not possible
+    DevArray<PersistSync> psync;
+    PersistSync *h_psync = nullptr;  // pinned
+    // AMIE_PERSIST_BARRIER_TEST=1 (tests): the barriers wait for one arrival more
+    // than the grid has and give up after 4096 polls
+    bool persist_barrier_test = false;
     ~SolverState()
     {
         if (graph64) cudaGraphExecDestroy(graph64);
@@ -127,6 +143,7 @@ struct SolverState {
         if (graph_fused) cudaGraphExecDestroy(graph_fused);
         pinned_put(h_ctl, sizeof(PcgCtl));
         pinned_put(h_ring, 2 * sizeof(PcgCtl));
+        pinned_put(h_psync, sizeof(PersistSync));
         for (cudaEvent_t e : ring_ev)
             if (e) cudaEventDestroy(e);
     }
@@ -342,6 +359,33 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         if (const char *e = std::getenv("AMIE_CGCG")) s->cgcg = std::atoi(e) != 0;
         s->grid_fused = resident(sell_fused_kernel(t->s, s->matrix_hint), 0);
         if (const char *e = std::getenv("AMIE_FUSED")) s->fused = std::atoi(e) != 0;
+        {
+            int coop = 0;
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, t->ctx->device);
+            auto one_per_sm = [&](const void *f, int threads) {
+                int k = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, f, threads, 0);
+                return coop && k >= 1 ? t->ctx->num_sms : 0;
+            };
+            if (t->s == 2) {
+                s->grid_persist[0] = one_per_sm((const void *)k_pcg_persist<2, float>, persist_threads<2, float>());
+                s->grid_persist[1] = one_per_sm((const void *)k_pcg_persist<2, double>, persist_threads<2, double>());
+            } else {
+                s->grid_persist[0] = one_per_sm((const void *)k_pcg_persist<3, float>, persist_threads<3, float>());
+                s->grid_persist[1] = one_per_sm((const void *)k_pcg_persist<3, double>, persist_threads<3, double>());
+            }
+            if (const char *e = std::getenv("AMIE_PERSIST")) s->persist_mode = std::atoi(e) != 0 ? 1 : 0;
+            if (const char *e = std::getenv("AMIE_PERSIST_BARRIER_TEST")) s->persist_barrier_test = std::atoi(e) != 0;
+            if (s->grid_persist[0] || s->grid_persist[1]) {
+                AMIE_TRY(ensure_sell_partition(t, t->ctx->num_sms));
+                AMIE_TRY(s->psync.alloc(t->ctx, 1));
+                s->h_psync = (PersistSync *)pinned_get(sizeof(PersistSync));
+                if (!s->h_psync) {
+                    set_error("pinned host allocation failed");
+                    return AMIE_OOM;
+                }
+            }
+        }
         AMIE_CUDA(cudaGetLastError());
         AMIE_TRY(ensure_sell_partition(t, s->grid_cgcg));
         AMIE_TRY(ensure_sell_partition(t, s->grid));
@@ -617,6 +661,55 @@ amie_status read_sum(amie_topo *t, const double *dev, int n, double *out)
     return AMIE_OK;
 }
 
+// The run prepared in the control block as one cooperative launch of
+// k_pcg_persist, when it is switched on and the system allows it (*used); the
+// control block ends as the graph would leave it.
+template <typename T>
+amie_status run_persist(amie_topo *t, SolverState *s, int64_t *iters, double *rr_out, bool *used)
+{
+    *used = false;
+    const int pi = sizeof(T) == 8 ? 1 : 0;
+    const int grid = s->grid_persist[pi];
+    if (s->persist_mode == 0 || !grid) return AMIE_OK;
+    SellView<T> sv = sell_of<T>(t);
+    PcgVecs<T> v = vecs_of<T>(t);
+    auto it = t->sell_cta_first.find(grid);
+    if (!sv.val || !v.p2 || it == t->sell_cta_first.end()) return AMIE_OK;
+    sv.cta_first = it->second.p;
+    cudaStream_t st = t->ctx->stream;
+    AMIE_CUDA(cudaMemsetAsync(s->psync.p, 0, sizeof(PersistSync), st));
+    PcgParts parts = parts_of(s);
+    uint64_t n = t->n;
+    PcgCtl *ctl = s->ctl.p;
+    PersistSync *sync = s->psync.p;
+    uint32_t polls = s->persist_barrier_test ? 4096u : kPersistPolls;
+    uint32_t expect = (uint32_t)grid + (s->persist_barrier_test ? 1u : 0u);
+    void *args[] = {&sv, &v, &n, &parts, &ctl, &sync, &polls, &expect};
+    const void *k = nullptr;
+    int threads = 0;
+    if (t->s == 2) {
+        k = (const void *)k_pcg_persist<2, T>;
+        threads = persist_threads<2, T>();
+    } else {
+        k = (const void *)k_pcg_persist<3, T>;
+        threads = persist_threads<3, T>();
+    }
+    AMIE_CUDA(cudaLaunchCooperativeKernel(k, dim3((unsigned)grid), dim3((unsigned)threads), args, 0, st));
+    AMIE_LAUNCHED();
+    AMIE_CUDA(cudaMemcpyAsync(s->h_ctl, s->ctl.p, sizeof(PcgCtl), cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaMemcpyAsync(s->h_psync, s->psync.p, sizeof(PersistSync), cudaMemcpyDeviceToHost, st));
+    AMIE_CUDA(cudaStreamSynchronize(st));
+    if (s->h_psync->err) {
+        set_error("persistent PCG: a grid barrier was not reached within %u polls (iterations %lld)", polls,
+                  (long long)s->h_ctl->iterations);
+        return AMIE_TIMEOUT;
+    }
+    *used = true;
+    *iters = s->h_ctl->iterations;
+    *rr_out = s->h_ctl->rr;
+    return AMIE_OK;
+}
+
 // Launches the PCG graph until the control block reports done.
 // Graphs of the FP32 runs: two-kernel standard PCG, single-reduction, one-kernel PCG.
 enum class Graph { standard, cgcg, fused };
@@ -625,6 +718,11 @@ template <typename T>
 amie_status drive_pcg(amie_topo *t, SolverState *s, int64_t maxit, int64_t *iters, double *rr_out,
                       Graph kind = Graph::standard)
 {
+    if (kind == Graph::standard) {
+        bool used = false;
+        AMIE_TRY(run_persist<T>(t, s, iters, rr_out, &used));
+        if (used) return AMIE_OK;
+    }
     cudaStream_t st = t->ctx->stream;
     cudaGraphExec_t *g = sizeof(T) == 8 ? &s->graph64 : &s->graph32;
     if (kind == Graph::cgcg) {
