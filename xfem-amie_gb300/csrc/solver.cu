@@ -354,6 +354,28 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         if (const char *e = std::getenv("AMIE_PREFETCH_KB")) s->prefetch_bytes = (uint32_t)std::min(1024, std::max(0, std::atoi(e))) * 1024u;
         s->grid_dir[0] = resident(sell_dir_kernel<float>(t->s, s->matrix_hint), 0);
         s->grid_dir[1] = resident(sell_dir_kernel<double>(t->s, s->matrix_hint), 0);
+        // A small system gets grids sized to its work (at least one CTA per SM,
+        // a multiple of the SM count): a slice per warp of the SpMV kernels, one
+        // two-pack step per thread of the vector kernels, so that fewer CTAs take
+        // tickets and fewer partials are summed (AMIE_WORK_GRID=0: the resident
+        // grids).  44.6 k-DOF P1, mixed: 19.2 instead of 22.6 ms per solve.
+        bool work_grid = true;
+        if (const char *e = std::getenv("AMIE_WORK_GRID")) work_grid = std::atoi(e) != 0;
+        if (work_grid) {
+            const uint64_t sms = (uint64_t)t->ctx->num_sms;
+            auto cap = [&](int g, uint64_t units, uint64_t per_cta) {
+                const uint64_t want = (units + per_cta - 1) / per_cta;
+                const uint64_t sized = std::max<uint64_t>(sms, (want + sms - 1) / sms * sms);
+                return (int)std::min<uint64_t>((uint64_t)g, sized);
+            };
+            const uint64_t slices = std::max<uint64_t>(((uint64_t)t->n_rows + 31) / 32, 1);
+            for (int k = 0; k < 2; k++) {
+                s->grid_sell[k] = cap(s->grid_sell[k], slices, kVecThreads / 32);
+                s->grid_dir[k] = cap(s->grid_dir[k], slices, kVecThreads / 32);
+            }
+            s->grid_vec[0] = cap(s->grid_vec[0], t->n, 2 * kVecThreads * Pack<float>::n);
+            s->grid_vec[1] = cap(s->grid_vec[1], t->n, 2 * kVecThreads * Pack<double>::n);
+        }
         s->grid_cgcg = std::min(resident(sell_cgcg_kernel<false>(t->s, s->matrix_hint), 0),
                                 resident(sell_cgcg_kernel<true>(t->s, s->matrix_hint), 0));
         if (const char *e = std::getenv("AMIE_CGCG")) s->cgcg = std::atoi(e) != 0;
