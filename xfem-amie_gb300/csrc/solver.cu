@@ -358,7 +358,10 @@ amie_status ensure_state(amie_topo *t, bool want32, SolverState **out)
         // a multiple of the SM count): a slice per warp of the SpMV kernels, one
         // two-pack step per thread of the vector kernels, so that fewer CTAs take
         // tickets and fewer partials are summed (AMIE_WORK_GRID=0: the resident
-        // grids).  44.6 k-DOF P1, mixed: 19.2 instead of 22.6 ms per solve.
+        // grids).  40 k-DOF P1, mixed: 18.4 instead of 22.4 ms per solve.  On the
+        // 1.2 M-DOF P2 problem fewer update CTAs than resident cost more in steps
+        // per thread than they save in tickets: 37.3 / 37.8 / 38.7 / 41.5 us per
+        // FP32 iteration with 4 / 3 / 2 / 1 CTAs per SM.
         bool work_grid = true;
         if (const char *e = std::getenv("AMIE_WORK_GRID")) work_grid = std::atoi(e) != 0;
         if (work_grid) {
