@@ -125,7 +125,8 @@ typedef struct amie_solve_opts {
     int32_t nssor;               /* AMIE_CG smoothing sweeps (Assembly::setSSORIterations); default 32 */
     int64_t maxit;               /* iteration cap; <= 0 = reference default n/2 (AMIE_CG) / 20 n (PCG) */
     double inner_rtol;           /* MIXED: FP32 residual reduction between two FP64 residual replacements
-                                    (reliable updates); <= 0 = default 0.1 */
+                                    (reliable updates); <= 0 = 0.1, and 0.3 with the stop at 0.5 rtol
+                                    once an FP32 run takes more than 1,000 iterations */
     int32_t use_x0;              /* 1 = start from x_inout (Assembly::extrapolate warm start) */
 } amie_solve_opts;
 

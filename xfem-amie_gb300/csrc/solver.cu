@@ -942,7 +942,8 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
     cudaStream_t st = t->ctx->stream;
     const double rtol = o && o->rtol > 0 ? o->rtol : 1e-10;
     const int64_t maxit = o && o->maxit > 0 ? o->maxit : std::max<int64_t>(1000, (int64_t)t->n);
-    const double inner_rtol = o && o->inner_rtol > 0 ? o->inner_rtol : 0.1;
+    const bool caller_inner = o && o->inner_rtol > 0;
+    double inner_rtol = caller_inner ? o->inner_rtol : kMixedInner;
     k_norm2_parts<<<s->grid, kVecThreads, 0, st>>>(t->n, t->rhs.p, s->parts.p);
     AMIE_LAUNCHED();
     double bb = 0.0;
@@ -961,7 +962,12 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
     AMIE_TRY(true_residual(t, s, &rr));
     int64_t total = 0;
     double prev_norm = 0.0;   // MIXED: scale of the FP32 run's vectors (0 = no run yet)
-    const double target2 = (rtol * bnorm) * (rtol * bnorm);
+    // the stop, as a fraction of rtol (mixed: kMixedStopLong once the run shows long
+    // segments; AMIE_MIXED_STOP fixes it for measurements)
+    double stop_fraction = 1.0;
+    const char *stop_env = mixed ? std::getenv("AMIE_MIXED_STOP") : nullptr;
+    if (stop_env) stop_fraction = std::min(1.0, std::max(0.01, std::atof(stop_env)));
+    double target2 = (stop_fraction * rtol * bnorm) * (stop_fraction * rtol * bnorm);
     amie_status result = AMIE_NOT_CONVERGED;
     for (int outer = 0; outer < 200; outer++) {
         if (!(rr == rr)) { result = AMIE_NAN; break; }
@@ -998,6 +1004,13 @@ amie_status solve_pcg(amie_topo *t, const amie_solve_opts *o, amie_solve_stats *
             k_accumulate<<<s->grid, kVecThreads, 0, st>>>(t->n, t->d32.p, norm, t->x.p);
             AMIE_LAUNCHED();
             st_out->refinements++;
+            if (it > kMixedLongSegment && !caller_inner && inner_rtol != kMixedInnerLong) {
+                inner_rtol = kMixedInnerLong;   // a long, drift-prone FP32 run: see kMixedLongSegment
+                if (!stop_env) {
+                    stop_fraction = kMixedStopLong;
+                    target2 = (stop_fraction * rtol * bnorm) * (stop_fraction * rtol * bnorm);
+                }
+            }
         }
         total += it;
         AMIE_TRY(true_residual(t, s, &rr));

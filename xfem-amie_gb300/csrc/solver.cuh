@@ -34,10 +34,27 @@ constexpr int kVecThreads = 256;
 // rtol within a quarter more iterations; at rtol = 1e-10 this keeps node
 // displacements within 1e-9 (relative to the largest) of a 1e-13 solve on the
 // 1.2 M-DOF P2 workload (5.8e-10; 4.1e-9 when stopped at 0.5 rtol) for 3.5 %
-// more iterations.  Mixed: the last FP32 segment aims at kMixedLastTarget rtol
-// (displacements within 1e-8 with a margin of two).
+// more iterations.  Mixed: the FP32 recursion is replaced by the true residual
+// after every reduction by kMixedInner, the last FP32 segment aims at
+// kMixedLastTarget rtol and the solve stops once the true residual is below
+// rtol.  A run whose segments take more than kMixedLongSegment iterations
+// drifts in FP32 and is ill-conditioned: it is replaced after every reduction
+// by kMixedInnerLong and stops below kMixedStopLong rtol.  Measured (mixed,
+// rtol 1e-10; iterations, node error vs a 1e-13 solve):
+//   1.2 M-DOF P2   inner 0.1: 19,307, 4.3e-9; 0.3: 16,109, 1.0e-8 (over the
+//                  1e-8 bound); 0.3 with the stop at 0.5 rtol: 16,702, 6.7e-9
+//                  (620 instead of 720 ms)
+//   40 k-DOF P1    inner 0.1: 1,585 in 18.4 ms; 0.3: 1,581 in 19.9 ms (nine
+//                  more replacements, no fewer iterations)
+//   824 k-DOF tets inner 0.1: 1,281 in 63.7 ms; 0.3: 1,281 in 65.5 ms
+// Segments there: ~1,700, ~160 and ~130 iterations.  The serving path keeps
+// its own constants.
 constexpr double kFp64StopFraction = 0.1;
 constexpr double kMixedLastTarget = 0.2;
+constexpr double kMixedInner = 0.1;
+constexpr int64_t kMixedLongSegment = 1000;
+constexpr double kMixedInnerLong = 0.3;
+constexpr double kMixedStopLong = 0.5;
 
 // Programmatic dependent launch: a kernel launched with programmatic stream
 // serialization may start while its predecessor finishes; pdl_wait() blocks
