@@ -47,8 +47,11 @@ constexpr int kVecThreads = 256;
 //   40 k-DOF P1    inner 0.1: 1,585 in 18.4 ms; 0.3: 1,581 in 19.9 ms (nine
 //                  more replacements, no fewer iterations)
 //   824 k-DOF tets inner 0.1: 1,281 in 63.7 ms; 0.3: 1,281 in 65.5 ms
-// Segments there: ~1,700, ~160 and ~130 iterations.  The serving path keeps
-// its own constants.
+// Segments there: ~1,700, ~160 and ~130 iterations.  Switching to 0.5 with the
+// stop at 0.2 rtol instead made the 1.2 M-DOF step 799 ms (21,415 iterations):
+// segments that only halve the residual meet the restart rule of solve_pcg (a
+// true residual that fell by less than half) and lose their directions.  The
+// serving path keeps its own constants.
 constexpr double kFp64StopFraction = 0.1;
 constexpr double kMixedLastTarget = 0.2;
 constexpr double kMixedInner = 0.1;
