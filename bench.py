@@ -471,8 +471,9 @@ def run_ours(args, world, rank, local, dist):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if solver == G.SOLVER_PCG_MIXED else "f64", "data": "synthetic (seeded)",
         "config": {"workload": name, "solver": args.solver, "rtol": args.rtol,
-                   "inner_rtol": args.inner_rtol if args.inner_rtol > 0 else
-                   "0.1; 0.3 with the stop at 0.5 rtol once an FP32 segment exceeds 1,000 iterations",
+                   **({"inner_rtol": args.inner_rtol if args.inner_rtol > 0 else
+                       "0.1; 0.3 with the stop at 0.5 rtol once an FP32 segment exceeds 1,000 iterations"}
+                      if args.solver == "mixed" else {}),
                    "n_dof": int(n),
                    "nnzb": int(topo.nnzb), "block": f"{m.stride}x{m.stride}",
                    "l2": "inputs larger than L2 (matrix + vectors > 129 MB)", "parallelism": f"replicas x{world}",
