@@ -341,7 +341,9 @@ def run_reference(args, world, rank, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": name, "n_dof": int(n), "nnzb": int(len(R["column_index"])), **_cfg_meta(meta)},
+        "config": {"workload": name, "solver": "fp64 (the CPU Jacobi-PCG with Kahan SpMV and dots)", "rtol": args.rtol,
+                   "n_dof": int(n), "nnzb": int(len(R["column_index"])), "block": f"{m.stride}x{m.stride}",
+                   "parallelism": "host cores", **_cfg_meta(meta)},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
                          "sample": f"{samples[0][0]} Jacobi-PCG iterations (Kahan SpMV/dots) per step on the "
                                    f"assembled {n}-DOF matrix, plus the CPU assembly ({t_asm:.2f} s) charged "
