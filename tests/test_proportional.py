@@ -167,3 +167,43 @@ def test_assembly_mirror_proportional(gpu_ctx):
             assert rel(B.getDisplacements(), u_moved) <= 1e-10
     assert abs(u_moved[moved_fixed]) <= 1e-10 * np.abs(u_moved).max()
     assert abs(u_moved[free] - 0.25 * u_moved[free ^ 1]) <= 1e-15 * np.abs(u_moved).max()
+
+
+@pytest.mark.gpu
+def test_device_proportional_3d_several_dofs(gpu_ctx):
+    """3x3 blocks (k_proportional<3>) and multipliers on two DOFs each (the
+    second setPointProportional overload, solvers/assembly.cpp:1699-1761): the
+    device substitution equals the oracle's restatement applied to the device's
+    own Dirichlet-eliminated matrix, and the solution meets every constraint."""
+    import amie_gpu as G
+    d = load_golden("voxel_t4")
+    m = am.from_golden(d, "auto")
+    bc_ids, bc_vals, bc_kinds = am.golden_bcs(d)
+    n = len(d["rhs"])
+    fixed = set(int(i) for i in bc_ids)
+    free_nodes = [k for k in range(n // 3) if all(3 * k + a not in fixed for a in range(3))]
+    nodes = free_nodes[:: max(1, len(free_nodes) // 12)][:12]
+    assert len(nodes) >= 6
+    ids = np.array([3 * k for k in nodes], np.uint32)                          # u_x of the node
+    pids = np.array([[3 * k + 1, 3 * k + 2] for k in nodes], np.uint32).ravel()   # on u_y and u_z
+    ptr = np.arange(0, len(pids) + 1, 2, dtype=np.uint32)
+    coefs = np.tile([0.5, -0.25], len(ids))
+    offs = np.linspace(1e-7, 2e-7, len(ids))
+    t = G.Topology(gpu_ctx, m)
+    try:
+        t.assemble()
+        t.apply_dirichlet(bc_ids, bc_vals, bc_kinds)
+        arr0, rhs0 = t.matrix()
+        rs, ci = t.pattern()
+        t.set_proportional(ids, offs, ptr, pids, coefs)
+        arr1, rhs1 = t.matrix()
+        arr_o, rhs_o = arr0.copy(), rhs0.copy()
+        O.proportional(3, rs, ci, arr_o, rhs_o, ids, offs, ptr, pids, coefs)
+        assert not np.array_equal(arr1, arr0)
+        assert rel(arr1, arr_o) <= 1e-14 and rel(rhs1, rhs_o) <= 1e-14
+        x, st = t.solve(G.SOLVER_PCG_FP64, rtol=1e-12)
+        assert st["relres"] <= 1e-12
+        want = offs + 0.5 * x[pids[0::2]] - 0.25 * x[pids[1::2]]
+        assert np.abs(x[ids] - want).max() <= 1e-14 * np.abs(x).max()
+    finally:
+        t.close()
