@@ -50,8 +50,10 @@ constexpr int kVecThreads = 256;
 // Segments there: ~1,700, ~160 and ~130 iterations.  Switching to 0.5 with the
 // stop at 0.2 rtol instead made the 1.2 M-DOF step 799 ms (21,415 iterations):
 // segments that only halve the residual meet the restart rule of solve_pcg (a
-// true residual that fell by less than half) and lose their directions.  The
-// serving path keeps its own constants.
+// true residual that fell by less than half) and lose their directions; with
+// that rule scaled to the segment's target (restart below a fall of 2x the
+// target) it was 625 ms (16,683 iterations, stop at 0.3 rtol).  The serving
+// path keeps its own constants.
 constexpr double kFp64StopFraction = 0.1;
 constexpr double kMixedLastTarget = 0.2;
 constexpr double kMixedInner = 0.1;
