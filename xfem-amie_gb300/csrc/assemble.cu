@@ -610,6 +610,49 @@ __global__ void k_sell_fill(uint32_t n_rows, uint32_t n_slices, const uint32_t *
     }
 }
 
+// SELL-32-sigma order on the device: one CTA per window of `sigma` rows (blockDim
+// >= sigma) places every row of the window at its rank in a stable sort by
+// descending length (rows with more blocks first, equal lengths in row order),
+// the order std::stable_sort gives; perm entries past n_rows keep the padding
+// value n_rows (set before).
+__global__ void k_sell_perm(uint32_t n_rows, uint32_t sigma, const uint32_t *row_ptr, uint32_t *perm)
+{
+    extern __shared__ uint32_t win_len[];
+    const uint32_t w0 = blockIdx.x * sigma;
+    const uint32_t cnt = min(sigma, n_rows - w0);
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) win_len[i] = row_ptr[w0 + i + 1] - row_ptr[w0 + i];
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const uint32_t li = win_len[i];
+        uint32_t rank = 0;
+        for (uint32_t q = 0; q < cnt; q++) {
+            const uint32_t lq = win_len[q];
+            rank += (lq > li || (lq == li && q < i)) ? 1u : 0u;
+        }
+        perm[w0 + rank] = w0 + i;
+    }
+}
+
+// Slots of every slice: 32 x the longest row among its lanes.
+__global__ void k_sell_slots(uint32_t n_rows, uint32_t n_slices, const uint32_t *perm, const uint32_t *row_ptr,
+                             uint64_t *slots)
+{
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    if (warp >= n_slices) return;
+    const uint32_t r = perm[warp * 32 + lane];
+    uint32_t len = r < n_rows ? row_ptr[r + 1] - row_ptr[r] : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+    if (lane == 0) slots[warp] = 32ull * len;
+}
+
+__global__ void k_fill_u32(uint64_t n, uint32_t v, uint32_t *out)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = v;
+}
+
 // Copy of the BSR values (row-major s x s blocks) into the chunked SELL layout.
 template <int S, typename T>
 __global__ void k_to_sell(uint64_t n_slots, const uint32_t *sell_blk, const double *val, T *out)
@@ -1022,21 +1065,62 @@ extern "C" amie_status amie_topology_build(amie_ctx *ctx, const amie_mesh *mesh,
         if (v >= 0 && v <= 7) t->sell_variant = v;
     }
 
-    // SELL-32-sigma structure: rows sorted by length inside windows, slices of 32
-    {
+    // SELL-32-sigma structure: rows sorted by length inside windows, slices of 32.
+    // Built on the device (k_sell_perm, k_sell_slots, a scan); the host build below
+    // is kept for windows wider than 1024 rows and for AMIE_SELL_HOST=1 (tests
+    // compare the two)
+    t->n_slices = (t->n_rows + 31) / 32;
+    // window of the length sort; tuning override for measurements: AMIE_SELL_SIGMA
+    // (a multiple of 32; 32 keeps every slice on 32 consecutive rows)
+    uint32_t sigma = kSellSigma;
+    if (const char *e = std::getenv("AMIE_SELL_SIGMA")) {
+        const long v = std::atol(e);
+        if (v >= 32 && v <= (1l << 24) && v % 32 == 0) sigma = (uint32_t)v;
+    }
+    bool sell_host = sigma > 1024;
+    if (const char *e = std::getenv("AMIE_SELL_HOST")) sell_host = sell_host || std::atoi(e) != 0;
+    if (!sell_host) {
+        const uint64_t n_perm = (uint64_t)t->n_slices * 32;
+        DevArray<uint64_t> slots;
+        if ((rc = t->sell_perm.alloc(ctx, n_perm)) || (rc = t->sell_ptr.alloc(ctx, (size_t)t->n_slices + 1)) ||
+            (rc = slots.alloc(ctx, (size_t)t->n_slices + 1)))
+            return fail(rc);
+        k_fill_u32<<<blocks_for(n_perm, 256), 256, 0, st>>>(n_perm, t->n_rows, t->sell_perm.p);
+        const uint32_t n_win = (t->n_rows + sigma - 1) / sigma;
+        k_sell_perm<<<n_win, std::min<uint32_t>(sigma, 1024), sigma * 4, st>>>(t->n_rows, sigma, t->row_ptr.p,
+                                                                             t->sell_perm.p);
+        k_sell_slots<<<blocks_for((uint64_t)t->n_slices * 32, 256), 256, 0, st>>>(t->n_rows, t->n_slices,
+                                                                                 t->sell_perm.p, t->row_ptr.p,
+                                                                                 slots.p);
+        g_launches += 3;
+        AMIE_CUDA(cudaMemsetAsync(slots.p + t->n_slices, 0, 8, st));
+        size_t sb = 0;
+        AMIE_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, sb, slots.p, t->sell_ptr.p, (int64_t)t->n_slices + 1, st));
+        tb = temp.n;
+        if (sb > tb) {
+            temp.release();
+            if ((rc = temp.alloc(ctx, sb))) return fail(rc);
+            tb = temp.n;
+        }
+        AMIE_CUDA(cub::DeviceScan::ExclusiveSum(temp.p, tb, slots.p, t->sell_ptr.p, (int64_t)t->n_slices + 1, st));
+        t->h_sell_ptr.resize((size_t)t->n_slices + 1);
+        AMIE_CUDA(cudaMemcpyAsync(t->h_sell_ptr.data(), t->sell_ptr.p, ((size_t)t->n_slices + 1) * 8,
+                                  cudaMemcpyDeviceToHost, st));
+        AMIE_CUDA(cudaStreamSynchronize(st));   // slots and temp are released at the end of this scope
+        t->n_slots = t->h_sell_ptr[t->n_slices];
+        if ((rc = t->sell_blk.alloc(ctx, t->n_slots)) || (rc = t->sell_col.alloc(ctx, t->n_slots)) ||
+            (rc = t->sell_dot.alloc(ctx, t->n_slices)))
+            return fail(rc);
+        k_sell_fill<<<t->ctx->num_sms * 8, 256, 0, st>>>(t->n_rows, t->n_slices, t->sell_perm.p, t->sell_ptr.p,
+                                                         t->row_ptr.p, t->col.p, t->sell_blk.p, t->sell_col.p);
+        g_launches += 1;
+        AMIE_CUDA(cudaGetLastError());
+    } else {
         std::vector<uint32_t> h_rp(t->n_rows + 1);
         AMIE_CUDA(cudaMemcpyAsync(h_rp.data(), t->row_ptr.p, h_rp.size() * 4, cudaMemcpyDeviceToHost, st));
         AMIE_CUDA(cudaStreamSynchronize(st));
-        t->n_slices = (t->n_rows + 31) / 32;
         std::vector<uint32_t> perm((size_t)t->n_slices * 32, t->n_rows);
         std::vector<uint64_t> sptr(t->n_slices + 1, 0);
-        // window of the length sort; tuning override for measurements: AMIE_SELL_SIGMA
-        // (a multiple of 32; 32 keeps every slice on 32 consecutive rows)
-        uint32_t sigma = kSellSigma;
-        if (const char *e = std::getenv("AMIE_SELL_SIGMA")) {
-            const long v = std::atol(e);
-            if (v >= 32 && v <= (1l << 24) && v % 32 == 0) sigma = (uint32_t)v;
-        }
         for (uint32_t w0 = 0; w0 < t->n_rows; w0 += sigma) {
             const uint32_t w1 = std::min<uint32_t>(t->n_rows, w0 + sigma);
             for (uint32_t r = w0; r < w1; r++) perm[r] = r;
