@@ -1,7 +1,9 @@
 """PCG runs as one cooperative launch (k_pcg_persist, xfem-amie_gb300/csrc/persist.cuh)
 against the graphs of kernels: the same solutions and about the same number of
-iterations, in 2D and 3D, mixed and FP64; and a grid barrier that gives up ends
-the launch with AMIE_TIMEOUT, after which the context still solves."""
+iterations, in 2D and 3D (the FP32 runs of the mixed solver, whose graphs fold
+the direction update; FP64 runs keep their graphs); and a grid barrier that
+gives up ends the launch with AMIE_TIMEOUT, after which the context still
+solves."""
 import numpy as np
 import pytest
 
@@ -31,7 +33,7 @@ def _solve(ctx, d, solver, rtol, monkeypatch, persist, unreachable=False):
 
 
 @pytest.mark.parametrize("name", ["incl_p1", "incl_p2", "crack_p2", "voxel_t4"])
-@pytest.mark.parametrize("solver", ["mixed", "fp64"])
+@pytest.mark.parametrize("solver", ["mixed"])
 def test_persistent_matches_graph(gpu_ctx, monkeypatch, name, solver):
     import amie_gpu as G
     d = load_golden(name)

@@ -121,7 +121,8 @@ struct SolverState {
     DevArray<double> slice5;
     cudaGraphExec_t graph_fused = nullptr;
     // Runs of the standard PCG as one cooperative launch (k_pcg_persist) instead
-    // of graphs of kernels; opt-in (AMIE_PERSIST=1).  Measured against the graphs
+    // of graphs of kernels (FP32 runs, whose graphs fold the direction update);
+    // opt-in (AMIE_PERSIST=1).  Measured against the graphs
     // (mixed, rtol 1e-10): 44.6 k-DOF P1 23.4 vs 22.6 ms (25.2 ms with an
     // atomicAdd arrival and a sleeping poll), the 250 k-DOF notched beam's
     // 60-step damage loop 35.0 vs 32.0 s, 824 k-DOF voxel tetrahedra 73.1 vs
@@ -695,7 +696,9 @@ amie_status run_persist(amie_topo *t, SolverState *s, int64_t *iters, double *rr
     *used = false;
     const int pi = sizeof(T) == 8 ? 1 : 0;
     const int grid = s->grid_persist[pi];
-    if (s->persist_mode == 0 || !grid) return AMIE_OK;
+    // only runs whose graph folds the direction update (FP32): the others form p in
+    // k_direction, on one buffer, and resume_pcg relies on that
+    if (s->persist_mode == 0 || !grid || !fold<T>(s)) return AMIE_OK;
     SellView<T> sv = sell_of<T>(t);
     PcgVecs<T> v = vecs_of<T>(t);
     auto it = t->sell_cta_first.find(grid);
